@@ -1,0 +1,838 @@
+// dfpt_api.cu - the C-ABI: scene validation and upload, pass scheduling (CUDA graphs), readback.
+//
+// One handle = one compiled scene resident in HBM + one film. dfpt_render replays a captured CUDA
+// graph per pass: camera -> [trace closest -> shade -> shadow rays] x depth -> final any-hit ->
+// film, the wavefront form of GPURendererKernel.run (GPURendererKernel.java:252-308).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dfpt.h"
+#include "dfpt_internal.h"
+#include "dfpt_launch.h"
+#include "dfpt_noise_tables.h"
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int dfpt_fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (expr);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            (void)cudaGetLastError();                                                           \
+            return dfpt_fail(e_ == cudaErrorMemoryAllocation ? DFPT_ERR_OUT_OF_MEMORY : DFPT_ERR_CUDA, \
+                             "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                       \
+    } while (0)
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        n = count;
+        return cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Validation of the compiled scene: every offset the kernels will follow is checked here so no
+// device access can leave its array.
+
+struct HostScene {
+    std::vector<float> point2fs, point3fs, vector3fs, spheres, terrains, textures, surfaces, o2w, w2o, camera;
+    std::vector<int> planes, triangles, bvh, primitives;
+};
+
+bool in_range(int64_t off, int64_t len, int64_t count) { return off >= 0 && len >= 0 && off + len <= count; }
+
+int check_triangle(const HostScene& s, int off) {
+    if (!in_range(off, 12, (int64_t)s.triangles.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "triangle offset %d out of range", off);
+    for (int k = 0; k < 3; ++k) {
+        if (!in_range(s.triangles[off + k], 3, (int64_t)s.point3fs.size()))
+            return dfpt_fail(DFPT_ERR_INVALID_SCENE, "triangle %d position offset out of range", off);
+        if (!in_range(s.triangles[off + 3 + k], 3, (int64_t)s.vector3fs.size()) || !in_range(s.triangles[off + 9 + k], 3, (int64_t)s.vector3fs.size()))
+            return dfpt_fail(DFPT_ERR_INVALID_SCENE, "triangle %d normal/tangent offset out of range", off);
+        if (!in_range(s.triangles[off + 6 + k], 2, (int64_t)s.point2fs.size()))
+            return dfpt_fail(DFPT_ERR_INVALID_SCENE, "triangle %d texture coordinate offset out of range", off);
+    }
+    return DFPT_OK;
+}
+
+int texture_min_size(int type) {
+    switch (type) {
+        case DFPT_TEXTURE_BLEND: return 5;
+        case DFPT_TEXTURE_BULLSEYE: return 4;
+        case DFPT_TEXTURE_CHECKERBOARD: return 8;
+        case DFPT_TEXTURE_CONSTANT: return 3;
+        case DFPT_TEXTURE_FBM: return 7;
+        case DFPT_TEXTURE_IMAGE: return 8;
+        case DFPT_TEXTURE_SURFACE_NORMAL: return 3;
+        case DFPT_TEXTURE_UV: return 2;
+        default: return -1;
+    }
+}
+
+int check_texture(const HostScene& s, int to, bool allow_blend) {
+    const int64_t n = (int64_t)s.textures.size();
+    if (!in_range(to, 1, n)) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "texture offset %d out of range", to);
+    const int type = (int)s.textures[to];
+    const int need = texture_min_size(type);
+    if (need < 0) {
+        // Unknown types evaluate to black in the reference (GRK:1615-1617); only the type is read.
+        return DFPT_OK;
+    }
+    if (!in_range(to, need, n)) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "texture record at %d truncated", to);
+    if (type == DFPT_TEXTURE_IMAGE) {
+        const float w = s.textures[to + 4], h = s.textures[to + 5];
+        if (!(w >= 1.0f && h >= 1.0f && w * h < 1.0e9f)) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "image texture at %d has bad size", to);
+        if (!in_range(to, 8 + (int64_t)((int)(w * h)), n)) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "image texture at %d truncated", to);
+    }
+    if (type == DFPT_TEXTURE_BLEND) {
+        if (!allow_blend) return DFPT_OK;  // nested blends evaluate to black; never followed
+        for (int k = 2; k <= 3; ++k) {
+            int r = check_texture(s, (int)s.textures[to + k], false);
+            if (r) return r;
+        }
+    }
+    return DFPT_OK;
+}
+
+int check_surface(const HostScene& s, int so) {
+    if (!in_range(so, 6, (int64_t)s.surfaces.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "surface offset %d out of range", so);
+    for (int k = 1; k <= 3; ++k) {
+        int r = check_texture(s, (int)s.surfaces[so + k], true);
+        if (r) return r;
+    }
+    return DFPT_OK;
+}
+
+struct Derived {
+    std::vector<int4> prim_info;
+    std::vector<float4> nodes, tris, sphere4, plane_a, plane_n;
+};
+
+float int_bits(int i) {
+    float f;
+    std::memcpy(&f, &i, 4);
+    return f;
+}
+
+int add_tri_record(const HostScene& s, Derived& d, int off, bool last) {
+    const float* P = s.point3fs.data();
+    const int a = s.triangles[off], b = s.triangles[off + 1], c = s.triangles[off + 2];
+    d.tris.push_back(make_float4(P[a], P[a + 1], P[a + 2], int_bits(off)));
+    d.tris.push_back(make_float4(P[b] - P[a], P[b + 1] - P[a + 1], P[b + 2] - P[a + 2], int_bits(last ? 1 : 0)));
+    d.tris.push_back(make_float4(P[c] - P[a], P[c + 1] - P[a + 1], P[c + 2] - P[a + 2], 0.0f));
+    return (int)(d.tris.size() / 3) - 1;
+}
+
+// Converts one flattened BVH (SceneCompiler.java:888-995) rooted at `root` to node records.
+int convert_bvh(const HostScene& s, Derived& d, int root, int& first_node) {
+    const int64_t nb = (int64_t)s.bvh.size();
+    std::vector<int> offs;       // relative offsets in preorder
+    int pending = 1, rel = 0;
+    while (pending > 0) {
+        const int at = root + rel;
+        if (!in_range(at, 5, nb)) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "BVH node at %d out of range", at);
+        offs.push_back(rel);
+        if (offs.size() > (size_t)nb) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "BVH at %d is not a tree", root);
+        const int type = s.bvh[at];
+        if (type == 1) {
+            pending += 1;
+            rel += 5;
+        } else if (type == 2) {
+            const int cnt = s.bvh[at + 4];
+            if (cnt < 0 || !in_range(at, 5 + (int64_t)cnt, nb)) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "BVH leaf at %d truncated", at);
+            pending -= 1;
+            rel += 5 + cnt;
+        } else {
+            return dfpt_fail(DFPT_ERR_INVALID_SCENE, "BVH node at %d has type %d", at, type);
+        }
+    }
+    std::vector<int> index_of_rel(rel + 1, -1);
+    for (size_t i = 0; i < offs.size(); ++i) index_of_rel[offs[i]] = (int)i;
+    first_node = (int)(d.nodes.size() / 2);
+    for (size_t i = 0; i < offs.size(); ++i) {
+        const int at = root + offs[i];
+        const int type = s.bvh[at], next = s.bvh[at + 1], mn = s.bvh[at + 2], mx = s.bvh[at + 3];
+        int next_index = -1;
+        if (next != -1) {
+            if (next <= offs[i] || next >= (int)index_of_rel.size() || index_of_rel[next] < 0)
+                return dfpt_fail(DFPT_ERR_INVALID_SCENE, "BVH node at %d has a bad next pointer %d", at, next);
+            next_index = first_node + index_of_rel[next];
+        }
+        if (!in_range(mn, 3, (int64_t)s.point3fs.size()) || !in_range(mx, 3, (int64_t)s.point3fs.size()))
+            return dfpt_fail(DFPT_ERR_INVALID_SCENE, "BVH node at %d has bounds out of range", at);
+        int leaf = -1;
+        if (type == 1) {
+            if (s.bvh[at + 4] != offs[i] + 5) return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "BVH node at %d: left child is not the next node", at);
+        } else {
+            const int cnt = s.bvh[at + 4];
+            if (cnt == 0) {
+                leaf = -2;
+            } else {
+                for (int k = 0; k < cnt; ++k) {
+                    const int toff = s.bvh[at + 5 + k];
+                    int r = check_triangle(s, toff);
+                    if (r) return r;
+                    const int rec = add_tri_record(s, d, toff, k == cnt - 1);
+                    if (k == 0) leaf = rec;
+                }
+            }
+        }
+        const float* P = s.point3fs.data();
+        d.nodes.push_back(make_float4(P[mn], P[mn + 1], P[mn + 2], int_bits(next_index)));
+        d.nodes.push_back(make_float4(P[mx], P[mx + 1], P[mx + 2], int_bits(leaf)));
+    }
+    return DFPT_OK;
+}
+
+int build_derived(const HostScene& s, Derived& d) {
+    const int np = (int)(s.primitives.size() / 3);
+    std::vector<std::pair<int, int>> bvh_roots;  // root offset -> first node
+    for (int i = 0; i < np; ++i) {
+        const int type = s.primitives[3 * i], off = s.primitives[3 * i + 1], so = s.primitives[3 * i + 2];
+        int r = check_surface(s, so);
+        if (r) return r;
+        int rec = 0;
+        if (type == DFPT_SHAPE_PLANE) {
+            if (!in_range(off, 4, (int64_t)s.planes.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "plane offset %d out of range", off);
+            for (int k = 0; k < 3; ++k)
+                if (!in_range(s.planes[off + k], 3, (int64_t)s.point3fs.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "plane %d point out of range", off);
+            if (!in_range(s.planes[off + 3], 3, (int64_t)s.vector3fs.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "plane %d normal out of range", off);
+            const float* A = s.point3fs.data() + s.planes[off];
+            const float* N = s.vector3fs.data() + s.planes[off + 3];
+            rec = (int)d.plane_a.size();
+            d.plane_a.push_back(make_float4(A[0], A[1], A[2], 0.0f));
+            d.plane_n.push_back(make_float4(N[0], N[1], N[2], 0.0f));
+        } else if (type == DFPT_SHAPE_SPHERE) {
+            if (!in_range(off, 2, (int64_t)s.spheres.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "sphere offset %d out of range", off);
+            const int po = (int)s.spheres[off];
+            if (!in_range(po, 3, (int64_t)s.point3fs.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "sphere %d position out of range", off);
+            rec = (int)d.sphere4.size();
+            d.sphere4.push_back(make_float4(s.point3fs[po], s.point3fs[po + 1], s.point3fs[po + 2], s.spheres[off + 1]));
+        } else if (type == DFPT_SHAPE_TERRAIN) {
+            if (!in_range(off, 5, (int64_t)s.terrains.size())) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "terrain offset %d out of range", off);
+        } else if (type == DFPT_SHAPE_TRIANGLE) {
+            int r2 = check_triangle(s, off);
+            if (r2) return r2;
+            rec = add_tri_record(s, d, off, true);
+        } else if (type == DFPT_SHAPE_TRIANGLE_MESH) {
+            rec = -1;
+            for (auto& pr : bvh_roots)
+                if (pr.first == off) rec = pr.second;
+            if (rec < 0) {
+                int first = 0;
+                int r2 = convert_bvh(s, d, off, first);
+                if (r2) return r2;
+                bvh_roots.emplace_back(off, first);
+                rec = first;
+            }
+        } else {
+            // Unknown shape types never intersect (GRK:1195-1243 has no branch for them).
+            rec = 0;
+        }
+        d.prim_info.push_back(make_int4(type, off, so, rec));
+    }
+    if (d.nodes.empty()) { d.nodes.push_back(make_float4(0, 0, 0, 0)); d.nodes.push_back(make_float4(0, 0, 0, 0)); }
+    if (d.tris.empty()) for (int k = 0; k < 3; ++k) d.tris.push_back(make_float4(0, 0, 0, 0));
+    if (d.sphere4.empty()) d.sphere4.push_back(make_float4(0, 0, 0, 0));
+    if (d.plane_a.empty()) { d.plane_a.push_back(make_float4(0, 0, 0, 0)); d.plane_n.push_back(make_float4(0, 0, 0, 0)); }
+    if (d.prim_info.empty()) d.prim_info.push_back(make_int4(0, 0, 0, 0));
+    return DFPT_OK;
+}
+
+template <typename T>
+void copy_array(std::vector<T>& dst, const T* src, int64_t n) {
+    dst.assign(src, src + n);
+    if (dst.empty()) dst.push_back(T());
+}
+
+uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+float powf_j(float a, float b) { return (float)std::pow((double)a, (double)b); }
+
+}  // namespace
+
+struct dfpt_handle {
+    HostScene host;
+    int width = 0, height = 0, n_pixels = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sms = 0;
+    KernelSet fast{}, strict{};
+    bool use_strict = false;
+    // Scene on the device.
+    DevBuf<float> point2fs, point3fs, vector3fs, spheres, terrains, textures, surfaces, o2w, w2o, camera;
+    DevBuf<int> planes, triangles, primitives;
+    DevBuf<int4> prim_info;
+    DevBuf<float4> nodes, tris, sphere4, plane_a, plane_n;
+    DevScene scene{};
+    // Parameters.
+    dfpt_params params{};
+    dfpt_sky sky{};
+    DevParams dev_params_host{};
+    DevBuf<DevParams> dev_params;
+    // Pass buffers.
+    DevBuf<float4> q_o0, q_o1, q_d0, q_d1, s_o, s_d, s_c, throughput, radiance, primary_o, primary_d, film_sum, film_comp;
+    DevBuf<int4> q_hit;
+    DevBuf<uint64_t> rng;
+    DevBuf<int> pixel_flags, counts, pass_index, film_n, primitive_offsets, hit_prim, hit_type, hit_off;
+    DevBuf<float> hit_dist, hit_normal, scratch_rgb;
+    DevBuf<uint8_t> bgra;
+    DevBuf<unsigned long long> stats;
+    DevBuf<double> mean;
+    DevPass pass{};
+    LaunchCtx ctx{};
+    int host_pass = 0;  // passes issued so far (mirrors the device pass counter)
+    int clear_pass = 0;
+    bool counting = false;
+    bool record_hits = false;
+    // Graph of one pass.
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_valid = false;
+    int graph_kernels = 0;
+    bool use_graph = true;
+    uint64_t launches = 0;
+};
+
+namespace {
+
+void release(dfpt_handle* h) {
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = nullptr;
+    DevBuf<float>* fb[] = {&h->point2fs, &h->point3fs, &h->vector3fs, &h->spheres, &h->terrains, &h->textures, &h->surfaces, &h->o2w, &h->w2o, &h->camera, &h->hit_dist, &h->hit_normal, &h->scratch_rgb};
+    for (auto* b : fb) b->release();
+    DevBuf<int>* ib[] = {&h->planes, &h->triangles, &h->primitives, &h->pixel_flags, &h->counts, &h->pass_index, &h->film_n, &h->primitive_offsets, &h->hit_prim, &h->hit_type, &h->hit_off};
+    for (auto* b : ib) b->release();
+    DevBuf<float4>* f4[] = {&h->nodes, &h->tris, &h->sphere4, &h->plane_a, &h->plane_n, &h->q_o0, &h->q_o1, &h->q_d0, &h->q_d1, &h->s_o, &h->s_d, &h->s_c, &h->throughput, &h->radiance, &h->primary_o, &h->primary_d, &h->film_sum, &h->film_comp};
+    for (auto* b : f4) b->release();
+    h->prim_info.release();
+    h->rng.release();
+    h->bgra.release();
+    h->stats.release();
+    h->mean.release();
+    h->dev_params.release();
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    h->stream = nullptr;
+}
+
+template <typename T>
+cudaError_t upload(DevBuf<T>& b, const std::vector<T>& v, cudaStream_t s) {
+    if (!b.p || b.n != v.size()) {
+        b.release();
+        cudaError_t e = b.alloc(v.size());
+        if (e != cudaSuccess) return e;
+    }
+    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+void fill_dev_params(dfpt_handle* h) {
+    DevParams& d = h->dev_params_host;
+    const dfpt_params& p = h->params;
+    const dfpt_sky& k = h->sky;
+    std::memset(&d, 0, sizeof(d));
+    d.renderer_type = p.renderer_type;
+    d.tone_mapper_type = p.tone_mapper_type;
+    d.shader_type = p.shader_type;
+    d.normal_mapping = p.normal_mapping;
+    d.wireframes = p.wireframes;
+    d.depth_max = p.pt_ray_depth_maximum;
+    d.depth_rr = p.pt_ray_depth_russian_roulette;
+    d.exposure = p.tone_mapper_exposure;
+    d.ao_max_distance = p.ao_maximum_distance;
+    d.g_amplitude = p.global_amplitude;
+    d.g_frequency = p.global_frequency;
+    d.g_gain = p.global_gain;
+    d.g_lacunarity = p.global_lacunarity;
+    d.g_octaves = p.global_octaves;
+    d.selected_primitive_offset = p.selected_primitive_offset;
+    d.rng_kind = p.rng_kind;
+    d.seed_lo = (uint32_t)p.seed;
+    d.seed_hi = (uint32_t)(p.seed >> 32);
+    d.width = h->width;
+    d.height = h->height;
+    d.record_hits = h->record_hits ? 1 : 0;
+    d.counting = h->counting ? 1 : 0;
+    d.clear_pass = h->clear_pass;
+    for (int i = 0; i < 3; ++i) {
+        d.sky_u[i] = k.orthonormal_basis_u[i];
+        d.sky_v[i] = k.orthonormal_basis_v[i];
+        d.sky_w[i] = k.orthonormal_basis_w[i];
+        d.sun_dir[i] = k.sun_direction[i];
+        d.sun_dir_world[i] = k.sun_direction_world[i];
+        d.sun_origin[i] = k.sun_origin[i];
+    }
+    d.theta = k.theta;
+    d.sky_active = k.is_sky_active;
+    d.sun_active = k.is_sun_active;
+    for (int i = 0; i < 5; ++i) {
+        d.perez_l[i] = (float)k.perez_relative_luminance[i];
+        d.perez_x[i] = (float)k.perez_x[i];
+        d.perez_y[i] = (float)k.perez_y[i];
+    }
+    d.zenith_l = (float)k.zenith_relative_luminance;
+    d.zenith_x = (float)k.zenith_x;
+    d.zenith_y = (float)k.zenith_y;
+    const double t0 = (double)k.theta, c0 = std::cos(t0);
+    const double* L = k.perez_relative_luminance;
+    d.den_l = (float)((1.0 + L[0] * std::exp(L[1])) * (1.0 + L[2] * std::exp(L[3] * t0) + L[4] * c0 * c0));
+    d.den_x_a = (float)(1.0 + k.perez_x[0] * std::exp(k.perez_x[1]));
+    d.den_y_a = (float)(1.0 + k.perez_y[0] * std::exp(k.perez_y[1]));
+    d.cos_theta0 = (float)c0;
+    // RGBColorSpace.SRGB (breakPoint 0.00304, gamma 2.4) derived constants, float arithmetic.
+    const float bp = 0.00304f, g = 2.4f;
+    const float pe = powf_j(bp, 1.0f / g - 1.0f);
+    d.cs_break = bp;
+    d.cs_gamma = g;
+    d.cs_slope = 1.0f / (g / pe - g * bp + bp);
+    d.cs_slope_match = g * d.cs_slope / pe;
+    d.cs_segment = d.cs_slope_match * powf_j(bp, 1.0f / g) - d.cs_slope * bp;
+}
+
+int push_params(dfpt_handle* h) {
+    fill_dev_params(h);
+    CUDA_TRY(cudaMemcpyAsync(h->dev_params.p, &h->dev_params_host, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
+    return DFPT_OK;
+}
+
+int reset_rng(dfpt_handle* h) {
+    std::vector<uint64_t> seeds((size_t)h->n_pixels);
+    for (int i = 0; i < h->n_pixels; ++i) seeds[i] = splitmix64(h->params.seed + (uint64_t)i);
+    CUDA_TRY(cudaMemcpyAsync(h->rng.p, seeds.data(), seeds.size() * 8, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+const KernelSet& kset(dfpt_handle* h) { return h->use_strict ? h->strict : h->fast; }
+
+bool is_simple_mode(int rt) {
+    return rt == DFPT_RENDERER_AMBIENT_OCCLUSION || rt == DFPT_RENDERER_RAY_CASTER || rt == DFPT_RENDERER_RAY_MARCHER ||
+           rt == DFPT_RENDERER_RAY_TRACER || rt == DFPT_RENDERER_SURFACE_NORMALS;
+}
+
+// Issues one pass on the handle's stream; returns the number of kernels launched.
+int issue_pass(dfpt_handle* h) {
+    const KernelSet& K = kset(h);
+    const LaunchCtx& c = h->ctx;
+    int k = 0;
+    cudaMemsetAsync(h->counts.p, 0, 64 * sizeof(int), h->stream);
+    if (is_simple_mode(h->params.renderer_type)) {
+        K.simple(c); ++k;
+    } else {
+        const int nb = h->params.pt_ray_depth_maximum < 1 ? 1 : (h->params.pt_ray_depth_maximum > DFPT_MAX_DEPTH ? DFPT_MAX_DEPTH : h->params.pt_ray_depth_maximum);
+        K.camera(c); ++k;
+        for (int b = 0; b < nb; ++b) {
+            K.trace_closest(c, b); ++k;
+            K.shade(c, b); ++k;
+            if (h->sky.is_sun_active == 1) { K.shadow(c, b); ++k; }
+        }
+        K.final_(c, nb); ++k;
+    }
+    if (h->params.wireframes == 1) { K.wireframe(c); ++k; }
+    K.film(c); ++k;
+    K.end_pass(c); ++k;
+    return k;
+}
+
+int build_graph(dfpt_handle* h) {
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = nullptr;
+    h->graph_valid = false;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int k = issue_pass(h);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return dfpt_fail(DFPT_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    }
+    e = cudaGraphInstantiate(&h->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        h->graph_exec = nullptr;
+        return dfpt_fail(DFPT_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    }
+    h->graph_kernels = k;
+    h->graph_valid = true;
+    return DFPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dfpt_last_error(void) { return g_last_error.c_str(); }
+
+int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, int32_t height, dfpt_handle** out) {
+    if (!sd || !sky || !out) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (width <= 0 || height <= 0 || (int64_t)width * (int64_t)height > (1ll << 28))
+        return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "resolution %d x %d is not supported", width, height);
+    if (sd->camera_count < 19 || !sd->camera) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "camera needs 19 floats");
+    if (sd->primitives_count % 3 != 0) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "primitives count %lld is not a multiple of 3", (long long)sd->primitives_count);
+    const int64_t np = sd->primitives_count / 3;
+    if (sd->primitives_object_to_world_count < np * 16 || sd->primitives_world_to_object_count < np * 16)
+        return dfpt_fail(DFPT_ERR_INVALID_SCENE, "primitive matrices need 16 floats per primitive");
+    auto h = new dfpt_handle();
+    HostScene& s = h->host;
+    copy_array(s.point2fs, sd->point2fs, sd->point2fs_count);
+    copy_array(s.point3fs, sd->point3fs, sd->point3fs_count);
+    copy_array(s.vector3fs, sd->vector3fs, sd->vector3fs_count);
+    copy_array(s.planes, sd->planes, sd->planes_count);
+    copy_array(s.spheres, sd->spheres, sd->spheres_count);
+    copy_array(s.terrains, sd->terrains, sd->terrains_count);
+    copy_array(s.triangles, sd->triangles, sd->triangles_count);
+    copy_array(s.bvh, sd->bounding_volume_hierarchies, sd->bounding_volume_hierarchies_count);
+    copy_array(s.textures, sd->textures, sd->textures_count);
+    copy_array(s.surfaces, sd->surfaces, sd->surfaces_count);
+    s.primitives.assign(sd->primitives, sd->primitives + sd->primitives_count);
+    s.o2w.assign(sd->primitives_object_to_world, sd->primitives_object_to_world + np * 16);
+    s.w2o.assign(sd->primitives_world_to_object, sd->primitives_world_to_object + np * 16);
+    if (s.o2w.empty()) { s.o2w.assign(16, 0.0f); s.w2o.assign(16, 0.0f); }
+    s.camera.assign(sd->camera, sd->camera + 19);
+    Derived d;
+    int r = build_derived(s, d);
+    if (r) { delete h; return r; }
+    if (d.nodes.size() / 2 > (size_t)INT32_MAX / 4 || d.tris.size() / 3 > (size_t)INT32_MAX / 4) { delete h; return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "scene too large"); }
+
+    h->width = width;
+    h->height = height;
+    h->n_pixels = width * height;
+    h->fast = dfpt_fast::kernel_set();
+    h->strict = dfpt_strict::kernel_set();
+    h->sky = *sky;
+    dfpt_params_default(&h->params);
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) { (void)cudaGetLastError(); delete h; return dfpt_fail(DFPT_ERR_CUDA, "CUDA device unavailable: %s", cudaGetErrorString(ce)); }
+    h->own_stream = true;
+
+#define TRY_R(expr) do { cudaError_t e_ = (expr); if (e_ != cudaSuccess) { (void)cudaGetLastError(); int code = e_ == cudaErrorMemoryAllocation ? DFPT_ERR_OUT_OF_MEMORY : DFPT_ERR_CUDA; dfpt_fail(code, "%s: %s", #expr, cudaGetErrorString(e_)); release(h); delete h; return code; } } while (0)
+    cudaStream_t st = h->stream;
+    TRY_R(upload(h->point2fs, s.point2fs, st));
+    TRY_R(upload(h->point3fs, s.point3fs, st));
+    TRY_R(upload(h->vector3fs, s.vector3fs, st));
+    TRY_R(upload(h->planes, s.planes, st));
+    TRY_R(upload(h->spheres, s.spheres, st));
+    TRY_R(upload(h->terrains, s.terrains, st));
+    TRY_R(upload(h->triangles, s.triangles, st));
+    TRY_R(upload(h->textures, s.textures, st));
+    TRY_R(upload(h->surfaces, s.surfaces, st));
+    TRY_R(upload(h->primitives, s.primitives, st));
+    TRY_R(upload(h->o2w, s.o2w, st));
+    TRY_R(upload(h->w2o, s.w2o, st));
+    TRY_R(upload(h->camera, s.camera, st));
+    TRY_R(upload(h->prim_info, d.prim_info, st));
+    TRY_R(upload(h->nodes, d.nodes, st));
+    TRY_R(upload(h->tris, d.tris, st));
+    TRY_R(upload(h->sphere4, d.sphere4, st));
+    TRY_R(upload(h->plane_a, d.plane_a, st));
+    TRY_R(upload(h->plane_n, d.plane_n, st));
+    DevScene& S = h->scene;
+    S.point2fs = h->point2fs.p; S.point3fs = h->point3fs.p; S.vector3fs = h->vector3fs.p;
+    S.planes = h->planes.p; S.spheres = h->spheres.p; S.terrains = h->terrains.p; S.triangles = h->triangles.p;
+    S.textures = h->textures.p; S.surfaces = h->surfaces.p; S.primitives = h->primitives.p;
+    S.o2w = h->o2w.p; S.w2o = h->w2o.p; S.camera = h->camera.p;
+    S.primitive_count = (int)np;
+    S.textures_count = (int)s.textures.size();
+    S.prim_info = h->prim_info.p; S.nodes = h->nodes.p; S.tris = h->tris.p; S.sphere4 = h->sphere4.p;
+    S.plane_a = h->plane_a.p; S.plane_n = h->plane_n.p;
+
+    const size_t n = (size_t)h->n_pixels;
+    TRY_R(h->q_o0.alloc(n)); TRY_R(h->q_o1.alloc(n)); TRY_R(h->q_d0.alloc(n)); TRY_R(h->q_d1.alloc(n));
+    TRY_R(h->q_hit.alloc(n)); TRY_R(h->s_o.alloc(n)); TRY_R(h->s_d.alloc(n)); TRY_R(h->s_c.alloc(n));
+    TRY_R(h->throughput.alloc(n)); TRY_R(h->radiance.alloc(n)); TRY_R(h->rng.alloc(n)); TRY_R(h->pixel_flags.alloc(n));
+    TRY_R(h->primary_o.alloc(n)); TRY_R(h->primary_d.alloc(n));
+    TRY_R(h->counts.alloc(64)); TRY_R(h->stats.alloc(4)); TRY_R(h->pass_index.alloc(1)); TRY_R(h->mean.alloc(3));
+    TRY_R(h->film_sum.alloc(n)); TRY_R(h->film_comp.alloc(n)); TRY_R(h->film_n.alloc(n)); TRY_R(h->bgra.alloc(n * 4));
+    TRY_R(h->primitive_offsets.alloc(n));
+    TRY_R(h->hit_prim.alloc(n)); TRY_R(h->hit_type.alloc(n)); TRY_R(h->hit_off.alloc(n)); TRY_R(h->hit_dist.alloc(n)); TRY_R(h->hit_normal.alloc(3 * n));
+    TRY_R(h->scratch_rgb.alloc(3 * n));
+    TRY_R(h->dev_params.alloc(1));
+    TRY_R(cudaMemsetAsync(h->film_sum.p, 0, n * sizeof(float4), st));
+    TRY_R(cudaMemsetAsync(h->film_comp.p, 0, n * sizeof(float4), st));
+    TRY_R(cudaMemsetAsync(h->film_n.p, 0, n * sizeof(int), st));
+    TRY_R(cudaMemsetAsync(h->primitive_offsets.p, 0xFF, n * sizeof(int), st));  // Arrays.fill(-1) (GRK:421)
+    TRY_R(cudaMemsetAsync(h->hit_normal.p, 0, 3 * n * sizeof(float), st));
+    TRY_R(cudaMemsetAsync(h->stats.p, 0, 4 * sizeof(unsigned long long), st));
+    TRY_R(cudaMemsetAsync(h->pass_index.p, 0, sizeof(int), st));
+    TRY_R(cudaMemsetAsync(h->pixel_flags.p, 0, n * sizeof(int), st));
+    DevPass& B = h->pass;
+    B.n_pixels = h->n_pixels;
+    B.q_o[0] = h->q_o0.p; B.q_o[1] = h->q_o1.p; B.q_d[0] = h->q_d0.p; B.q_d[1] = h->q_d1.p;
+    B.q_hit = h->q_hit.p; B.s_o = h->s_o.p; B.s_d = h->s_d.p; B.s_c = h->s_c.p;
+    B.throughput = h->throughput.p; B.radiance = h->radiance.p; B.rng = h->rng.p; B.pixel_flags = h->pixel_flags.p;
+    B.primary_o = h->primary_o.p; B.primary_d = h->primary_d.p; B.counts = h->counts.p; B.stats = h->stats.p;
+    B.pass_index = h->pass_index.p; B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p;
+    B.bgra = h->bgra.p; B.primitive_offsets = h->primitive_offsets.p;
+    B.hit_prim_offset = h->hit_prim.p; B.hit_shape_type = h->hit_type.p; B.hit_shape_offset = h->hit_off.p;
+    B.hit_distance = h->hit_dist.p; B.hit_normal = h->hit_normal.p;
+
+    // Noise tables (both kernel sets own a copy).
+    std::vector<int> perm(DFPT_PERMUTATION, DFPT_PERMUTATION + 256);
+    std::vector<float> grad(DFPT_GRADIENT3, DFPT_GRADIENT3 + 36);
+    DevBuf<int> dperm;
+    DevBuf<float> dgrad;
+    TRY_R(upload(dperm, perm, st));
+    TRY_R(upload(dgrad, grad, st));
+    h->fast.init_tables(st, dperm.p, dgrad.p);
+    h->strict.init_tables(st, dperm.p, dgrad.p);
+    TRY_R(cudaGetLastError());
+    TRY_R(cudaStreamSynchronize(st));
+    dperm.release();
+    dgrad.release();
+#undef TRY_R
+
+    h->ctx.scene = &h->scene;
+    h->ctx.params = h->dev_params.p;
+    h->ctx.pass = &h->pass;
+    h->ctx.stream = h->stream;
+    h->fast.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
+    r = push_params(h);
+    if (!r) r = reset_rng(h);
+    if (r) { release(h); delete h; return r; }
+    *out = h;
+    return DFPT_OK;
+}
+
+int dfpt_destroy(dfpt_handle* h) {
+    if (!h) return DFPT_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    release(h);
+    delete h;
+    return DFPT_OK;
+}
+
+int dfpt_set_stream(dfpt_handle* h, void* stream) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    h->own_stream = false;
+    h->stream = (cudaStream_t)stream;
+    if (!h->stream) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    h->ctx.stream = h->stream;
+    h->graph_valid = false;
+    return DFPT_OK;
+}
+
+int dfpt_set_camera(dfpt_handle* h, const float* camera19) {
+    if (!h || !camera19) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    h->host.camera.assign(camera19, camera19 + 19);
+    CUDA_TRY(cudaMemcpyAsync(h->camera.p, h->host.camera.data(), 19 * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_set_transforms(dfpt_handle* h, const float* o2w, const float* w2o, int32_t count) {
+    if (!h || !o2w || !w2o) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (count != h->scene.primitive_count) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive count %d != %d", count, h->scene.primitive_count);
+    h->host.o2w.assign(o2w, o2w + (size_t)count * 16);
+    h->host.w2o.assign(w2o, w2o + (size_t)count * 16);
+    if (count == 0) return DFPT_OK;
+    CUDA_TRY(cudaMemcpyAsync(h->o2w.p, h->host.o2w.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->w2o.p, h->host.w2o.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_set_surfaces(dfpt_handle* h, const float* surfaces, int64_t count) {
+    if (!h || !surfaces) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (count != (int64_t)h->host.surfaces.size()) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "surfaces count %lld != %zu", (long long)count, h->host.surfaces.size());
+    std::vector<float> old = h->host.surfaces;
+    h->host.surfaces.assign(surfaces, surfaces + count);
+    for (int i = 0; i < h->scene.primitive_count; ++i) {
+        int r = check_surface(h->host, h->host.primitives[3 * i + 2]);
+        if (r) { h->host.surfaces.swap(old); return r; }
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->surfaces.p, h->host.surfaces.data(), (size_t)count * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_set_sky(dfpt_handle* h, const dfpt_sky* sky) {
+    if (!h || !sky) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    const bool sun_changed = (h->sky.is_sun_active == 1) != (sky->is_sun_active == 1);
+    h->sky = *sky;
+    if (sun_changed) h->graph_valid = false;
+    return push_params(h);
+}
+
+int dfpt_set_params(dfpt_handle* h, const dfpt_params* p) {
+    if (!h || !p) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (p->rng_kind != DFPT_RNG_COUNTER && p->rng_kind != DFPT_RNG_LCG) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown rng kind %d", p->rng_kind);
+    const bool reseed = p->seed != h->params.seed || p->rng_kind != h->params.rng_kind;
+    if (p->renderer_type != h->params.renderer_type || p->pt_ray_depth_maximum != h->params.pt_ray_depth_maximum ||
+        p->wireframes != h->params.wireframes)
+        h->graph_valid = false;
+    h->params = *p;
+    int r = push_params(h);
+    if (r) return r;
+    if (reseed) return reset_rng(h);
+    return DFPT_OK;
+}
+
+// Not part of the public header: switches between the fast and the strict kernel set (the
+// strict set reproduces the reference's float arithmetic operation for operation).
+int dfpt_set_strict(dfpt_handle* h, int32_t strict) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    h->use_strict = strict != 0;
+    if (h->use_strict) h->strict.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
+    else h->fast.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
+    h->graph_valid = false;
+    return DFPT_OK;
+}
+
+int dfpt_set_record_hits(dfpt_handle* h, int32_t enabled) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    h->record_hits = enabled != 0;
+    return push_params(h);
+}
+
+int dfpt_set_graphs(dfpt_handle* h, int32_t enabled) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    h->use_graph = enabled != 0;
+    return DFPT_OK;
+}
+
+int dfpt_set_counting(dfpt_handle* h, int32_t enabled) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    h->counting = enabled != 0;
+    return push_params(h);
+}
+
+int dfpt_clear(dfpt_handle* h) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    h->clear_pass = h->host_pass;
+    return push_params(h);
+}
+
+int dfpt_render(dfpt_handle* h, int32_t passes) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    if (passes < 0) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "passes < 0");
+    if (h->counting) CUDA_TRY(cudaMemsetAsync(h->stats.p, 0, 4 * sizeof(unsigned long long), h->stream));
+    if (passes == 0) return DFPT_OK;
+    if (h->use_graph) {
+        if (!h->graph_valid) {
+            int r = build_graph(h);
+            if (r) return r;
+        }
+        for (int i = 0; i < passes; ++i) {
+            CUDA_TRY(cudaGraphLaunch(h->graph_exec, h->stream));
+            h->launches += (uint64_t)h->graph_kernels;
+        }
+    } else {
+        for (int i = 0; i < passes; ++i) h->launches += (uint64_t)issue_pass(h);
+        CUDA_TRY(cudaGetLastError());
+    }
+    h->host_pass += passes;
+    return DFPT_OK;
+}
+
+int dfpt_synchronize(dfpt_handle* h) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_read_bgra8(dfpt_handle* h, uint8_t* out) {
+    if (!h || !out) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaMemcpyAsync(out, h->bgra.p, (size_t)h->n_pixels * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_read_film(dfpt_handle* h, float* rgb, int32_t* samples) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    kset(h).film_average(h->ctx, h->scratch_rgb.p, h->film_n.p == nullptr ? nullptr : nullptr);
+    h->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    if (rgb) CUDA_TRY(cudaMemcpyAsync(rgb, h->scratch_rgb.p, (size_t)h->n_pixels * 12, cudaMemcpyDeviceToHost, h->stream));
+    if (samples) CUDA_TRY(cudaMemcpyAsync(samples, h->film_n.p, (size_t)h->n_pixels * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_read_film_mean(dfpt_handle* h, double* mean3) {
+    if (!h || !mean3) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaMemsetAsync(h->mean.p, 0, 3 * sizeof(double), h->stream));
+    kset(h).film_mean(h->ctx, h->mean.p);
+    h->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    double sums[3];
+    CUDA_TRY(cudaMemcpyAsync(sums, h->mean.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < 3; ++i) mean3[i] = sums[i] / (double)h->n_pixels;
+    return DFPT_OK;
+}
+
+int dfpt_read_primitive_offsets(dfpt_handle* h, int32_t* out) {
+    if (!h || !out) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaMemcpyAsync(out, h->primitive_offsets.p, (size_t)h->n_pixels * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_read_hits(dfpt_handle* h, int32_t* prim, int32_t* type, int32_t* off, float* dist, float* normal3) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    if (!h->record_hits) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "hit recording is off (dfpt_set_record_hits)");
+    const size_t n = (size_t)h->n_pixels;
+    if (prim) CUDA_TRY(cudaMemcpyAsync(prim, h->hit_prim.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (type) CUDA_TRY(cudaMemcpyAsync(type, h->hit_type.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (off) CUDA_TRY(cudaMemcpyAsync(off, h->hit_off.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (dist) CUDA_TRY(cudaMemcpyAsync(dist, h->hit_dist.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (normal3) CUDA_TRY(cudaMemcpyAsync(normal3, h->hit_normal.p, n * 12, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return DFPT_OK;
+}
+
+int dfpt_read_counters(dfpt_handle* h, uint64_t* c4) {
+    if (!h || !c4) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    unsigned long long v[4];
+    CUDA_TRY(cudaMemcpyAsync(v, h->stats.p, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < 4; ++i) c4[i] = v[i];
+    return DFPT_OK;
+}
+
+int dfpt_launch_count(dfpt_handle* h, uint64_t* launches) {
+    if (!h || !launches) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *launches = h->launches;
+    return DFPT_OK;
+}
+
+}  // extern "C"

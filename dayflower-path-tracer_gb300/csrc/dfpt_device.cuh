@@ -1,0 +1,384 @@
+// dfpt_device.cuh - device code of the renderer core (sm_103a).
+//
+// This header is compiled twice: by dfpt_kernels_fast.cu (namespace dfpt_fast, FMA contraction
+// allowed) and by dfpt_kernels_strict.cu (namespace dfpt_strict, -fmad=false) whose arithmetic
+// is one IEEE rounding per operation, the Java float semantics of the reference kernel, so
+// ray-cast hit ids, distances and normals come out bit-identical to a strict FP32 restatement.
+//
+// Reference: src/main/java/org/dayflower/pathtracer/kernel/GPURendererKernel.java (cited below
+// as GRK:line), AbstractKernel.java (AK:line), AbstractImageKernel.java (AIK:line).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dfpt_device_types.h"
+#include "dfpt_internal.h"
+#include "dfpt_noise_tables.h"
+
+#ifndef DFPT_NS
+#error "define DFPT_NS before including dfpt_device.cuh"
+#endif
+
+namespace DFPT_NS {
+
+// ---------------------------------------------------------------------------------------------
+// Constants (AK:56, GRK:76-78, MathF PI family: float products/quotients of (float)Math.PI).
+constexpr float INF = 100000.0f;
+constexpr float PI_F = 3.14159274101257324219f;
+constexpr float TWO_PI = PI_F * 2.0f;
+constexpr float INV_PI = 1.0f / PI_F;
+constexpr float INV_TWO_PI = 1.0f / TWO_PI;
+constexpr float PI_OVER_180 = PI_F / 180.0f;
+constexpr float COLOR_RECIPROCAL = 1.0f / 255.0f;
+constexpr float EPSILON_AK = 0.02f;
+
+// Noise tables in global memory (divergent gathers go through L1, not the serialising constant
+// cache); filled from DFPT_PERMUTATION / DFPT_GRADIENT3 when a handle is created.
+__device__ int g_perm[512];
+__device__ float g_grad3[36];
+__device__ __forceinline__ int perm(int i) { return __ldg(g_perm + i); }
+__device__ __forceinline__ float grad(int i) { return __ldg(g_grad3 + i); }
+
+// Java Math.min/max: NaN propagates (PTX min.NaN / max.NaN, sm_80+).
+__device__ __forceinline__ float jmin(float a, float b) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float jmax(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+// Aparapi's rsqrt is 1 / sqrt: both correctly rounded here (no fast-math).
+__device__ __forceinline__ float rsqrt_j(float x) { return 1.0f / sqrtf(x); }
+__device__ __forceinline__ float saturate_j(float v, float a, float b) {
+    const float lo = jmin(a, b), hi = jmax(a, b);
+    return v < lo ? lo : v > hi ? hi : v;
+}
+__device__ __forceinline__ float modulo_j(float v) { return v - floorf(v); }                    // AK:420
+__device__ __forceinline__ float remainder_j(float x, float y) { return x - (float)(int)(x / y) * y; }  // AK:529
+__device__ __forceinline__ int f2i(float f) { return (int)f; }  // cvt.rzi saturates, NaN -> 0 (Java)
+__device__ __forceinline__ float lerp_j(float a, float b, float t) { return (1.0f - t) * a + t * b; }
+__device__ __forceinline__ float blerp_j(float v00, float v01, float v10, float v11, float tx, float ty) {
+    return lerp_j(lerp_j(v00, v01, tx), lerp_j(v10, v11, tx), ty);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Random numbers. Counter mode: Philox4x32-10 (Salmon et al., SC'11) keyed by (pixel, seed),
+// counted by (pass, draw/4); a path draws its numbers in the reference's order, one per call.
+// LCG mode: the reference's per-pixel 48-bit LCG (AK:438-440, 1101-1110).
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+struct Rng {
+    uint64_t state;  // LCG: 48-bit state; counter: draws made this pass
+    uint32_t pixel, pass, seed_lo, seed_hi;
+    int kind;
+    uint4 block;
+    uint32_t block_id;
+
+    __device__ __forceinline__ float next() {
+        if (kind == DFPT_RNG_LCG) {
+            state = (state * 0x5DEECE66Dull + 0xBull) & ((1ull << 48) - 1ull);
+            return (float)(uint32_t)(state >> 24) * (1.0f / 16777216.0f);
+        }
+        const uint32_t i = (uint32_t)state;
+        state = (uint64_t)(i + 1u);
+        const uint32_t bid = i >> 2;
+        if (bid != block_id) {
+            block = philox4x32_10(make_uint4(pass, bid, seed_hi, 0x44465054u), make_uint2(pixel, seed_lo));
+            block_id = bid;
+        }
+        const uint32_t lane = i & 3u;
+        const uint32_t x = lane == 0 ? block.x : lane == 1 ? block.y : lane == 2 ? block.z : block.w;
+        return (float)(x >> 8) * (1.0f / 16777216.0f);
+    }
+};
+
+__device__ __forceinline__ Rng make_rng(const DevParams& P, uint32_t pixel, uint32_t pass, uint64_t state) {
+    Rng r;
+    r.state = state;
+    r.pixel = pixel;
+    r.pass = pass;
+    r.seed_lo = P.seed_lo;
+    r.seed_hi = P.seed_hi;
+    r.kind = P.rng_kind;
+    r.block_id = 0xFFFFFFFFu;
+    r.block = make_uint4(0, 0, 0, 0);
+    return r;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Simplex noise (Gustavson) and fBm as the reference writes them (AK:600-716, 762-900).
+
+__device__ __forceinline__ int fast_floor(float v) {
+    const int i = (int)v;
+    return v < (float)i ? i - 1 : i;
+}
+
+__device__ float simplex2(float x, float y) {
+    const float F2 = 0.3660254037844386f, G2 = 0.21132486540518713f;
+    const float s = (x + y) * F2;
+    const int i = fast_floor(x + s), j = fast_floor(y + s);
+    const float t = (float)(i + j) * G2;
+    const float x0 = x - ((float)i - t), y0 = y - ((float)j - t);
+    const int i1 = x0 > y0 ? 1 : 0, j1 = x0 > y0 ? 0 : 1;
+    const float x1 = x0 - (float)i1 + G2, y1 = y0 - (float)j1 + G2;
+    const float x2 = x0 - 1.0f + 2.0f * G2, y2 = y0 - 1.0f + 2.0f * G2;
+    const int ii = i & 0xFF, jj = j & 0xFF;
+    const int gi0 = perm(ii + perm(jj)) % 12;
+    const int gi1 = perm(ii + i1 + perm(jj + j1)) % 12;
+    const int gi2 = perm(ii + 1 + perm(jj + 1)) % 12;
+    const float t0 = 0.5f - x0 * x0 - y0 * y0;
+    const float n0 = t0 < 0.0f ? 0.0f : (t0 * t0) * (t0 * t0) * (grad(gi0 * 3) * x0 + grad(gi0 * 3 + 1) * y0);
+    const float t1 = 0.5f - x1 * x1 - y1 * y1;
+    const float n1 = t1 < 0.0f ? 0.0f : (t1 * t1) * (t1 * t1) * (grad(gi1 * 3) * x1 + grad(gi1 * 3 + 1) * y1);
+    const float t2 = 0.5f - x2 * x2 - y2 * y2;
+    const float n2 = t2 < 0.0f ? 0.0f : (t2 * t2) * (t2 * t2) * (grad(gi2 * 3) * x2 + grad(gi2 * 3 + 1) * y2);
+    return 70.0f * (n0 + n1 + n2);
+}
+
+__device__ float simplex3(float x, float y, float z) {
+    const float F3 = 1.0f / 3.0f, G3 = 1.0f / 6.0f;
+    const float s = (x + y + z) * F3;
+    const int i = fast_floor(x + s), j = fast_floor(y + s), k = fast_floor(z + s);
+    const float t = (float)(i + j + k) * G3;
+    const float x0 = x - ((float)i - t), y0 = y - ((float)j - t), z0 = z - ((float)k - t);
+    int i1, j1, k1, i2, j2, k2;
+    if (x0 >= y0) {
+        if (y0 >= z0) { i1 = 1; j1 = 0; k1 = 0; i2 = 1; j2 = 1; k2 = 0; }
+        else if (x0 >= z0) { i1 = 1; j1 = 0; k1 = 0; i2 = 1; j2 = 0; k2 = 1; }
+        else { i1 = 0; j1 = 0; k1 = 1; i2 = 1; j2 = 0; k2 = 1; }
+    } else {
+        if (y0 < z0) { i1 = 0; j1 = 0; k1 = 1; i2 = 0; j2 = 1; k2 = 1; }
+        else if (x0 < z0) { i1 = 0; j1 = 1; k1 = 0; i2 = 0; j2 = 1; k2 = 1; }
+        else { i1 = 0; j1 = 1; k1 = 0; i2 = 1; j2 = 1; k2 = 0; }
+    }
+    const float x1 = x0 - (float)i1 + G3, y1 = y0 - (float)j1 + G3, z1 = z0 - (float)k1 + G3;
+    const float x2 = x0 - (float)i2 + 2.0f * G3, y2 = y0 - (float)j2 + 2.0f * G3, z2 = z0 - (float)k2 + 2.0f * G3;
+    const float x3 = x0 - 1.0f + 3.0f * G3, y3 = y0 - 1.0f + 3.0f * G3, z3 = z0 - 1.0f + 3.0f * G3;
+    const int ii = i & 0xFF, jj = j & 0xFF, kk = k & 0xFF;
+    const int gi0 = perm(ii + perm(jj + perm(kk))) % 12;
+    const int gi1 = perm(ii + i1 + perm(jj + j1 + perm(kk + k1))) % 12;
+    const int gi2 = perm(ii + i2 + perm(jj + j2 + perm(kk + k2))) % 12;
+    const int gi3 = perm(ii + 1 + perm(jj + 1 + perm(kk + 1))) % 12;
+    float n = 0.0f, tt;
+    tt = 0.6f - x0 * x0 - y0 * y0 - z0 * z0;
+    const float n0 = tt < 0.0f ? 0.0f : (tt * tt) * (tt * tt) * (grad(gi0 * 3) * x0 + grad(gi0 * 3 + 1) * y0 + grad(gi0 * 3 + 2) * z0);
+    tt = 0.6f - x1 * x1 - y1 * y1 - z1 * z1;
+    const float n1 = tt < 0.0f ? 0.0f : (tt * tt) * (tt * tt) * (grad(gi1 * 3) * x1 + grad(gi1 * 3 + 1) * y1 + grad(gi1 * 3 + 2) * z1);
+    tt = 0.6f - x2 * x2 - y2 * y2 - z2 * z2;
+    const float n2 = tt < 0.0f ? 0.0f : (tt * tt) * (tt * tt) * (grad(gi2 * 3) * x2 + grad(gi2 * 3 + 1) * y2 + grad(gi2 * 3 + 2) * z2);
+    tt = 0.6f - x3 * x3 - y3 * y3 - z3 * z3;
+    const float n3 = tt < 0.0f ? 0.0f : (tt * tt) * (tt * tt) * (grad(gi3 * 3) * x3 + grad(gi3 * 3 + 1) * y3 + grad(gi3 * 3 + 2) * z3);
+    n = 32.0f * (n0 + n1 + n2 + n3);
+    return n;
+}
+
+// simplexFractionalBrownianMotionXYZ (AK:695-716)
+__device__ float fbm3(float frequency, float gain, float minimum, float maximum, int octaves, float x, float y, float z) {
+    float amp = 1.0f, max_amp = 0.0f, freq = frequency, noise = 0.0f;
+    for (int i = 0; i < octaves; ++i) {
+        noise += simplex3(x * freq, y * freq, z * freq) * amp;
+        max_amp += amp;
+        amp *= gain;
+        freq *= 2.0f;
+    }
+    noise /= max_amp;
+    return noise * (maximum - minimum) / 2.0f + (maximum + minimum) / 2.0f;
+}
+
+// simplexFractalXY (AK:560-575), used by the ray marcher's height function (GRK:726-728)
+__device__ float fractal2(float amplitude, float frequency, float gain, float lacunarity, int octaves, float x, float y) {
+    float result = 0.0f, amp = amplitude, freq = frequency;
+    for (int i = 0; i < octaves; ++i) {
+        result += amp * simplex2(x * freq, y * freq);
+        amp *= gain;
+        freq *= lacunarity;
+    }
+    return result;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Shape intersections (GRK:1414-1594). tmin/tmax exclusive, INF on a miss.
+
+__device__ __forceinline__ float isect_plane(float ox, float oy, float oz, float dx, float dy, float dz, float4 a, float4 n, float tmax) {
+    const float dp = n.x * dx + n.y * dy + n.z * dz;
+    if (dp < 0.0f || dp > 0.0f) {
+        const float t = ((a.x - ox) * n.x + (a.y - oy) * n.y + (a.z - oz) * n.z) / dp;
+        if (t > 0.001f && t < tmax) return t;
+    }
+    return INF;
+}
+
+__device__ __forceinline__ float isect_sphere(float ox, float oy, float oz, float dx, float dy, float dz, float4 s, float tmax) {
+    const float px = ox - s.x, py = oy - s.y, pz = oz - s.z;
+    const float r2 = s.w * s.w;
+    const float a = dx * dx + dy * dy + dz * dz;
+    const float b = 2.0f * (px * dx + py * dy + pz * dz);
+    const float c = (px * px + py * py + pz * pz) - r2;
+    const float disc2 = b * b - 4.0f * a * c;
+    if (disc2 >= 0.0f) {
+        const float disc = sqrtf(disc2);
+        const float q = -0.5f * (b < 0.0f ? b - disc : b + disc);
+        const float r0 = q / a;
+        const float r1 = q == 0.0f ? r0 : c / q;
+        const float t0 = jmin(r0, r1), t1 = jmax(r0, r1);
+        if (t0 > 0.001f && t0 < tmax) return t0;
+        if (t1 > 0.001f && t1 < tmax) return t1;
+    }
+    return INF;
+}
+
+// Moller-Trumbore with the reference's tolerances; e0 = b - a and e1 = c - a precomputed.
+__device__ __forceinline__ float isect_triangle(float ox, float oy, float oz, float dx, float dy, float dz, float4 a, float4 e0, float4 e1, float tmax) {
+    const float v0x = dy * e1.z - dz * e1.y;
+    const float v0y = dz * e1.x - dx * e1.z;
+    const float v0z = dx * e1.y - dy * e1.x;
+    const float det = e0.x * v0x + e0.y * v0y + e0.z * v0z;
+    float t = INF;
+    if (det < -0.0001f || det > 0.0001f) {
+        const float inv = 1.0f / det;
+        const float v1x = ox - a.x, v1y = oy - a.y, v1z = oz - a.z;
+        const float u = (v1x * v0x + v1y * v0y + v1z * v0z) * inv;
+        if (u >= 0.0f && u <= 1.0f) {
+            const float v2x = v1y * e0.z - v1z * e0.y;
+            const float v2y = v1z * e0.x - v1x * e0.z;
+            const float v2z = v1x * e0.y - v1y * e0.x;
+            const float v = (dx * v2x + dy * v2y + dz * v2z) * inv;
+            t = v >= 0.0f && u + v <= 1.0f ? (e1.x * v2x + e1.y * v2y + e1.z * v2z) * inv : 0.001f;
+            t = t > 0.001f && t < tmax ? t : INF;
+        }
+    }
+    return t;
+}
+
+// Ray march of the (parameter-free) sin(x)sin(z) terrain (GRK:1470-1505).
+__device__ float isect_terrain(float ox, float oy, float oz, float dx, float dy, float dz) {
+    const float scale_r = 1.0f / 10.0f;
+    float t = 0.0f, t_delta = 0.01f, lh = 0.0f, ly = 0.0f;
+    for (float tc = 0.001f; tc < 10.0f; tc += t_delta) {
+        const float px = ox * scale_r + dx * tc;
+        const float py = oy * scale_r + dy * tc;
+        const float pz = oz * scale_r + dz * tc;
+        const float h = sinf(px) * sinf(pz);
+        if (py < h) {
+            t = tc - t_delta + t_delta * (lh - ly) / (py - ly - h + lh);
+            tc = 10.0f;
+        }
+        t_delta = 0.01f * tc;
+        lh = h;
+        ly = py;
+    }
+    return t > EPSILON_AK ? t : INF;
+}
+
+struct Hit {
+    float t;
+    int prim;        // primitive index (primitive offset / 3), -1 on a miss
+    int shape_type;  // Triangle (4) for mesh hits
+    int shape_offset;
+};
+
+struct TraceStats {
+    uint32_t nodes, tris;
+};
+
+// doIntersectPrimitives (GRK:1048-1256): a linear loop over primitives, each ray transformed
+// to object space; meshes walk the threaded (preorder, skip-pointer) BVH exactly as flattened.
+// ANY = isTesting: return at the first primitive with a hit.
+template <bool ANY>
+__device__ Hit trace(const DevScene& S, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
+    Hit h;
+    h.t = INF;
+    h.prim = -1;
+    h.shape_type = -1;
+    h.shape_offset = -1;
+    const int np = S.primitive_count;
+    for (int i = 0; i < np; ++i) {
+        const int4 info = __ldg(S.prim_info + i);
+        const float4* W = reinterpret_cast<const float4*>(S.w2o) + i * 4;
+        const float4 r0 = __ldg(W), r1 = __ldg(W + 1), r2 = __ldg(W + 2);
+        const float oxo = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
+        const float oyo = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
+        const float ozo = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
+        const float dxo = r0.x * dx + r0.y * dy + r0.z * dz;
+        const float dyo = r1.x * dx + r1.y * dy + r1.z * dz;
+        const float dzo = r2.x * dx + r2.y * dy + r2.z * dz;
+        float t = INF;
+        const int type = info.x;
+        if (type == DFPT_SHAPE_TRIANGLE_MESH) {
+            const float ix = 1.0f / dxo, iy = 1.0f / dyo, iz = 1.0f / dzo;
+            int node = info.w;
+            while (node != -1) {
+                const float4 n0 = __ldg(S.nodes + 2 * node);
+                const float4 n1 = __ldg(S.nodes + 2 * node + 1);
+                st.nodes++;
+                const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
+                const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
+                const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
+                const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+                const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
+                const int next = __float_as_int(n0.w);
+                const int leaf = __float_as_int(n1.w);
+                if (tb < 0.0f) {
+                    node = next;
+                } else if (leaf == -1) {
+                    node = node + 1;
+                } else {
+                    int k = leaf;  // -2 marks an empty leaf
+                    for (; k >= 0;) {
+                        const float4 a = __ldg(S.tris + 3 * k);
+                        const float4 e0 = __ldg(S.tris + 3 * k + 1);
+                        const float4 e1 = __ldg(S.tris + 3 * k + 2);
+                        st.tris++;
+                        t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, a, e0, e1, h.t);
+                        if (t < h.t) {
+                            h.t = t;
+                            h.prim = i;
+                            h.shape_type = DFPT_SHAPE_TRIANGLE;
+                            h.shape_offset = __float_as_int(a.w);
+                        }
+                        if (ANY && h.prim != -1) return h;
+                        if (__float_as_int(e0.w) != 0) break;
+                        ++k;
+                    }
+                    node = next;
+                }
+            }
+            t = INF;  // the mesh updated the closest hit in place
+        } else if (type == DFPT_SHAPE_PLANE) {
+            t = isect_plane(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.plane_a + info.w), __ldg(S.plane_n + info.w), h.t);
+        } else if (type == DFPT_SHAPE_SPHERE) {
+            t = isect_sphere(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.sphere4 + info.w), h.t);
+        } else if (type == DFPT_SHAPE_TERRAIN) {
+            t = isect_terrain(oxo, oyo, ozo, dxo, dyo, dzo);
+        } else if (type == DFPT_SHAPE_TRIANGLE) {
+            st.tris++;
+            t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.tris + 3 * info.w), __ldg(S.tris + 3 * info.w + 1),
+                               __ldg(S.tris + 3 * info.w + 2), h.t);
+        }
+        if (t < h.t) {
+            h.t = t;
+            h.prim = i;
+            h.shape_type = type;
+            h.shape_offset = info.y;
+        }
+        if (ANY && h.prim != -1) return h;
+    }
+    return h;
+}
+
+}  // namespace DFPT_NS

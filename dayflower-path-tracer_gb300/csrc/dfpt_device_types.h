@@ -1,0 +1,104 @@
+// dfpt_device_types.h - device-side views of the scene, the parameters and the pass buffers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dfpt.h"
+
+// The uploaded scene. The reference's arrays are kept as they are (shading reads them through
+// the same element offsets); the traversal reads the derived, 16-byte aligned records below.
+struct DevScene {
+    const float* point2fs;
+    const float* point3fs;
+    const float* vector3fs;
+    const int* planes;
+    const float* spheres;
+    const float* terrains;
+    const int* triangles;
+    const float* textures;
+    const float* surfaces;
+    const int* primitives;
+    const float* o2w;  // 16 floats per primitive, row-major
+    const float* w2o;
+    const float* camera;
+    int primitive_count;
+    int textures_count;
+    // Derived records.
+    const int4* prim_info;  // {shape type, shape offset, surface offset, record index}
+    const float4* nodes;    // 2 per BVH node: {min.xyz, next}, {max.xyz, first triangle or -1}
+    const float4* tris;     // 3 per triangle: {a.xyz, triangle offset}, {b-a, last-in-leaf}, {c-a, 0}
+    const float4* sphere4;  // {position.xyz, radius} per sphere record
+    const float4* plane_a;  // point A per plane record
+    const float4* plane_n;  // surface normal per plane record
+};
+
+// Renderer parameters and derived per-scene constants, in device memory (read through __ldg) so
+// captured CUDA graphs stay valid when they change.
+struct DevParams {
+    int renderer_type;
+    int tone_mapper_type;
+    int shader_type;
+    int normal_mapping;
+    int wireframes;
+    int depth_max;
+    int depth_rr;
+    float exposure;
+    float ao_max_distance;
+    float g_amplitude, g_frequency, g_gain, g_lacunarity;
+    int g_octaves;
+    int selected_primitive_offset;
+    int rng_kind;
+    uint32_t seed_lo, seed_hi;
+    int width, height;
+    int record_hits;
+    int counting;
+    int clear_pass;  // the film is replaced (not averaged) on this pass index
+    // Sky (float copies of the Perez model; den_l is the theta0-only denominator).
+    float sky_u[3], sky_v[3], sky_w[3];
+    float sun_dir[3], sun_dir_world[3], sun_origin[3];
+    float theta;
+    int sky_active, sun_active;
+    float perez_l[5], perez_x[5], perez_y[5];
+    float zenith_l, zenith_x, zenith_y;
+    float den_l;        // (1 + l0 e^l1)(1 + l2 e^(l3 theta0) + l4 cos^2 theta0)
+    float den_x_a, den_y_a;  // 1 + x0 e^x1, 1 + y0 e^y1
+    float cos_theta0;
+    // sRGB redo-gamma constants (RGBColorSpace.SRGB).
+    float cs_break, cs_gamma, cs_slope, cs_slope_match, cs_segment;
+};
+
+// Wavefront buffers of one handle. Queue entries are SoA float4 records.
+struct DevPass {
+    int n_pixels;
+    float4* q_o[2];       // {origin.xyz, path id}
+    float4* q_d[2];       // {direction.xyz, 0}
+    int4* q_hit;          // {t bits, primitive index, shape type, shape offset}
+    float4* s_o;          // shadow rays {origin.xyz, path id}
+    float4* s_d;          // {direction.xyz, 0}
+    float4* s_c;          // pending sun contribution {rgb, 0}
+    float4* throughput;   // per path
+    float4* radiance;     // per path
+    uint64_t* rng;        // per pixel: LCG state or draw counter
+    int* pixel_flags;     // bit 0: film set to black this pass
+    float4* primary_o;    // primary rays (wireframe overlay)
+    float4* primary_d;
+    int* counts;          // [0..31] ray queue counts per bounce, [32..63] shadow counts
+    unsigned long long* stats;  // closest, any, nodes, triangles
+    int* pass_index;      // device pass counter
+    // Film (Kahan-compensated sums), image and selection buffers.
+    float4* film_sum;
+    float4* film_comp;
+    int* film_n;
+    uint8_t* bgra;
+    int* primitive_offsets;
+    // Primary hit record (optional).
+    int* hit_prim_offset;
+    int* hit_shape_type;
+    int* hit_shape_offset;
+    float* hit_distance;
+    float* hit_normal;
+};
+
+#define DFPT_COUNTS_SHADOW 32
+#define DFPT_MAX_DEPTH 30

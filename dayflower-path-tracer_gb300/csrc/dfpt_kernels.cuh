@@ -1,0 +1,1138 @@
+// dfpt_kernels.cuh - surface evaluation, shading and the wavefront kernels.
+//
+// Included by dfpt_kernels_fast.cu and dfpt_kernels_strict.cu after dfpt_device.cuh, inside the
+// namespace chosen by DFPT_NS. References: GRK = GPURendererKernel.java, AIK =
+// AbstractImageKernel.java (src/main/java/org/dayflower/pathtracer/kernel/).
+#pragma once
+
+#include "dfpt_device.cuh"
+#include "dfpt_launch.h"
+
+namespace DFPT_NS {
+
+// ---------------------------------------------------------------------------------------------
+// The intersection record the shading reads (GRK:79-94): point, shading normal, UV, tangent.
+struct Surf {
+    float px, py, pz;
+    float nx, ny, nz;
+    float u, v;
+    float tx, ty, tz;
+};
+
+__device__ __forceinline__ float3 p3(const DevScene& S, int off) {
+    return make_float3(__ldg(S.point3fs + off), __ldg(S.point3fs + off + 1), __ldg(S.point3fs + off + 2));
+}
+__device__ __forceinline__ float3 v3(const DevScene& S, int off) {
+    return make_float3(__ldg(S.vector3fs + off), __ldg(S.vector3fs + off + 1), __ldg(S.vector3fs + off + 2));
+}
+__device__ __forceinline__ float texf(const DevScene& S, int off) { return __ldg(S.textures + off); }
+
+// Image texture lookup without filtering (GRK:1894-1929).
+__device__ int image_texture_simple(const DevScene& S, int to, float u, float v) {
+    const float width = texf(S, to + 4), height = texf(S, to + 5);
+    const float su = texf(S, to + 6), sv = texf(S, to + 7);
+    const float ca = texf(S, to + 2), sa = texf(S, to + 3);
+    const float u0 = (u * ca - v * sa), v0 = (v * ca + u * sa);
+    const float u1 = remainder_j(u0 * su * width, width), v1 = remainder_j(v0 * sv * height, height);
+    const float u2 = u1 >= 0.0f ? u1 : width - fabsf(u1);
+    const float v2 = v1 >= 0.0f ? v1 : height - fabsf(v1);
+    const int x = f2i(u2), y = f2i(v2);
+    const int w = f2i(width), res = f2i(width * height);
+    const int index = y * w + x;
+    return index >= 0 && index < res ? f2i(texf(S, to + 8 + index)) : 0;
+}
+
+// Object-space surface properties of the hit, the transform to world space and normal mapping
+// (GRK:1258-1400, 2349-2650, 2658-2846, 3998-4073).
+__device__ Surf surface(const DevScene& S, const DevParams& P, float ox, float oy, float oz, float dx, float dy, float dz, const Hit& h) {
+    const float4* W = reinterpret_cast<const float4*>(S.w2o) + h.prim * 4;
+    const float4 w0 = __ldg(W), w1 = __ldg(W + 1), w2 = __ldg(W + 2);
+    const float4* O = reinterpret_cast<const float4*>(S.o2w) + h.prim * 4;
+    const float4 m0 = __ldg(O), m1 = __ldg(O + 1), m2 = __ldg(O + 2);
+    const float oxo = w0.x * ox + w0.y * oy + w0.z * oz + w0.w;
+    const float oyo = w1.x * ox + w1.y * oy + w1.z * oz + w1.w;
+    const float ozo = w2.x * ox + w2.y * oy + w2.z * oz + w2.w;
+    const float dxo = w0.x * dx + w0.y * dy + w0.z * dz;
+    const float dyo = w1.x * dx + w1.y * dy + w1.z * dz;
+    const float dzo = w2.x * dx + w2.y * dy + w2.z * dz;
+    const float t = h.t;
+    Surf s;
+    s.tx = s.ty = s.tz = 0.0f;
+    s.u = s.v = 0.0f;
+    const int off = h.shape_offset;
+    if (h.shape_type == DFPT_SHAPE_PLANE) {
+        const float3 a = p3(S, __ldg(S.planes + off)), b = p3(S, __ldg(S.planes + off + 1)), c = p3(S, __ldg(S.planes + off + 2));
+        const float3 n = v3(S, __ldg(S.planes + off + 3));
+        s.px = oxo + dxo * t; s.py = oyo + dyo * t; s.pz = ozo + dzo * t;
+        const float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
+        const bool isX = ax > ay && ax > az;
+        const bool isY = ay > az;
+        const float a1x = isX ? a.y : isY ? a.z : a.x;
+        const float a1y = isX ? a.z : isY ? a.x : a.y;
+        const float b1x = isX ? c.y - a.x : isY ? c.z - a.x : c.x - a.x;
+        const float b1y = isX ? c.z - a.y : isY ? c.x - a.y : c.y - a.y;
+        const float c1x = isX ? b.y - a.x : isY ? b.z - a.x : b.x - a.x;
+        const float c1y = isX ? b.z - a.y : isY ? b.x - a.y : b.y - a.y;
+        const float det = b1x * c1y - b1y * c1x;
+        const float dr = 1.0f / det;
+        const float bnu = -b1y * dr, bnv = b1x * dr, bnd = (b1y * a1x - b1x * a1y) * dr;
+        const float cnu = c1y * dr, cnv = -c1x * dr, cnd = (c1x * a1y - c1y * a1x) * dr;
+        const float hu = isX ? s.py : isY ? s.pz : s.px;
+        const float hv = isX ? s.pz : isY ? s.px : s.py;
+        s.u = hu * bnu + hv * bnv + bnd;
+        s.v = hu * cnu + hv * cnv + cnd;
+        s.nx = n.x; s.ny = n.y; s.nz = n.z;
+    } else if (h.shape_type == DFPT_SHAPE_SPHERE) {
+        const float3 c = p3(S, f2i(__ldg(S.spheres + off)));
+        s.px = oxo + dxo * t; s.py = oyo + dyo * t; s.pz = ozo + dzo * t;
+        const float n0x = s.px - c.x, n0y = s.py - c.y, n0z = s.pz - c.z;
+        const float r = rsqrt_j(n0x * n0x + n0y * n0y + n0z * n0z);
+        s.nx = n0x * r; s.ny = n0y * r; s.nz = n0z * r;
+        s.u = 0.5f + atan2f(-s.nz, -s.nx) * INV_TWO_PI;
+        s.v = 0.5f - asinf(-s.ny) * INV_PI;
+    } else if (h.shape_type == DFPT_SHAPE_TERRAIN) {
+        const float sr = 1.0f / 10.0f;
+        s.px = oxo * sr + dxo * t; s.py = oyo * sr + dyo * t; s.pz = ozo * sr + dzo * t;
+        const float e = 0.02f;
+        const float nx = (sinf(s.px - e) * sinf(s.pz)) - (sinf(s.px + e) * sinf(s.pz));
+        const float ny = 2.0f * e;
+        const float nz = (sinf(s.px) * sinf(s.pz - e)) - (sinf(s.px) * sinf(s.pz + e));
+        const float r = rsqrt_j(nx * nx + ny * ny + nz * nz);
+        s.nx = nx * r; s.ny = ny * r; s.nz = nz * r;
+        s.u = s.px; s.v = s.pz;
+    } else {  // Triangle
+        const int* T = S.triangles + off;
+        const float3 a = p3(S, __ldg(T + 0)), b = p3(S, __ldg(T + 1)), c = p3(S, __ldg(T + 2));
+        s.px = oxo + dxo * t; s.py = oyo + dyo * t; s.pz = ozo + dzo * t;
+        const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
+        const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
+        const float v0x = dyo * acz - dzo * acy, v0y = dzo * acx - dxo * acz, v0z = dxo * acy - dyo * acx;
+        const float v1x = oxo - a.x, v1y = oyo - a.y, v1z = ozo - a.z;
+        const float v2x = v1y * abz - v1z * aby, v2y = v1z * abx - v1x * abz, v2z = v1x * aby - v1y * abx;
+        const float det = abx * v0x + aby * v0y + abz * v0z;
+        const float dr = 1.0f / det;
+        const float bu = (v1x * v0x + v1y * v0y + v1z * v0z) * dr;
+        const float bv = (dxo * v2x + dyo * v2y + dzo * v2z) * dr;
+        const float bw = 1.0f - bu - bv;
+        const int ta = __ldg(T + 6), tb = __ldg(T + 7), tc = __ldg(T + 8);
+        s.u = bw * __ldg(S.point2fs + ta) + bu * __ldg(S.point2fs + tb) + bv * __ldg(S.point2fs + tc);
+        s.v = bw * __ldg(S.point2fs + ta + 1) + bu * __ldg(S.point2fs + tb + 1) + bv * __ldg(S.point2fs + tc + 1);
+        float n0x = 0.0f, n0y = 0.0f, n0z = 0.0f, t0x = 0.0f, t0y = 0.0f, t0z = 0.0f;
+        if (P.shader_type == DFPT_SHADER_FLAT) {
+            n0x = aby * acz - abz * acy;
+            n0y = abz * acx - abx * acz;
+            n0z = abx * acy - aby * acx;
+        } else if (P.shader_type == DFPT_SHADER_GOURAUD) {
+            const float3 na = v3(S, __ldg(T + 3)), nb = v3(S, __ldg(T + 4)), nc = v3(S, __ldg(T + 5));
+            const float3 tga = v3(S, __ldg(T + 9)), tgb = v3(S, __ldg(T + 10)), tgc = v3(S, __ldg(T + 11));
+            n0x = na.x * bw + nb.x * bu + nc.x * bv;
+            n0y = na.y * bw + nb.y * bu + nc.y * bv;
+            n0z = na.z * bw + nb.z * bu + nc.z * bv;
+            t0x = tga.x * bw + tgb.x * bu + tgc.x * bv;
+            t0y = tga.y * bw + tgb.y * bu + tgc.y * bv;
+            t0z = tga.z * bw + tgb.z * bu + tgc.z * bv;
+        }
+        const float nr = rsqrt_j(n0x * n0x + n0y * n0y + n0z * n0z);
+        s.nx = n0x * nr; s.ny = n0y * nr; s.nz = n0z * nr;
+        const float tr = rsqrt_j(t0x * t0x + t0y * t0y + t0z * t0z);
+        s.tx = t0x * tr; s.ty = t0y * tr; s.tz = t0z * tr;
+    }
+    // To world space: the point by object-to-world, directions by the transposed
+    // world-to-object (not renormalised).
+    const float wpx = m0.x * s.px + m0.y * s.py + m0.z * s.pz + m0.w;
+    const float wpy = m1.x * s.px + m1.y * s.py + m1.z * s.pz + m1.w;
+    const float wpz = m2.x * s.px + m2.y * s.py + m2.z * s.pz + m2.w;
+    const float wnx = w0.x * s.nx + w1.x * s.ny + w2.x * s.nz;
+    const float wny = w0.y * s.nx + w1.y * s.ny + w2.y * s.nz;
+    const float wnz = w0.z * s.nx + w1.z * s.ny + w2.z * s.nz;
+    const float wtx = w0.x * s.tx + w1.x * s.ty + w2.x * s.tz;
+    const float wty = w0.y * s.tx + w1.y * s.ty + w2.y * s.tz;
+    const float wtz = w0.z * s.tx + w1.z * s.ty + w2.z * s.tz;
+    s.px = wpx; s.py = wpy; s.pz = wpz;
+    s.nx = wnx; s.ny = wny; s.nz = wnz;
+    s.tx = wtx; s.ty = wty; s.tz = wtz;
+
+    const int4 info = __ldg(S.prim_info + h.prim);
+    const int so = info.z;
+    if (P.normal_mapping == 1) {
+        // Normal mapping via image texture (GRK:2714-2846).
+        const int nto = f2i(__ldg(S.surfaces + so + 3));
+        if (f2i(texf(S, nto)) == DFPT_TEXTURE_IMAGE) {
+            const int rgb = image_texture_simple(S, nto, s.u, s.v);
+            const float r = ((((rgb >> 16) & 0xFF) * COLOR_RECIPROCAL) - 0.5f) * 2.0f;
+            const float g = ((((rgb >> 8) & 0xFF) * COLOR_RECIPROCAL) - 0.5f) * 2.0f;
+            const float bb = ((((rgb >> 0) & 0xFF) * COLOR_RECIPROCAL) - 0.0f) * 2.0f;
+            const float wx = s.nx, wy = s.ny, wz = s.nz;
+            float sx, sy, sz;
+            if (info.x == DFPT_SHAPE_SPHERE) {
+                const float v0x = -2.0f * PI_F * wy, v0y = 2.0f * PI_F * wx, v0z = 0.0f;
+                const float u0x = v0y * wz - v0z * wy, u0y = v0z * wx - v0x * wz, u0z = v0x * wy - v0y * wx;
+                const float ur = rsqrt_j(u0x * u0x + u0y * u0y + u0z * u0z);
+                const float u1x = u0x * ur, u1y = u0y * ur, u1z = u0z * ur;
+                const float v1x = wy * u1z - wz * u1y, v1y = wz * u1x - wx * u1z, v1z = wx * u1y - wy * u1x;
+                const float vr = rsqrt_j(v1x * v1x + v1y * v1y + v1z * v1z);
+                const float v2x = v1x * vr, v2y = v1y * vr, v2z = v1z * vr;
+                sx = r * u1x + g * v2x + bb * wx; sy = r * u1y + g * v2y + bb * wy; sz = r * u1z + g * v2z + bb * wz;
+            } else if (info.x == DFPT_SHAPE_TRIANGLE) {
+                const float ux = s.tx, uy = s.ty, uz = s.tz;
+                const float v0x = wy * uz - wz * uy, v0y = wz * ux - wx * uz, v0z = wx * uy - wy * ux;
+                const float vr = rsqrt_j(v0x * v0x + v0y * v0y + v0z * v0z);
+                const float v1x = v0x * vr, v1y = v0y * vr, v1z = v0z * vr;
+                sx = r * ux + g * v1x + bb * wx; sy = r * uy + g * v1y + bb * wy; sz = r * uz + g * v1z + bb * wz;
+            } else {
+                const float awx = fabsf(wx), awy = fabsf(wy), awz = fabsf(wz);
+                const bool isWX = awx < awy && awx < awz;
+                const bool isWY = awy < awz;
+                const float v0x = isWX ? 0.0f : isWY ? wz : wy;
+                const float v0y = isWX ? wz : isWY ? 0.0f : -wx;
+                const float v0z = isWX ? -wy : isWY ? -wx : 0.0f;
+                const float vr = rsqrt_j(v0x * v0x + v0y * v0y + v0z * v0z);
+                const float v1x = v0x * vr, v1y = v0y * vr, v1z = v0z * vr;
+                const float u0x = v1y * wz - v1z * wy, u0y = v1z * wx - v1x * wz, u0z = v1x * wy - v1y * wx;
+                const float ur = rsqrt_j(u0x * u0x + u0y * u0y + u0z * u0z);
+                const float u1x = u0x * ur, u1y = u0y * ur, u1z = u0z * ur;
+                sx = r * u1x + g * v1x + bb * wx; sy = r * u1y + g * v1y + bb * wy; sz = r * u1z + g * v1z + bb * wz;
+            }
+            const float sr = rsqrt_j(sx * sx + sy * sy + sz * sz);
+            s.nx = sx * sr; s.ny = sy * sr; s.nz = sz * sr;
+        }
+        // Normal mapping via noise (GRK:2658-2712).
+        const float amount = __ldg(S.surfaces + so + 4), scale = __ldg(S.surfaces + so + 5);
+        if (amount > 0.0f && scale > 0.0f) {
+            const float sr = 1.0f / scale;
+            const float x1 = s.px * sr, y1 = s.py * sr, z1 = s.pz * sr;
+            const float nx = fbm3(scale, 0.5f, -0.26f, 0.26f, 16, x1, y1, z1);
+            const float ny = fbm3(scale, 0.5f, -0.26f, 0.26f, 16, y1, z1, x1);
+            const float nz = fbm3(scale, 0.5f, -0.26f, 0.26f, 16, z1, x1, y1);
+            const float qx = s.nx + nx * amount, qy = s.ny + ny * amount, qz = s.nz + nz * amount;
+            const float qr = rsqrt_j(qx * qx + qy * qy + qz * qz);
+            s.nx = qx * qr; s.ny = qy * qr; s.nz = qz * qr;
+        }
+    }
+    return s;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Textures: packed 0xRRGGBB (GRK:1596-1960).
+
+__device__ __forceinline__ int pack8(float r, float g, float b) {
+    const int ri = f2i(saturate_j(r, 0.0f, 1.0f) * 255.0f + 0.5f);
+    const int gi = f2i(saturate_j(g, 0.0f, 1.0f) * 255.0f + 0.5f);
+    const int bi = f2i(saturate_j(b, 0.0f, 1.0f) * 255.0f + 0.5f);
+    return ((ri & 0xFF) << 16) | ((gi & 0xFF) << 8) | (bi & 0xFF);
+}
+__device__ __forceinline__ float cr(int rgb) { return ((rgb >> 16) & 0xFF) * COLOR_RECIPROCAL; }
+__device__ __forceinline__ float cg(int rgb) { return ((rgb >> 8) & 0xFF) * COLOR_RECIPROCAL; }
+__device__ __forceinline__ float cb(int rgb) { return (rgb & 0xFF) * COLOR_RECIPROCAL; }
+
+__device__ int texture_leaf(const DevScene& S, int to, const Surf& s) {
+    const int type = f2i(texf(S, to));
+    if (type == DFPT_TEXTURE_BULLSEYE) {
+        const int ca = f2i(texf(S, to + 2)), cbb = f2i(texf(S, to + 3));
+        const float len = sqrtf(s.px * s.px + s.py * s.py + s.pz * s.pz);
+        const float value = remainder_j(len * 0.25f, 1.0f);
+        float r = value > 0.5f ? cr(ca) : cr(cbb);
+        float g = value > 0.5f ? cg(ca) : cg(cbb);
+        float b = value > 0.5f ? cb(ca) : cb(cbb);
+        const float m = value > 0.5f ? 0.8f : 1.2f;
+        if (cr(ca) == cr(cbb) && cg(ca) == cg(cbb) && cb(ca) == cb(cbb)) { r *= m; g *= m; b *= m; }
+        return pack8(r, g, b);
+    } else if (type == DFPT_TEXTURE_CHECKERBOARD) {
+        const int c0 = f2i(texf(S, to + 2)), c1 = f2i(texf(S, to + 3));
+        const float ca = texf(S, to + 4), sa = texf(S, to + 5), su = texf(S, to + 6), sv = texf(S, to + 7);
+        const float tu = modulo_j((s.u * ca - s.v * sa) * su);
+        const float tv = modulo_j((s.v * ca + s.u * sa) * sv);
+        const bool dark = (tu > 0.5f) ^ (tv > 0.5f);
+        const float m = dark ? 0.8f : 1.2f;
+        float r = dark ? cr(c0) : cr(c1), g = dark ? cg(c0) : cg(c1), b = dark ? cb(c0) : cb(c1);
+        if (cr(c0) == cr(c1) && cg(c0) == cg(c1) && cb(c0) == cb(c1)) { r *= m; g *= m; b *= m; }
+        return pack8(r, g, b);
+    } else if (type == DFPT_TEXTURE_CONSTANT) {
+        return f2i(texf(S, to + 2));
+    } else if (type == DFPT_TEXTURE_FBM) {
+        const int add = f2i(texf(S, to + 2)), mul = f2i(texf(S, to + 3));
+        const float noise = fbm3(texf(S, to + 4), texf(S, to + 5), 0.0f, 1.0f, f2i(texf(S, to + 6)), s.px, s.py, s.pz);
+        return pack8(noise * cr(mul) + cr(add), noise * cg(mul) + cg(add), noise * cb(mul) + cb(add));
+    } else if (type == DFPT_TEXTURE_IMAGE) {
+        const float width = texf(S, to + 4), height = texf(S, to + 5);
+        const float su = texf(S, to + 6), sv = texf(S, to + 7);
+        const float ca = texf(S, to + 2), sa = texf(S, to + 3);
+        const float u0 = (s.u * ca - s.v * sa), v0 = (s.v * ca + s.u * sa);
+        const float u1 = remainder_j(u0 * su * width, width), v1 = remainder_j(v0 * sv * height, height);
+        const float u2 = u1 >= 0.0f ? u1 : width - fabsf(u1);
+        const float v2 = v1 >= 0.0f ? v1 : height - fabsf(v1);
+        const int x = f2i(u2), y = f2i(v2);
+        const int w = f2i(width), res = f2i(width * height);
+        const int i00 = y * w + x, i01 = y * w + (x + 1), i10 = (y + 1) * w + x, i11 = (y + 1) * w + (x + 1);
+        const int c00 = i00 >= 0 && i00 < res ? f2i(texf(S, to + 8 + i00)) : 0;
+        const int c01 = i01 >= 0 && i01 < res ? f2i(texf(S, to + 8 + i01)) : 0;
+        const int c10 = i10 >= 0 && i10 < res ? f2i(texf(S, to + 8 + i10)) : 0;
+        const int c11 = i11 >= 0 && i11 < res ? f2i(texf(S, to + 8 + i11)) : 0;
+        const float fx = u2 - (float)x, fy = v2 - (float)y;
+        return pack8(blerp_j(cr(c00), cr(c01), cr(c10), cr(c11), fx, fy), blerp_j(cg(c00), cg(c01), cg(c10), cg(c11), fx, fy),
+                     blerp_j(cb(c00), cb(c01), cb(c10), cb(c11), fx, fy));
+    } else if (type == DFPT_TEXTURE_SURFACE_NORMAL) {
+        return pack8((s.nx + 1.0f) * 0.5f, (s.ny + 1.0f) * 0.5f, (s.nz + 1.0f) * 0.5f);
+    } else if (type == DFPT_TEXTURE_UV) {
+        return pack8(s.u, s.v, 0.0f);
+    }
+    return 0;
+}
+
+__device__ int texture_color(const DevScene& S, int to, const Surf& s) {
+    if (f2i(texf(S, to)) == DFPT_TEXTURE_BLEND) {
+        const int ta = f2i(texf(S, to + 2)), tb = f2i(texf(S, to + 3));
+        const float f = texf(S, to + 4);
+        const int a = texture_leaf(S, ta, s), b = texture_leaf(S, tb, s);
+        return pack8((1.0f - f) * cr(a) + f * cr(b), (1.0f - f) * cg(a) + f * cg(b), (1.0f - f) * cb(a) + f * cb(b));
+    }
+    return texture_leaf(S, to, s);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Perez sky (GRK:2127-2236), evaluated in FP32 on the device; the reference evaluates the
+// Perez functions in FP64. cos(acos(x)) is x on [-1, 1].
+__device__ float3 sky_color(const DevParams& P, float dx, float dy, float dz) {
+    float d0x = dx * P.sky_u[0] + dy * P.sky_u[1] + dz * P.sky_u[2];
+    float d0y = dx * P.sky_v[0] + dy * P.sky_v[1] + dz * P.sky_v[2];
+    float d0z = dx * P.sky_w[0] + dy * P.sky_w[1] + dz * P.sky_w[2];
+    float3 c = make_float3(0.01f, 0.01f, 0.01f);
+    if (d0z >= 0.0f && P.sky_active == 1) {
+        d0z = jmax(d0z, 0.001f);
+        const float lr = rsqrt_j(d0x * d0x + d0y * d0y + d0z * d0z);
+        const float d1x = d0x * lr, d1y = d0y * lr, d1z = d0z * lr;
+        const float dp = d1x * P.sun_dir[0] + d1y * P.sun_dir[1] + d1z * P.sun_dir[2];
+        const float cos1 = fminf(fmaxf(d1z, -1.0f), 1.0f);
+        const float theta1 = acosf(cos1);
+        const float cos1r = 1.0f / (cos1 + 0.01f);
+        const float cosg = fminf(fmaxf(dp, -1.0f), 1.0f);
+        const float gamma = acosf(cosg);
+        const float c0sq = P.cos_theta0 * P.cos_theta0;
+        const float num_l = (1.0f + P.perez_l[0] * expf(P.perez_l[1] * cos1r)) * (1.0f + P.perez_l[2] * expf(P.perez_l[3] * gamma) + P.perez_l[4] * cosg * cosg);
+        const float rel_l = P.zenith_l * num_l / P.den_l * 1.0e-4f;
+        const float den_x = P.den_x_a * (1.0f + P.perez_x[2] * expf(P.perez_x[3] * theta1) + P.perez_x[4] * c0sq);
+        const float num_x = (1.0f + P.perez_x[0] * expf(P.perez_x[1] * cos1r)) * (1.0f + P.perez_x[2] * expf(P.perez_x[3] * gamma) + P.perez_x[4] * cosg * cosg);
+        const float x = P.zenith_x * num_x / den_x;
+        const float den_y = P.den_y_a * (1.0f + P.perez_y[2] * expf(P.perez_y[3] * theta1) + P.perez_y[4] * c0sq);
+        const float num_y = (1.0f + P.perez_y[0] * expf(P.perez_y[1] * cos1r)) * (1.0f + P.perez_y[2] * expf(P.perez_y[3] * gamma) + P.perez_y[4] * cosg * cosg);
+        const float y = P.zenith_y * num_y / den_y;
+        const float c0 = 1.0f / (0.0241f + 0.2562f * x - 0.7341f * y);
+        const float c1 = (-1.3515f - 1.7703f * x + 5.9114f * y) * c0;
+        const float c2 = (0.03f - 31.4424f * x + 30.0717f * y) * c0;
+        const float X = 10246.121f + c1 * 187.75537f + c2 * 213.14803f;
+        const float Y = 10676.695f + c1 * 192.59653f + c2 * 76.29494f;
+        const float Z = 12372.504f + c1 * 3482.8765f + c2 * -235.71611f;
+        const float Yr = 1.0f / Y;
+        const float R = X * rel_l * Yr, G = rel_l, B = Z * rel_l * Yr;
+        float r = 3.2410042f * R + -1.5373994f * G + -0.49861607f * B;
+        float g = -0.9692241f * R + 1.8759298f * G + 0.041554242f * B;
+        float b = 0.05563942f * R + -0.20401107f * G + 1.0571486f * B;
+        const float w = jmax(0.0f, -jmin(0.0f, jmin(r, jmin(g, b))));
+        c = make_float3(r + w, g + w, b + w);
+    }
+    return c;
+}
+
+// Sun sample of doCalculateColorForSun (GRK:2238-2347): a direction in the 500-radius cone
+// around the sun direction; returns false when the sample faces away from the sun or surface.
+__device__ bool sun_sample(const DevParams& P, float px, float py, float pz, float nx, float ny, float nz, float u, float v,
+                           float& ldx, float& ldy, float& ldz, float& dot1) {
+    const float sr2 = 500.0f * 500.0f;
+    const float tx = P.sun_origin[0] - px, ty = P.sun_origin[1] - py, tz = P.sun_origin[2] - pz;
+    const float tl2 = tx * tx + ty * ty + tz * tz;
+    const float sin2 = sr2 / tl2;
+    const float cos_max = sqrtf(jmax(0.0f, 1.0f - sin2));
+    const float cos_t = u * (cos_max - 1.0f) + 1.0f;
+    const float sin_t = sqrtf(jmax(0.0f, 1.0f - cos_t * cos_t));
+    const float phi = TWO_PI * v;
+    const float x = cosf(phi) * sin_t, y = sinf(phi) * sin_t, z = cos_t;
+    const float wx = P.sun_dir_world[0], wy = P.sun_dir_world[1], wz = P.sun_dir_world[2];
+    const float ax = fabsf(wx), ay = fabsf(wy), az = fabsf(wz);
+    const float vx = ax < ay && ax < az ? 0.0f : ay < az ? wz : wy;
+    const float vy = ax < ay && ax < az ? wz : ay < az ? 0.0f : -wx;
+    const float vz = ax < ay && ax < az ? -wy : ay < az ? -wx : 0.0f;
+    const float vr = rsqrt_j(vx * vx + vy * vy + vz * vz);
+    const float vnx = vx * vr, vny = vy * vr, vnz = vz * vr;
+    const float unx = vny * wz - vnz * wy, uny = vnz * wx - vnx * wz, unz = vnx * wy - vny * wx;
+    const float rx = unx * x + vnx * y + wx * z;
+    const float ry = uny * x + vny * y + wy * z;
+    const float rz = unz * x + vnz * y + wz * z;
+    const float rr = rsqrt_j(rx * rx + ry * ry + rz * rz);
+    ldx = rx * rr; ldy = ry * rr; ldz = rz * rr;
+    const float dot0 = ldx * wx + ldy * wy + ldz * wz;
+    dot1 = ldx * nx + ldy * ny + ldz * nz;
+    return dot0 > 0.0f && dot1 > 0.0f;
+}
+
+// Cosine-weighted hemisphere direction around w (GRK:3466-3500).
+__device__ __forceinline__ void cosine_dir(float wx, float wy, float wz, float u, float v, float& ox, float& oy, float& oz) {
+    const float phi = TWO_PI * u;
+    const float ct = sqrtf(v), st = sqrtf(1.0f - v);
+    const float x = cosf(phi) * st, y = sinf(phi) * st, z = ct;
+    const bool isY = fabsf(wx) > 0.1f;
+    const float ux = (isY ? 1.0f : 0.0f) * wz;
+    const float uy = -((isY ? 0.0f : 1.0f) * wz);
+    const float uz = (isY ? 0.0f : 1.0f) * wy - (isY ? 1.0f : 0.0f) * wx;
+    const float ur = rsqrt_j(ux * ux + uy * uy + uz * uz);
+    const float unx = ux * ur, uny = uy * ur, unz = uz * ur;
+    const float vnx = wy * unz - wz * uny, vny = wz * unx - wx * unz, vnz = wx * uny - wy * unx;
+    const float dx = unx * x + vnx * y + wx * z;
+    const float dy = uny * x + vny * y + wy * z;
+    const float dz = unz * x + vnz * y + wz * z;
+    const float dr = rsqrt_j(dx * dx + dy * dy + dz * dz);
+    ox = dx * dr; oy = dy * dr; oz = dz * dr;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Camera ray (GRK:573-724). Returns false for pixels outside a fisheye lens.
+__device__ bool primary_ray(const DevScene& S, const DevParams& P, int pixel, bool jitter, Rng& rng, float4& o, float4& d) {
+    const int y = pixel / P.width;
+    const int x = pixel - y * P.width;
+    const float* C = S.camera;
+    const float ex = __ldg(C + 1), ey = __ldg(C + 2), ez = __ldg(C + 3);
+    const float ux = __ldg(C + 7), uy = __ldg(C + 8), uz = __ldg(C + 9);
+    const float vx = __ldg(C + 10), vy = __ldg(C + 11), vz = __ldg(C + 12);
+    const float wx = __ldg(C + 13), wy = __ldg(C + 14), wz = __ldg(C + 15);
+    const float fx = tanf(__ldg(C + 4) * 0.5f * PI_OVER_180);
+    const float fy = tanf(-__ldg(C + 5) * 0.5f * PI_OVER_180);
+    const float hx = ux * fx, hy = uy * fx, hz = uz * fx;
+    const float gx = vx * fy, gy = vy * fy, gz = vz * fy;
+    float sx = 0.5f, sy = 0.5f;
+    if (jitter) {
+        sx = rng.next();
+        sy = rng.next();
+        sx = sx < 0.5f ? sqrtf(2.0f * sx) - 1.0f : 1.0f - sqrtf(2.0f - 2.0f * sx);
+        sy = sy < 0.5f ? sqrtf(2.0f * sy) - 1.0f : 1.0f - sqrtf(2.0f - 2.0f * sy);
+    }
+    const float psx = (sx + (float)x) / (__ldg(C + 16) - 1.0f);
+    const float psy = (sy + (float)y) / (__ldg(C + 17) - 1.0f);
+    const float sx0 = 2.0f * psx - 1.0f, sy0 = 2.0f * psy - 1.0f;
+    float w = 1.0f;
+    if (__ldg(C + 18) == 2.0f) {
+        const float dp = sx0 * sx0 + sy0 * sy0;
+        if (dp > 1.0f) return false;
+        w = sqrtf(1.0f - dp);
+    }
+    const float mx = ex + wx * w, my = ey + wy * w, mz = ez + wz * w;
+    const float qx = mx + (hx * sx0) + (gx * sy0);
+    const float qy = my + (hy * sx0) + (gy * sy0);
+    const float qz = mz + (hz * sx0) + (gz * sy0);
+    const float focal = __ldg(C + 6);
+    const float ipx = ex + (qx - ex) * focal, ipy = ey + (qy - ey) * focal, ipz = ez + (qz - ez) * focal;
+    const float aperture = __ldg(C + 0);
+    float apx = ex, apy = ey, apz = ez;
+    if (aperture > 0.00001f) {
+        const float r1 = rng.next(), r2 = rng.next();
+        const float angle = TWO_PI * r1;
+        const float dist = aperture * sqrtf(r2);
+        const float ax = cosf(angle) * dist, ay = sinf(angle) * dist;
+        apx = ex + ux * ax + vx * ay;
+        apy = ey + uy * ax + vy * ay;
+        apz = ez + uz * ax + vz * ay;
+    }
+    const float tx = ipx - apx, ty = ipy - apy, tz = ipz - apz;
+    const float tr = rsqrt_j(tx * tx + ty * ty + tz * tz);
+    o = make_float4(apx, apy, apz, 0.0f);
+    d = make_float4(tx * tr, ty * tr, tz * tr, 0.0f);
+    return true;
+}
+
+// Warp-aggregated queue append: one atomic per warp; returns the slot or -1. Every lane of the
+// warp must call it.
+__device__ __forceinline__ int warp_push(int* counter, bool active) {
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, active);
+    if (mask == 0u) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return active ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
+}
+
+__device__ __forceinline__ void warp_add_stats(const DevParams& P, unsigned long long* stats, int which, uint32_t a, uint32_t b, uint32_t c) {
+    if (!P.counting) return;
+    const unsigned long long sa = __reduce_add_sync(0xFFFFFFFFu, a);
+    const unsigned long long sb = __reduce_add_sync(0xFFFFFFFFu, b);
+    const unsigned long long sc = __reduce_add_sync(0xFFFFFFFFu, c);
+    if ((threadIdx.x & 31) == 0) {
+        if (sa) atomicAdd(stats + which, sa);
+        if (sb) atomicAdd(stats + 2, sb);
+        if (sc) atomicAdd(stats + 3, sc);
+    }
+}
+
+#define GRID_STRIDE_UNIFORM(i, n)                                                              \
+    for (int i##_base = blockIdx.x * blockDim.x; i##_base < (n); i##_base += gridDim.x * blockDim.x) \
+        for (int i = i##_base + (int)threadIdx.x, i##_once = 1; i##_once; i##_once = 0)
+
+// ---------------------------------------------------------------------------------------------
+// Path tracer wavefront (doRenderWithPathTracer, GRK:3151-3705).
+
+__global__ void __launch_bounds__(256) k_camera(DevScene S, const DevParams* __restrict__ Pp, DevPass B) {
+    const DevParams& P = *Pp;
+    const int n = B.n_pixels;
+    const uint32_t pass = (uint32_t)*B.pass_index;
+    const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
+                    (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
+    GRID_STRIDE_UNIFORM(i, n) {
+        const bool valid = i < n;
+        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 0, 0);
+        bool live = false;
+        if (valid) {
+            Rng rng = make_rng(P, (uint32_t)i, pass, P.rng_kind == DFPT_RNG_LCG ? B.rng[i] : 0ull);
+            live = primary_ray(S, P, i, pt, rng, o, d);
+            B.rng[i] = rng.state;
+            B.pixel_flags[i] = live ? 0 : 1;
+            B.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            B.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (P.wireframes == 1) {
+                B.primary_o[i] = o;
+                B.primary_d[i] = d;
+            }
+        }
+        const int slot = warp_push(B.counts + 0, live);
+        if (slot >= 0) {
+            o.w = __int_as_float(i);
+            B.q_o[0][slot] = o;
+            B.q_d[0][slot] = d;
+        }
+    }
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(256) k_trace(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce, int which_queue) {
+    const DevParams& P = *Pp;
+    const int n = B.counts[bounce];
+    const float4* __restrict__ qo = B.q_o[which_queue];
+    const float4* __restrict__ qd = B.q_d[which_queue];
+    GRID_STRIDE_UNIFORM(i, n) {
+        TraceStats st{0, 0};
+        if (i < n) {
+            const float4 o = qo[i], d = qd[i];
+            const Hit h = trace<ANY>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
+        }
+        warp_add_stats(P, B.stats, ANY ? 1 : 0, i < n ? 1u : 0u, st.nodes, st.tris);
+    }
+}
+
+// One bounce of shading: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
+// roulette, material sampling and the next ray (GRK:3185-3686).
+__global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+    const DevParams& P = *Pp;
+    const int n = B.counts[bounce];
+    const int qi = bounce & 1;
+    const uint32_t pass = (uint32_t)*B.pass_index;
+    const int depth_max = P.depth_max;
+    GRID_STRIDE_UNIFORM(i, n) {
+        bool emit_next = false, emit_shadow = false;
+        float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
+        float4 so = make_float4(0, 0, 0, 0), sd = make_float4(0, 0, 0, 0), sc = make_float4(0, 0, 0, 0);
+        int path = 0;
+        if (i < n) {
+            const float4 o4 = B.q_o[qi][i], d4 = B.q_d[qi][i];
+            path = __float_as_int(o4.w);
+            const int4 hr = B.q_hit[i];
+            Hit h;
+            h.t = __int_as_float(hr.x);
+            h.prim = hr.y;
+            h.shape_type = hr.z;
+            h.shape_offset = hr.w;
+            float4 T = B.throughput[path];
+            float4 L = B.radiance[path];
+            if (bounce == 0) B.primitive_offsets[path] = h.prim >= 0 ? h.prim * 3 : -1;
+            if (h.t == INF || h.prim == -1) {
+                const float3 sky = sky_color(P, d4.x, d4.y, d4.z);
+                L.x += T.x * sky.x * INV_PI;
+                L.y += T.y * sky.y * INV_PI;
+                L.z += T.z * sky.z * INV_PI;
+                B.radiance[path] = L;
+                if (bounce == 0 && P.record_hits) {
+                    B.hit_prim_offset[path] = -1; B.hit_shape_type[path] = -1; B.hit_shape_offset[path] = -1;
+                    B.hit_distance[path] = INF;
+                }
+            } else {
+                Rng rng = make_rng(P, (uint32_t)path, pass, B.rng[path]);
+                const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
+                if (bounce == 0 && P.record_hits) {
+                    B.hit_prim_offset[path] = h.prim * 3; B.hit_shape_type[path] = h.shape_type; B.hit_shape_offset[path] = h.shape_offset;
+                    B.hit_distance[path] = h.t;
+                    B.hit_normal[3 * path] = s.nx; B.hit_normal[3 * path + 1] = s.ny; B.hit_normal[3 * path + 2] = s.nz;
+                }
+                const int so_off = __ldg(S.prim_info + h.prim).z;
+                const float dp = s.nx * d4.x + s.ny * d4.y + s.nz * d4.z;
+                const float dp2 = dp * 2.0f;
+                const bool correct = dp < 0.0f;
+                const float wx = correct ? s.nx : -s.nx, wy = correct ? s.ny : -s.ny, wz = correct ? s.nz : -s.nz;
+                const int albedo = texture_color(S, f2i(__ldg(S.surfaces + so_off + 1)), s);
+                const int emission = texture_color(S, f2i(__ldg(S.surfaces + so_off + 2)), s);
+                float ar = cr(albedo), ag = cg(albedo), ab = cb(albedo);
+                const float er = cr(emission), eg = cg(emission), eb = cb(emission);
+                const int material = f2i(__ldg(S.surfaces + so_off + 0));
+                if ((material == DFPT_MATERIAL_CLEAR_COAT || material == DFPT_MATERIAL_LAMBERTIAN || material == DFPT_MATERIAL_PHONG) &&
+                    P.sun_active == 1) {
+                    const float u = rng.next(), v = rng.next();
+                    float lx, ly, lz, dot1;
+                    if (sun_sample(P, s.px, s.py, s.pz, wx, wy, wz, u, v, lx, ly, lz, dot1)) {
+                        emit_shadow = true;
+                        so = make_float4(s.px, s.py, s.pz, __int_as_float(path));
+                        sd = make_float4(lx, ly, lz, 0.0f);
+                        sc = make_float4(T.x * (ar * 1.0f * dot1 * INV_PI), T.y * (ag * 1.0f * dot1 * INV_PI), T.z * (ab * 1.0f * dot1 * INV_PI), 0.0f);
+                    }
+                }
+                L.x += T.x * er;
+                L.y += T.y * eg;
+                L.z += T.z * eb;
+                const int depth = bounce + 1;
+                bool alive = true;
+                if (depth >= P.depth_rr) {
+                    const float q = jmax(ar, jmax(ag, ab));
+                    const float r = rng.next();
+                    // The reference then tests the same ray for any hit; it just hit, so the
+                    // test always hits and adds no sky (GRK:3293-3311).
+                    if (r >= q) alive = false;
+                    else {
+                        const float qr = 1.0f / q;
+                        ar *= qr; ag *= qr; ab *= qr;
+                    }
+                }
+                if (alive) {
+                    float ox = o4.x, oy = o4.y, oz = o4.z, dx = d4.x, dy = d4.y, dz = d4.z;
+                    const float rx = dx - s.nx * dp2, ry = dy - s.ny * dp2, rz = dz - s.nz * dp2;
+                    if (material == DFPT_MATERIAL_CLEAR_COAT) {
+                        const float a = 1.5f - 1.0f, b = 1.5f + 1.0f, c = 1.0f / 1.5f;
+                        const float e = (a * a) / (b * b);
+                        const float d0 = wx * dx + wy * dy + wz * dz;
+                        const float tir = 1.0f - c * c * (1.0f - d0 * d0);
+                        if (tir < 0.0f) {
+                            ox = s.px + wx * 0.02f; oy = s.py + wy * 0.02f; oz = s.pz + wz * 0.02f;
+                            dx = rx; dy = ry; dz = rz;
+                        } else {
+                            const float a2 = 1.0f - (-d0);
+                            const float refl = e + (1.0f - e) * a2 * a2 * a2 * a2 * a2;
+                            const float trans = 1.0f - refl;
+                            const float pr = 0.25f + 0.5f * refl;
+                            const float rp = refl / pr, tp = trans / (1.0f - pr);
+                            const bool is_refl = rng.next() < pr;
+                            const float m = is_refl ? rp : tp;
+                            T.x *= m; T.y *= m; T.z *= m;
+                            if (is_refl) {
+                                ox = s.px + wx * 0.02f; oy = s.py + wy * 0.02f; oz = s.pz + wz * 0.02f;
+                                dx = rx; dy = ry; dz = rz;
+                            } else {
+                                const float u = rng.next(), v = rng.next();
+                                cosine_dir(wx, wy, wz, u, v, dx, dy, dz);
+                                ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
+                                T.x *= ar; T.y *= ag; T.z *= ab;
+                            }
+                        }
+                    } else if (material == DFPT_MATERIAL_LAMBERTIAN) {
+                        const float u = rng.next(), v = rng.next();
+                        cosine_dir(wx, wy, wz, u, v, dx, dy, dz);
+                        ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
+                        T.x *= ar; T.y *= ag; T.z *= ab;
+                    } else if (material == DFPT_MATERIAL_PHONG) {
+                        const float u = rng.next(), v = rng.next();
+                        const float phi = TWO_PI * u;
+                        const float ct = powf(1.0f - v, 1.0f / (50.0f + 1.0f));
+                        const float st = sqrtf(jmax(0.0f, 1.0f - ct * ct));
+                        const float x = cosf(phi) * st, y = sinf(phi) * st, z = ct;
+                        const float rwr = rsqrt_j(rx * rx + ry * ry + rz * rz);
+                        const float rnx = rx * rwr, rny = ry * rwr, rnz = rz * rwr;
+                        const bool isY = fabsf(rnx) > 0.1f;
+                        const float ux = (isY ? 1.0f : 0.0f) * rnz;
+                        const float uy = -((isY ? 0.0f : 1.0f) * rnz);
+                        const float uz = (isY ? 0.0f : 1.0f) * rny - (isY ? 1.0f : 0.0f) * rnx;
+                        const float ur = rsqrt_j(ux * ux + uy * uy + uz * uz);
+                        const float unx = ux * ur, uny = uy * ur, unz = uz * ur;
+                        const float vnx = rny * unz - rnz * uny, vny = rnz * unx - rnx * unz, vnz = rnx * uny - rny * unx;
+                        // The reference mixes the unnormalised reflection vector in here (GRK:3555-3557).
+                        const float px = unx * x + vnx * y + rx * z;
+                        const float py = uny * x + vny * y + ry * z;
+                        const float pz = unz * x + vnz * y + rz * z;
+                        const float pr = rsqrt_j(px * px + py * py + pz * pz);
+                        ox = s.px + rnx * 0.01f; oy = s.py + rny * 0.01f; oz = s.pz + rnz * 0.01f;
+                        dx = px * pr; dy = py * pr; dz = pz * pr;
+                        T.x *= ar; T.y *= ag; T.z *= ab;
+                    } else if (material == DFPT_MATERIAL_GLASS) {
+                        const float a = 1.5f - 1.0f, b = 1.5f + 1.0f, c = 1.0f / 1.5f, dd = 1.5f / 1.0f;
+                        const float e = (a * a) / (b * b);
+                        const bool going_in = s.nx * wx + s.ny * wy + s.nz * wz > 0.0f;
+                        const float nnt = going_in ? c : dd;
+                        const float dw = wx * dx + wy * dy + wz * dz;
+                        const float tir = 1.0f - nnt * nnt * (1.0f - dw * dw);
+                        if (tir < 0.0f) {
+                            ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
+                            dx = rx; dy = ry; dz = rz;
+                        } else {
+                            const float st = sqrtf(tir);
+                            const float scl = going_in ? dw * nnt + st : -(dw * nnt + st);
+                            const float t0x = dx * nnt - s.nx * scl, t0y = dy * nnt - s.ny * scl, t0z = dz * nnt - s.nz * scl;
+                            const float tr = rsqrt_j(t0x * t0x + t0y * t0y + t0z * t0z);
+                            const float tdx = t0x * tr, tdy = t0y * tr, tdz = t0z * tr;
+                            const float a1 = going_in ? -dw : tdx * s.nx + tdy * s.ny + tdz * s.nz;
+                            const float a2 = 1.0f - a1;
+                            const float refl = e + (1.0f - e) * a2 * a2 * a2 * a2 * a2;
+                            const float trans = 1.0f - refl;
+                            const float pr = 0.25f + 0.5f * refl;
+                            const float rp = refl / pr, tp = trans / (1.0f - pr);
+                            const bool is_refl = rng.next() < pr;
+                            const float m = is_refl ? rp : tp;
+                            T.x *= m; T.y *= m; T.z *= m;
+                            const float eps = is_refl ? 0.01f : 0.000001f;
+                            ox = s.px + wx * eps; oy = s.py + wy * eps; oz = s.pz + wz * eps;
+                            dx = is_refl ? rx : tdx; dy = is_refl ? ry : tdy; dz = is_refl ? rz : tdz;
+                        }
+                    } else if (material == DFPT_MATERIAL_REFLECTION) {
+                        ox = s.px + s.nx * 0.000001f; oy = s.py + s.ny * 0.000001f; oz = s.pz + s.nz * 0.000001f;
+                        dx = rx; dy = ry; dz = rz;
+                        T.x *= ar; T.y *= ag; T.z *= ab;
+                    }
+                    emit_next = true;
+                    no = make_float4(ox, oy, oz, __int_as_float(path));
+                    nd = make_float4(dx, dy, dz, 0.0f);
+                    (void)depth_max;
+                }
+                B.throughput[path] = T;
+                B.radiance[path] = L;
+                B.rng[path] = rng.state;
+            }
+        }
+        const int slot = warp_push(B.counts + bounce + 1, emit_next);
+        if (slot >= 0) {
+            B.q_o[qi ^ 1][slot] = no;
+            B.q_d[qi ^ 1][slot] = nd;
+        }
+        const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW + bounce, emit_shadow);
+        if (sslot >= 0) {
+            B.s_o[sslot] = so;
+            B.s_d[sslot] = sd;
+            B.s_c[sslot] = sc;
+        }
+    }
+}
+
+// Sun visibility: any hit (GRK:2324-2340); unoccluded samples add their contribution.
+__global__ void __launch_bounds__(256) k_shadow(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+    const DevParams& P = *Pp;
+    const int n = B.counts[DFPT_COUNTS_SHADOW + bounce];
+    GRID_STRIDE_UNIFORM(i, n) {
+        TraceStats st{0, 0};
+        if (i < n) {
+            const float4 o = B.s_o[i], d = B.s_d[i];
+            const Hit h = trace<true>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            if (h.t >= INF - 0.0001f) {
+                const int path = __float_as_int(o.w);
+                const float4 c = B.s_c[i];
+                float4 L = B.radiance[path];
+                L.x += c.x; L.y += c.y; L.z += c.z;
+                B.radiance[path] = L;
+            }
+        }
+        warp_add_stats(P, B.stats, 1, i < n ? 1u : 0u, st.nodes, st.tris);
+    }
+}
+
+// After the last bounce: any-hit test of the continuation ray, sky if it escapes (GRK:3689-3701).
+__global__ void __launch_bounds__(256) k_final(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+    const DevParams& P = *Pp;
+    const int n = B.counts[bounce];
+    const int qi = bounce & 1;
+    GRID_STRIDE_UNIFORM(i, n) {
+        TraceStats st{0, 0};
+        if (i < n) {
+            const float4 o = B.q_o[qi][i], d = B.q_d[qi][i];
+            const Hit h = trace<true>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            if (!(h.t < INF)) {
+                const int path = __float_as_int(o.w);
+                const float4 T = B.throughput[path];
+                const float3 sky = sky_color(P, d.x, d.y, d.z);
+                float4 L = B.radiance[path];
+                L.x += T.x * sky.x * INV_PI;
+                L.y += T.y * sky.y * INV_PI;
+                L.z += T.z * sky.z * INV_PI;
+                B.radiance[path] = L;
+            }
+        }
+        warp_add_stats(P, B.stats, 1, i < n ? 1u : 0u, st.nodes, st.tris);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// The per-pixel modes: ray caster, ambient occlusion, surface normals, ray tracer, ray marcher.
+
+// doShaderPhongReflectionModel0 (GRK:1962-2039), with the reference's closest-hit shadow test.
+__device__ int phong0(const DevScene& S, const DevParams& P, bool test, float px, float py, float pz, float nx, float ny, float nz,
+                      float vx, float vy, float vz, float ar, float ag, float ab, TraceStats& st) {
+    float r = 0.0f, g = 0.0f, b = 0.0f;
+    r += ar * 0.2f * 1.0f; g += ag * 0.2f * 1.0f; b += ab * 0.2f * 1.0f;
+    const float lx = P.sun_origin[0] - px, ly = P.sun_origin[1] - py, lz = P.sun_origin[2] - pz;
+    const float l2 = lx * lx + ly * ly + lz * lz;
+    const float ll = sqrtf(l2);
+    const float lr = 1.0f / ll;
+    const float lnx = lx * lr, lny = ly * lr, lnz = lz * lr;
+    float t = INF;
+    if (test) t = trace<false>(S, px, py, pz, lnx, lny, lnz, st).t;
+    if (t >= INF || t > l2) {
+        const float ldn = lnx * nx + lny * ny + lnz * nz;
+        r += ar * 0.5f * jmax(ldn, 0.0f) * 1.0f;
+        g += ag * 0.5f * jmax(ldn, 0.0f) * 1.0f;
+        b += ab * 0.5f * jmax(ldn, 0.0f) * 1.0f;
+        if (ldn > 0.0f) {
+            const float rx = 2.0f * ldn * nx - lnx, ry = 2.0f * ldn * ny - lny, rz = 2.0f * ldn * nz - lnz;
+            const float rr = rsqrt_j(rx * rx + ry * ry + rz * rz);
+            const float rdv = rx * rr * vx + ry * rr * vy + rz * rr * vz;
+            const float sh = powf(jmax(rdv, 0.0f), 250.0f);
+            r += 0.5f * sh * 1.0f; g += 0.5f * sh * 1.0f; b += 0.5f * sh * 1.0f;
+        }
+    }
+    r = saturate_j(r, 0.0f, 1.0f); g = saturate_j(g, 0.0f, 1.0f); b = saturate_j(b, 0.0f, 1.0f);
+    return ((f2i(r * 255.0f + 0.5f) & 0xFF) << 16) | ((f2i(g * 255.0f + 0.5f) & 0xFF) << 8) | (f2i(b * 255.0f + 0.5f) & 0xFF);
+}
+
+__device__ __forceinline__ void record_primary(const DevParams& P, DevPass& B, int pixel, const Hit& h, const Surf* s) {
+    if (!P.record_hits) return;
+    B.hit_prim_offset[pixel] = h.prim >= 0 ? h.prim * 3 : -1;
+    B.hit_shape_type[pixel] = h.prim >= 0 ? h.shape_type : -1;
+    B.hit_shape_offset[pixel] = h.prim >= 0 ? h.shape_offset : -1;
+    B.hit_distance[pixel] = h.t;
+    if (s) {
+        B.hit_normal[3 * pixel] = s->nx; B.hit_normal[3 * pixel + 1] = s->ny; B.hit_normal[3 * pixel + 2] = s->nz;
+    }
+}
+
+__device__ float height_rm(const DevParams& P, float x, float z) {
+    return fractal2(P.g_amplitude, P.g_frequency, P.g_gain, P.g_lacunarity, P.g_octaves, x, z);
+}
+
+__global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __restrict__ Pp, DevPass B) {
+    const DevParams& P = *Pp;
+    const int n = B.n_pixels;
+    const uint32_t pass = (uint32_t)*B.pass_index;
+    const int mode = P.renderer_type;
+    GRID_STRIDE_UNIFORM(i, n) {
+        TraceStats st{0, 0};
+        uint32_t segs = 0;
+        if (i < n) {
+            Rng rng = make_rng(P, (uint32_t)i, pass, P.rng_kind == DFPT_RNG_LCG ? B.rng[i] : 0ull);
+            float4 o4, d4;
+            const bool live = primary_ray(S, P, i, false, rng, o4, d4);
+            B.pixel_flags[i] = live ? 0 : 1;
+            if (P.wireframes == 1) { B.primary_o[i] = o4; B.primary_d[i] = d4; }
+            float cr_ = 0.0f, cg_ = 0.0f, cb_ = 0.0f;
+            if (live) {
+                float ox = o4.x, oy = o4.y, oz = o4.z, dx = d4.x, dy = d4.y, dz = d4.z;
+                if (mode == DFPT_RENDERER_RAY_MARCHER) {
+                    // doRenderWithRayMarcher (GRK:3802-3864)
+                    oy = height_rm(P, ox, oz) + 0.1f;
+                    const float max_t = jmax(oy, 1.0f) * 20.0f;
+                    const float3 sky = sky_color(P, dx, dy, dz);
+                    cr_ = sky.x; cg_ = sky.y; cb_ = sky.z;
+                    float del_t = 0.01f;
+                    for (float t = 0.001f; t < max_t; t += del_t) {
+                        const float px = ox + dx * t, py = oy + dy * t, pz = oz + dz * t;
+                        const float hh = height_rm(P, px, pz);
+                        if (py < hh) {
+                            const float nx = height_rm(P, px - EPSILON_AK, pz) - height_rm(P, px + EPSILON_AK, pz);
+                            const float ny = 2.0f * EPSILON_AK;
+                            const float nz = height_rm(P, px, pz - EPSILON_AK) - height_rm(P, px, pz + EPSILON_AK);
+                            const float nr = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+                            const float noise = fbm3(8.0f, 0.5f, 0.0f, 1.0f, 16, px, py, pz);
+                            const float al = saturate_j(noise * 1.0f + 0.1f, 0.0f, 1.0f);
+                            const int c = phong0(S, P, false, px, py, pz, nx * nr, ny * nr, nz * nr, -dx, -dy, -dz, al, al, al, st);
+                            cr_ = cr(c); cg_ = cg(c); cb_ = cb(c);
+                            t = max_t;
+                        }
+                        del_t = 0.01f * t;
+                    }
+                } else {
+                    const int depth_max = mode == DFPT_RENDERER_RAY_TRACER ? 5 : 1;
+                    for (int depth = 0; depth < depth_max; ++depth) {
+                        const Hit h = trace<false>(S, ox, oy, oz, dx, dy, dz, st);
+                        segs++;
+                        if (depth == 0) B.primitive_offsets[i] = h.prim >= 0 ? h.prim * 3 : -1;
+                        if (h.t == INF || h.prim == -1) {
+                            if (depth == 0) record_primary(P, B, i, h, nullptr);
+                            if (mode != DFPT_RENDERER_AMBIENT_OCCLUSION) {
+                                const float3 sky = sky_color(P, dx, dy, dz);
+                                cr_ += sky.x; cg_ += sky.y; cb_ += sky.z;
+                            }
+                            break;
+                        }
+                        const Surf s = surface(S, P, ox, oy, oz, dx, dy, dz, h);
+                        if (depth == 0) record_primary(P, B, i, h, &s);
+                        if (mode == DFPT_RENDERER_SURFACE_NORMALS) {
+                            cr_ = (s.nx + 1.0f) * 0.5f; cg_ = (s.ny + 1.0f) * 0.5f; cb_ = (s.nz + 1.0f) * 0.5f;
+                            break;
+                        }
+                        const float dp = s.nx * dx + s.ny * dy + s.nz * dz;
+                        const bool correct = dp < 0.0f;
+                        const float wx = correct ? s.nx : -s.nx, wy = correct ? s.ny : -s.ny, wz = correct ? s.nz : -s.nz;
+                        if (mode == DFPT_RENDERER_AMBIENT_OCCLUSION) {
+                            // doRenderWithAmbientOcclusion (GRK:3029-3149)
+                            const float w0r = rsqrt_j(wx * wx + wy * wy + wz * wz);
+                            const float w1x = wx * w0r, w1y = wy * w0r, w1z = wz * w0r;
+                            const bool isY = fabsf(w1x) > 0.1f;
+                            const float u0x = isY ? 0.0f : 1.0f, u0y = isY ? 1.0f : 0.0f;
+                            const float u1x = u0y * w1z, u1y = -(u0x * w1z), u1z = u0x * w1y - u0y * w1x;
+                            const float ur = rsqrt_j(u1x * u1x + u1y * u1y + u1z * u1z);
+                            const float u2x = u1x * ur, u2y = u1y * ur, u2z = u1z * ur;
+                            const float v0x = w1y * u2z - w1z * u2y, v0y = w1z * u2x - w1x * u2z, v0z = w1x * u2y - w1y * u2x;
+                            const float xi = rng.next(), xj = rng.next();
+                            const float phi = TWO_PI * xi;
+                            const float cp = cosf(phi), sp = sinf(phi), sth = sqrtf(xj), cth = sqrtf(1.0f - xj);
+                            const float e0x = cp * sth, e0y = sp * sth, e0z = cth;
+                            const float e1x = e0x * u2x + e0y * v0x + e0z * w1x;
+                            const float e1y = e0x * u2y + e0y * v0y + e0z * w1y;
+                            const float e1z = e0x * u2z + e0y * v0z + e0z * w1z;
+                            const float er = rsqrt_j(e1x * e1x + e1y * e1y + e1z * e1z);
+                            const float aox = s.px + w1x * 0.01f, aoy = s.py + w1y * 0.01f, aoz = s.pz + w1z * 0.01f;
+                            const float t = trace<false>(S, aox, aoy, aoz, e1x * er, e1y * er, e1z * er, st).t;
+                            segs++;
+                            const bool hit = t < P.ao_max_distance;
+                            const float v = hit ? 1.0f : 0.0f;  // bright 1, dark 0
+                            cr_ += (1.0f - v) * 1.0f + v * 0.0f;
+                            cg_ += (1.0f - v) * 1.0f + v * 0.0f;
+                            cb_ += (1.0f - v) * 1.0f + v * 0.0f;
+                            break;
+                        }
+                        const int so_off = __ldg(S.prim_info + h.prim).z;
+                        const int albedo = texture_color(S, f2i(__ldg(S.surfaces + so_off + 1)), s);
+                        float ar, ag, ab;
+                        if (mode == DFPT_RENDERER_RAY_TRACER) {
+                            ar = ((albedo >> 16) & 0xFF) / 255.0f; ag = ((albedo >> 8) & 0xFF) / 255.0f; ab = (albedo & 0xFF) / 255.0f;
+                        } else {
+                            ar = cr(albedo); ag = cg(albedo); ab = cb(albedo);
+                        }
+                        const int c = phong0(S, P, true, s.px, s.py, s.pz, wx, wy, wz, -dx, -dy, -dz, ar, ag, ab, st);
+                        segs++;
+                        if (mode == DFPT_RENDERER_RAY_CASTER) {
+                            cr_ = cr(c); cg_ = cg(c); cb_ = cb(c);
+                            break;
+                        }
+                        // Ray tracer (GRK:3866-3996)
+                        cr_ += cr(c); cg_ += cg(c); cb_ += cb(c);
+                        const int material = f2i(__ldg(S.surfaces + so_off));
+                        if (material != DFPT_MATERIAL_REFLECTION) break;
+                        const float dp2 = dp * 2.0f;
+                        ox = s.px + s.nx * 0.000001f; oy = s.py + s.ny * 0.000001f; oz = s.pz + s.nz * 0.000001f;
+                        dx = dx - s.nx * dp2; dy = dy - s.ny * dp2; dz = dz - s.nz * dp2;
+                    }
+                }
+            }
+            B.radiance[i] = make_float4(cr_, cg_, cb_, 0.0f);
+            B.rng[i] = rng.state;
+        }
+        warp_add_stats(P, B.stats, 0, segs, st.nodes, st.tris);
+    }
+}
+
+// Wireframe overlay (GRK:2910-3027): pixels on a triangle edge are set to black.
+__global__ void __launch_bounds__(128) k_wireframe(DevScene S, const DevParams* __restrict__ Pp, DevPass B) {
+    const DevParams& P = *Pp;
+    const int n = B.n_pixels;
+    GRID_STRIDE_UNIFORM(i, n) {
+        if (i < n && B.pixel_flags[i] == 0) {
+            TraceStats st{0, 0};
+            const float4 o = B.primary_o[i], d = B.primary_d[i];
+            const Hit h = trace<false>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            const float line_cos = cosf(PI_F * 0.5f / 4096.0f);
+            if (h.t != INF && h.prim != -1 && h.shape_type == DFPT_SHAPE_TRIANGLE) {
+                const Surf s = surface(S, P, o.x, o.y, o.z, d.x, d.y, d.z, h);
+                const float* C = S.camera;
+                const float ux = __ldg(C + 7), uy = __ldg(C + 8), uz = __ldg(C + 9);
+                const float vx = __ldg(C + 10), vy = __ldg(C + 11), vz = __ldg(C + 12);
+                const float wx = __ldg(C + 13), wy = __ldg(C + 14), wz = __ldg(C + 15);
+                const float spx = s.px * ux + s.py * uy + s.pz * uz;
+                const float spy = s.px * vx + s.py * vy + s.pz * vz;
+                const float spz = s.px * wx + s.py * wy + s.pz * wz;
+                const float spn = rsqrt_j(spx * spx + spy * spy + spz * spz);
+                float cx[3], cy[3], cz[3];
+                for (int k = 0; k < 3; ++k) {
+                    const float3 q = p3(S, __ldg(S.triangles + h.shape_offset + k));
+                    cx[k] = q.x * ux + q.y * uy + q.z * uz;
+                    cy[k] = q.x * vx + q.y * vy + q.z * vz;
+                    cz[k] = q.x * wx + q.y * wy + q.z * wz;
+                }
+                // Edges AC, BA, CB as (from, to) vertex pairs.
+                const int ef[3] = {0, 1, 2}, et[3] = {2, 0, 1};
+                bool edge = false;
+                for (int k = 0; k < 3; ++k) {
+                    const int f = ef[k], tt = et[k];
+                    const float ds = ((cx[f] - cx[tt]) * (cx[f] - cx[tt])) + ((cy[f] - cy[tt]) * (cy[f] - cy[tt])) + ((cz[f] - cz[tt]) * (cz[f] - cz[tt]));
+                    const float t0 = ((spx - cx[f]) * (cx[tt] - cx[f])) + ((spy - cy[f]) * (cy[tt] - cy[f])) + ((spz - cz[f]) * (cz[tt] - cz[f]));
+                    const float t1 = t0 / ds;
+                    const float qx = (1.0f - t1) * cx[f] + t1 * cx[tt];
+                    const float qy = (1.0f - t1) * cy[f] + t1 * cy[tt];
+                    const float qz = (1.0f - t1) * cz[f] + t1 * cz[tt];
+                    const float qn = rsqrt_j(qx * qx + qy * qy + qz * qz);
+                    const float dpq = qx * spx + qy * spy + qz * spz;
+                    if (dpq * qn * spn >= line_cos) edge = true;
+                }
+                if (edge) B.pixel_flags[i] = 1;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Film accumulation (Kahan-compensated running sums) and the image pipeline: selection tint,
+// tone map, sRGB redo-gamma, BGRA8 (GRK:279-307, AIK:333-472, 503-534, 702-774).
+
+__device__ __forceinline__ float redo_gamma(const DevParams& P, float v) {
+    return v <= 0.0f ? 0.0f : v >= 1.0f ? 1.0f : v <= P.cs_break ? v * P.cs_slope : P.cs_slope_match * powf(v, 1.0f / P.cs_gamma) - P.cs_segment;
+}
+
+__device__ __forceinline__ float filmic(float v, float exposure, float a, float b, float c, float d, float e, float subtract, float minimum) {
+    const float m = jmax(v * exposure - subtract, minimum);
+    return saturate_j((m * (a * m + b)) / (m * (c * m + d) + e), 0.0f, 1.0f);
+}
+
+__global__ void __launch_bounds__(256) k_film(const DevParams* __restrict__ Pp, DevPass B) {
+    const DevParams& P = *Pp;
+    const int n = B.n_pixels;
+    const int pass = *B.pass_index;
+    const bool clear = pass == P.clear_pass;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 L = B.radiance[i];
+        float4 sum = B.film_sum[i], comp = B.film_comp[i];
+        int cnt = B.film_n[i];
+        if (B.pixel_flags[i] & 1) {
+            sum = make_float4(0, 0, 0, 0); comp = make_float4(0, 0, 0, 0); cnt = 1;
+        } else if (clear || cnt == 0) {
+            sum = make_float4(L.x, L.y, L.z, 0); comp = make_float4(0, 0, 0, 0); cnt = 1;
+        } else {
+            float y, t;
+            y = L.x - comp.x; t = sum.x + y; comp.x = (t - sum.x) - y; sum.x = t;
+            y = L.y - comp.y; t = sum.y + y; comp.y = (t - sum.y) - y; sum.y = t;
+            y = L.z - comp.z; t = sum.z + y; comp.z = (t - sum.z) - y; sum.z = t;
+            cnt += 1;
+        }
+        B.film_sum[i] = sum; B.film_comp[i] = comp; B.film_n[i] = cnt;
+        const float inv = 1.0f / (float)cnt;
+        float r = sum.x * inv, g = sum.y * inv, b = sum.z * inv;
+        const int po = B.primitive_offsets[i];
+        g += (po > -1 && po == P.selected_primitive_offset) ? 1.0f : 0.0f;
+        const float ex = P.exposure;
+        switch (P.tone_mapper_type) {
+            case DFPT_TONE_MAPPER_REINHARD:
+                r = (r * ex) / (1.0f + r * ex); g = (g * ex) / (1.0f + g * ex); b = (b * ex) / (1.0f + b * ex);
+                break;
+            case DFPT_TONE_MAPPER_REINHARD_MODIFIED_1:
+                r = 1.0f - expf(-r * ex); g = 1.0f - expf(-g * ex); b = 1.0f - expf(-b * ex);
+                break;
+            case DFPT_TONE_MAPPER_REINHARD_MODIFIED_2: {
+                const float lw2r = 1.0f / (4.0f * 4.0f);
+                const float rm = r * ex, gm = g * ex, bm = b * ex;
+                r = rm * (1.0f + rm * lw2r) / (1.0f + rm); g = gm * (1.0f + gm * lw2r) / (1.0f + gm); b = bm * (1.0f + bm * lw2r) / (1.0f + bm);
+                break;
+            }
+            case DFPT_TONE_MAPPER_FILMIC_CURVE_ACES_MODIFIED:
+                r = filmic(r, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
+                g = filmic(g, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
+                b = filmic(b, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
+                break;
+            default:
+                break;
+        }
+        r = redo_gamma(P, r); g = redo_gamma(P, g); b = redo_gamma(P, b);
+        const int ri = f2i(jmax(jmin(r * 255.0f + 0.5f, 255.0f), 0.0f));
+        const int gi = f2i(jmax(jmin(g * 255.0f + 0.5f, 255.0f), 0.0f));
+        const int bi = f2i(jmax(jmin(b * 255.0f + 0.5f, 255.0f), 0.0f));
+        reinterpret_cast<uchar4*>(B.bgra)[i] = make_uchar4((unsigned char)bi, (unsigned char)gi, (unsigned char)ri, 255);
+    }
+}
+
+__global__ void k_end_pass(DevPass B) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *B.pass_index += 1;
+}
+
+// FP64 mean of the film average (AIK film semantics: sum / samples per pixel).
+__global__ void __launch_bounds__(256) k_film_mean(DevPass B, double* out3) {
+    double r = 0.0, g = 0.0, b = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n_pixels; i += gridDim.x * blockDim.x) {
+        const float4 s = B.film_sum[i];
+        const int c = B.film_n[i];
+        if (c > 0) {
+            const float inv = 1.0f / (float)c;
+            r += (double)(s.x * inv); g += (double)(s.y * inv); b += (double)(s.z * inv);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        r += __shfl_down_sync(0xFFFFFFFFu, r, off);
+        g += __shfl_down_sync(0xFFFFFFFFu, g, off);
+        b += __shfl_down_sync(0xFFFFFFFFu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out3, r);
+        atomicAdd(out3 + 1, g);
+        atomicAdd(out3 + 2, b);
+    }
+}
+
+__global__ void k_film_average(DevPass B, float* rgb, int* samples) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n_pixels; i += gridDim.x * blockDim.x) {
+        const float4 s = B.film_sum[i];
+        const int c = B.film_n[i];
+        const float inv = c > 0 ? 1.0f / (float)c : 0.0f;
+        if (rgb) { rgb[3 * i] = s.x * inv; rgb[3 * i + 1] = s.y * inv; rgb[3 * i + 2] = s.z * inv; }
+        if (samples) samples[i] = c;
+    }
+}
+
+__global__ void k_init_tables(const int* perm256, const float* grad36) {
+    const int i = threadIdx.x;
+    if (i < 512) g_perm[i] = perm256[i & 255];
+    if (i < 36) g_grad3[i] = grad36[i];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host-side launchers (the kernel set of this translation unit).
+
+static void launch_camera(const LaunchCtx& c) { k_camera<<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
+static void launch_trace_closest(const LaunchCtx& c, int bounce) {
+    k_trace<false><<<c.grid_trace, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce, bounce & 1);
+}
+static void launch_shade(const LaunchCtx& c, int bounce) { k_shade<<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce); }
+static void launch_shadow(const LaunchCtx& c, int bounce) { k_shadow<<<c.grid_trace, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce); }
+static void launch_final(const LaunchCtx& c, int bounce) { k_final<<<c.grid_trace, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce); }
+static void launch_simple(const LaunchCtx& c) { k_simple<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
+static void launch_wireframe(const LaunchCtx& c) { k_wireframe<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
+static void launch_film(const LaunchCtx& c) { k_film<<<c.grid, 256, 0, c.stream>>>(c.params, *c.pass); }
+static void launch_end_pass(const LaunchCtx& c) { k_end_pass<<<1, 32, 0, c.stream>>>(*c.pass); }
+static void launch_film_mean(const LaunchCtx& c, double* out3) { k_film_mean<<<c.grid, 256, 0, c.stream>>>(*c.pass, out3); }
+static void launch_film_average(const LaunchCtx& c, float* rgb, int* samples) {
+    k_film_average<<<c.grid, 256, 0, c.stream>>>(*c.pass, rgb, samples);
+}
+static void launch_init_tables(cudaStream_t s, const int* perm, const float* grad) { k_init_tables<<<1, 512, 0, s>>>(perm, grad); }
+
+static void occupancy(int sms, int& grid, int& grid_trace, int& grid_simple) {
+    int b1 = 0, b2 = 0, b3 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_shade, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_trace<false>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_simple, 128, 0);
+    grid = sms * (b1 > 0 ? b1 : 1);
+    grid_trace = sms * (b2 > 0 ? b2 : 1);
+    grid_simple = sms * (b3 > 0 ? b3 : 1);
+}
+
+KernelSet kernel_set() {
+    KernelSet k;
+    k.camera = launch_camera;
+    k.trace_closest = launch_trace_closest;
+    k.shade = launch_shade;
+    k.shadow = launch_shadow;
+    k.final_ = launch_final;
+    k.simple = launch_simple;
+    k.wireframe = launch_wireframe;
+    k.film = launch_film;
+    k.end_pass = launch_end_pass;
+    k.film_mean = launch_film_mean;
+    k.film_average = launch_film_average;
+    k.init_tables = launch_init_tables;
+    k.occupancy = occupancy;
+    return k;
+}
+
+}  // namespace DFPT_NS

@@ -1,0 +1,33 @@
+// dfpt_launch.h - the interface between the host API and a compiled kernel set.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dfpt_device_types.h"
+
+struct LaunchCtx {
+    const DevScene* scene;
+    const DevParams* params;  // device pointer
+    const DevPass* pass;
+    cudaStream_t stream;
+    int grid, grid_trace, grid_simple;
+};
+
+struct KernelSet {
+    void (*camera)(const LaunchCtx&);
+    void (*trace_closest)(const LaunchCtx&, int bounce);
+    void (*shade)(const LaunchCtx&, int bounce);
+    void (*shadow)(const LaunchCtx&, int bounce);
+    void (*final_)(const LaunchCtx&, int bounce);
+    void (*simple)(const LaunchCtx&);
+    void (*wireframe)(const LaunchCtx&);
+    void (*film)(const LaunchCtx&);
+    void (*end_pass)(const LaunchCtx&);
+    void (*film_mean)(const LaunchCtx&, double* out3);
+    void (*film_average)(const LaunchCtx&, float* rgb, int* samples);
+    void (*init_tables)(cudaStream_t, const int* perm256, const float* grad36);
+    void (*occupancy)(int sms, int& grid, int& grid_trace, int& grid_simple);
+};
+
+namespace dfpt_fast { KernelSet kernel_set(); }
+namespace dfpt_strict { KernelSet kernel_set(); }

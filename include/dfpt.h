@@ -1,0 +1,253 @@
+/*
+ * dfpt.h - C-ABI of the GB300 renderer core.
+ *
+ * The core replaces Aparapi's Kernel.execute/put/get for Dayflower's renderer kernel
+ * (src/main/java/org/dayflower/pathtracer/kernel/GPURendererKernel.java) and keeps its data
+ * contract: the compiled-scene float/int arrays produced by SceneCompiler
+ * (src/main/java/org/dayflower/pathtracer/scene/compiler/SceneCompiler.java:79-188) are passed
+ * in unchanged, as plain pointers and element counts, and uploaded to the device once.
+ *
+ * Conventions
+ *  - Every entry point returns DFPT_OK (0) or a negative DFPT_ERR_* code; dfpt_last_error()
+ *    returns a message for the last failure on the calling thread.
+ *  - All buffers are host memory owned by the caller unless the name says "device".
+ *  - A handle is not thread-safe; use one handle per host thread / CUDA stream.
+ *  - Offsets inside the scene arrays are element offsets, exactly as the reference writes them.
+ */
+#ifndef DFPT_H
+#define DFPT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DFPT_OK 0
+#define DFPT_ERR_INVALID_ARGUMENT (-1)  /* IllegalArgumentException in the reference */
+#define DFPT_ERR_CUDA (-2)
+#define DFPT_ERR_OUT_OF_MEMORY (-3)
+#define DFPT_ERR_INVALID_SCENE (-4)     /* offsets that point outside their arrays */
+#define DFPT_ERR_TIMEOUT (-5)           /* a bounded device-side wait gave up */
+#define DFPT_ERR_NOT_SUPPORTED (-6)
+
+/* Renderer, tone mapper and shader enums: AbstractRendererKernel.java:40-105. */
+#define DFPT_RENDERER_AMBIENT_OCCLUSION 1
+#define DFPT_RENDERER_PATH_TRACER 2
+#define DFPT_RENDERER_RAY_CASTER 3
+#define DFPT_RENDERER_RAY_MARCHER 4
+#define DFPT_RENDERER_RAY_TRACER 5
+#define DFPT_RENDERER_SURFACE_NORMALS 6
+#define DFPT_SHADER_FLAT 1
+#define DFPT_SHADER_GOURAUD 2
+#define DFPT_TONE_MAPPER_FILMIC_CURVE_ACES_MODIFIED 1
+#define DFPT_TONE_MAPPER_REINHARD 2
+#define DFPT_TONE_MAPPER_REINHARD_MODIFIED_1 3
+#define DFPT_TONE_MAPPER_REINHARD_MODIFIED_2 4
+
+/* Random number streams. DFPT_RNG_COUNTER is the counter-based Philox4x32-10 stream keyed by
+ * (seed, pixel) and counted by (pass, bounce, slot); DFPT_RNG_LCG is the reference's per-pixel
+ * 48-bit LCG (AbstractKernel.java:1101-1110) seeded from dfpt_params.seed. */
+#define DFPT_RNG_COUNTER 0
+#define DFPT_RNG_LCG 1
+
+/* The 14 compiled-scene arrays plus the camera, as CompiledScene holds them
+ * (CompiledScene.java:55-71). Counts are element counts (floats or ints), not bytes. */
+typedef struct dfpt_scene_desc {
+    const float* point2fs;                    int64_t point2fs_count;
+    const float* point3fs;                    int64_t point3fs_count;
+    const float* vector3fs;                   int64_t vector3fs_count;
+    const int32_t* planes;                    int64_t planes_count;
+    const float* spheres;                     int64_t spheres_count;
+    const float* terrains;                    int64_t terrains_count;
+    const int32_t* triangles;                 int64_t triangles_count;
+    const int32_t* bounding_volume_hierarchies; int64_t bounding_volume_hierarchies_count;
+    const float* textures;                    int64_t textures_count;
+    const float* surfaces;                    int64_t surfaces_count;
+    const int32_t* primitives;                int64_t primitives_count;
+    const float* primitives_object_to_world;  int64_t primitives_object_to_world_count;
+    const float* primitives_world_to_object;  int64_t primitives_world_to_object_count;
+    const float* camera;                      int64_t camera_count; /* 19 floats, Camera.java:87-222 */
+} dfpt_scene_desc;
+
+/* Sun and sky state: the scalars and arrays GPURendererKernel copies from Sky
+ * (GPURendererKernel.java:201-233, Sky.java:295-333). */
+typedef struct dfpt_sky {
+    double perez_relative_luminance[5];
+    double perez_x[5];
+    double perez_y[5];
+    double zenith_relative_luminance;
+    double zenith_x;
+    double zenith_y;
+    float theta;
+    float orthonormal_basis_u[3];
+    float orthonormal_basis_v[3];
+    float orthonormal_basis_w[3];
+    float sun_direction[3];        /* sun direction in the sky basis */
+    float sun_direction_world[3];
+    float sun_origin[3];
+    int32_t is_sky_active;
+    int32_t is_sun_active;
+} dfpt_sky;
+
+/* The renderer knobs of AbstractRendererKernel (setters at AbstractRendererKernel.java:383-580)
+ * and the global noise knobs of AbstractKernel (AbstractKernel.java:250-288). */
+typedef struct dfpt_params {
+    int32_t renderer_type;
+    int32_t tone_mapper_type;
+    int32_t shader_type;
+    int32_t normal_mapping;             /* BOOLEAN_TRUE/FALSE */
+    int32_t wireframes;                 /* BOOLEAN_TRUE/FALSE */
+    int32_t pt_ray_depth_maximum;
+    int32_t pt_ray_depth_russian_roulette;
+    float tone_mapper_exposure;
+    float ao_maximum_distance;
+    float global_amplitude;
+    float global_frequency;
+    float global_gain;
+    float global_lacunarity;
+    int32_t global_octaves;
+    int32_t selected_primitive_offset;  /* -1 = no selection */
+    int32_t rng_kind;                   /* DFPT_RNG_* */
+    uint64_t seed;
+} dfpt_params;
+
+typedef struct dfpt_handle dfpt_handle;
+
+/* Defaults of AbstractRendererKernel's constructor (AbstractRendererKernel.java:171-184). */
+void dfpt_params_default(dfpt_params* params);
+
+/* Replaces new GPURendererKernel(sceneLoader) + update(w, h, bytes, localSize) + the 19 put()
+ * calls of GPURendererKernel.update (GPURendererKernel.java:166-234, 411-449): validates the
+ * arrays, uploads them once and allocates the film for width x height pixels.
+ * Returns DFPT_ERR_INVALID_ARGUMENT for non-positive sizes (AbstractImageKernel.java:146-148). */
+int dfpt_create(const dfpt_scene_desc* scene, const dfpt_sky* sky, int32_t width, int32_t height,
+                dfpt_handle** out_handle);
+
+/* Replaces Kernel.dispose (DayflowerApplication.java:502). */
+int dfpt_destroy(dfpt_handle* handle);
+
+/* Issues all device work of the handle on this CUDA stream (a cudaStream_t); 0 = legacy stream. */
+int dfpt_set_stream(dfpt_handle* handle, void* cuda_stream);
+
+/* Replaces updateCamera() (GPURendererKernel.java:455-461): uploads the 19-float camera. */
+int dfpt_set_camera(dfpt_handle* handle, const float* camera19);
+
+/* Replaces updatePrimitives() (GPURendererKernel.java:467-521): 16 floats per primitive each. */
+int dfpt_set_transforms(dfpt_handle* handle, const float* object_to_world,
+                        const float* world_to_object, int32_t primitive_count);
+
+/* Replaces togglePrimitiveMaterial()'s put(surfaces) (GPURendererKernel.java:314-342). */
+int dfpt_set_surfaces(dfpt_handle* handle, const float* surfaces, int64_t surfaces_count);
+
+/* Replaces updateSunAndSky() and toggleSky/toggleSun (GPURendererKernel.java:375-397, 527-569). */
+int dfpt_set_sky(dfpt_handle* handle, const dfpt_sky* sky);
+
+/* Replaces the AbstractRendererKernel setters; takes effect at the next pass. */
+int dfpt_set_params(dfpt_handle* handle, const dfpt_params* params);
+
+/* Replaces clear() (AbstractImageKernel.java:119-121): the next pass replaces the film. */
+int dfpt_clear(dfpt_handle* handle);
+
+/* Replaces kernel.execute(range) + kernel.clearFilmFlags() (DayflowerApplication.java:853-854):
+ * renders `passes` passes of one sample per pixel each, accumulates the film and resolves
+ * the BGRA8 image and the primitive-offset buffer. Asynchronous on the handle's stream. */
+int dfpt_render(dfpt_handle* handle, int32_t passes);
+
+/* Waits for the handle's stream. */
+int dfpt_synchronize(dfpt_handle* handle);
+
+/* Replaces kernel.get(byte[]) (DayflowerApplication.java:855): width*height*4 bytes, B,G,R,A. */
+int dfpt_read_bgra8(dfpt_handle* handle, uint8_t* bgra);
+
+/* The film: running-average linear radiance (width*height*3 floats, filmData of
+ * AbstractImageKernel.java:333-359) and samples per pixel (filmDataSamples). Either may be NULL. */
+int dfpt_read_film(dfpt_handle* handle, float* rgb, int32_t* samples);
+
+/* Mean linear radiance of the film, reduced in FP64 on the device. */
+int dfpt_read_film_mean(dfpt_handle* handle, double* mean_rgb3);
+
+/* Replaces get(primitiveOffsets) of togglePrimitiveSelection (GPURendererKernel.java:351-369). */
+int dfpt_read_primitive_offsets(dfpt_handle* handle, int32_t* primitive_offsets);
+
+/* The primary-ray hit record of the last pass (hit record of GPURendererKernel.java:79-94):
+ * primitive offset, shape type, shape offset, distance (INFINITY=100000 on a miss) and the
+ * world-space shading normal (3 floats per pixel). Any pointer may be NULL. */
+int dfpt_read_hits(dfpt_handle* handle, int32_t* primitive_offset, int32_t* shape_type,
+                   int32_t* shape_offset, float* distance, float* normal3);
+
+/* Ray-segment counters of the last dfpt_render call: closest-hit segments, any-hit segments,
+ * BVH nodes visited and triangles tested (summed over all segments). */
+int dfpt_read_counters(dfpt_handle* handle, uint64_t* counters4);
+/* Enables (1) or disables (0, the default) the traversal counters; counting costs atomics. */
+int dfpt_set_counting(dfpt_handle* handle, int32_t enabled);
+
+/* Number of kernels the handle launched since it was created (for launch accounting). */
+int dfpt_launch_count(dfpt_handle* handle, uint64_t* launches);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* dfpt_last_error(void);
+
+/* ---------------------------------------------------------------------------------------------
+ * Scene compiler (host only). Restates SceneCompiler.compile (SceneCompiler.java:79-188) and the
+ * BVH builder (BoundingVolumeHierarchy.java:118-157, 805-986) so callers without a JVM can build
+ * the same arrays. A scene is described by flat records and compiled into a dfpt_compiled. */
+
+#define DFPT_SHAPE_PLANE 1
+#define DFPT_SHAPE_SPHERE 2
+#define DFPT_SHAPE_TERRAIN 3
+#define DFPT_SHAPE_TRIANGLE 4
+#define DFPT_SHAPE_TRIANGLE_MESH 5
+#define DFPT_MATERIAL_CLEAR_COAT 1
+#define DFPT_MATERIAL_GLASS 2
+#define DFPT_MATERIAL_LAMBERTIAN 3
+#define DFPT_MATERIAL_PHONG 4
+#define DFPT_MATERIAL_REFLECTION 5
+#define DFPT_TEXTURE_BLEND 1
+#define DFPT_TEXTURE_BULLSEYE 2
+#define DFPT_TEXTURE_CHECKERBOARD 3
+#define DFPT_TEXTURE_CONSTANT 4
+#define DFPT_TEXTURE_FBM 5
+#define DFPT_TEXTURE_IMAGE 6
+#define DFPT_TEXTURE_SURFACE_NORMAL 7
+#define DFPT_TEXTURE_UV 8
+
+typedef struct dfpt_scene_builder dfpt_scene_builder;
+typedef struct dfpt_compiled dfpt_compiled;
+
+int dfpt_builder_create(dfpt_scene_builder** out_builder);
+int dfpt_builder_destroy(dfpt_scene_builder* builder);
+/* Adds a texture record exactly as Texture.toArray() lays it out (type, size, ...); Blend
+ * textures give the builder indices of their two textures in slots 2 and 3. Returns the index. */
+int dfpt_builder_add_texture(dfpt_scene_builder* builder, const float* record, int32_t count);
+/* Adds a Surface (Surface.java:33-63); texture arguments are builder texture indices. */
+int dfpt_builder_add_surface(dfpt_scene_builder* builder, int32_t material, int32_t albedo,
+                             int32_t emission, int32_t normal, float noise_amount, float noise_scale);
+/* Adds a shape; params: plane a,b,c (9); sphere position + radius (4); terrain 5 floats. */
+int dfpt_builder_add_shape(dfpt_scene_builder* builder, int32_t shape_type, const float* params);
+/* Adds a triangle mesh (or a single triangle when triangle_count == 1 and as_mesh == 0).
+ * Per vertex: position 3, normal 3, uv 2, tangent 3 (11 floats); indices 3 per triangle. */
+int dfpt_builder_add_mesh(dfpt_scene_builder* builder, const float* vertices11, int64_t vertex_count,
+                          const int32_t* indices, int64_t triangle_count, int32_t as_mesh);
+/* Adds a Primitive with a Transform (position 3, quaternion x,y,z,w 4, scale 3). */
+int dfpt_builder_add_primitive(dfpt_scene_builder* builder, int32_t shape, int32_t surface,
+                               const float* transform10);
+/* Camera: eye, look-at point, field of view X in degrees, resolution, aperture, focal distance,
+ * lens (1 thin, 2 fisheye). */
+int dfpt_builder_set_camera(dfpt_scene_builder* builder, const float* eye3, const float* look_at3,
+                            float field_of_view_x, float resolution_x, float resolution_y,
+                            float aperture_radius, float focal_distance, int32_t lens);
+/* Compiles; threads <= 0 uses all cores for the BVH sweeps (results do not depend on it). */
+int dfpt_builder_compile(dfpt_scene_builder* builder, int32_t threads, dfpt_compiled** out_compiled);
+int dfpt_compiled_destroy(dfpt_compiled* compiled);
+/* Points desc at the compiled arrays (valid until dfpt_compiled_destroy). */
+int dfpt_compiled_describe(const dfpt_compiled* compiled, dfpt_scene_desc* desc);
+
+/* Sky.set(sunDirectionWorld, turbidity) (Sky.java:295-333). */
+int dfpt_sky_set(dfpt_sky* sky, const float* sun_direction_world3, float turbidity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DFPT_H */
