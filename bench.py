@@ -1,0 +1,356 @@
+"""Benchmark: M path samples/s of the GB300 renderer core on the 1080p triangle-mesh workload.
+
+One step = one pass of the path tracer over the whole 1920x1080 image (one sample per pixel), the
+unit of the reference's Kernel.execute (DayflowerApplication.java:853). The workload is
+mesh_scene: an fBm-displaced geodesic icosphere (200,000 triangles, 4 Lambertian/Phong regions)
+over a 512x512 fBm heightfield (522,242 triangles), BVHs built by the restated reference builder,
+depth 8, ACES; seeded synthetic data (the reference publishes no scenes).
+
+  value : device-resident throughput (scene uploaded once, per-step CUDA events on the handle's
+          stream, L2 flushed between steps with a 256 MiB write);
+  e2e   : the same metric through the C-ABI as the reference's render loop uses it
+          (dfpt_set_camera from host memory, dfpt_render, dfpt_read_bgra8 into host memory);
+  roofline : the dominant kernel (closest-hit traversal), algorithmic bytes per segment =
+          nodes*32 + triangles*48 + 64 with the mean visit counts measured by the CPU
+          restatement on the cpu_baseline sample, against MEASURED_PEAKS.json's HBM copy rate;
+  cpu_baseline : the oracle's strict-FP32 restatement of the reference kernel on all host cores,
+          over a bounded band of rows (the reference's Java thread-pool path needs a JVM).
+--impl reference times that CPU restatement alone on the same workload and metric.
+Multi-GPU: pixels are independent, so N ranks render N replicas (weak scaling, no collective on
+the data path); value sums the ranks' samples over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "dayflower-path-tracer_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "M path samples/s @1080p (1 spp passes)"
+UNIT = "M samples/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=32)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="dfpt", choices=["dfpt", "reference"])
+    ap.add_argument("--workload", default="mesh_scene", choices=["mesh_scene", "sphere_scene", "instances_scene"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def build_workload(name, width, height):
+    from dfpt import synthetic
+
+    if name == "mesh_scene":
+        return synthetic.mesh_scene(width=width, height=height)
+    if name == "sphere_scene":
+        return synthetic.sphere_scene(0, width, height)
+    return synthetic.instances_scene(width=width, height=height)
+
+
+def params_struct(d):
+    from dfpt.kernel import default_params
+
+    p = default_params()
+    for k, v in d.items():
+        setattr(p, k, v)
+    return p
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device_index=0):
+        self.rows = []
+        self.proc = None
+        self.device_index = device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        import statistics
+
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_baseline(scene, sky, params, width, height, seconds, threads=0):
+    """Times the oracle's strict-FP32 restatement on a band of rows sized to ~`seconds`."""
+    from oracle import oracle
+
+    p = params_struct(params)
+    threads = threads or os.cpu_count() or 1
+    rows = max(1, threads // 2)
+    t0 = time.perf_counter()
+    out = oracle.render(scene, sky, p, width, height, passes=1, precision=32, threads=threads, rows=(0, rows))
+    dt = time.perf_counter() - t0
+    target = min(height, max(rows, int(rows * seconds / max(dt, 1e-3))))
+    r0 = max(0, height // 2 - target // 2)
+    t0 = time.perf_counter()
+    out = oracle.render(scene, sky, p, width, height, passes=1, precision=32, threads=threads, rows=(r0, r0 + target))
+    dt = time.perf_counter() - t0
+    samples = target * width
+    c = out["counters"].astype(float)
+    segs = c[0] + c[1]
+    return {
+        "value": samples / dt / 1e6,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"rows {r0}..{r0 + target} of {width}x{height}, 1 pass (1 spp), strict FP32 restatement, "
+                  f"{threads} threads, {dt:.1f} s",
+        "segments_per_sample": segs / samples,
+        "nodes_per_segment": c[2] / max(segs, 1),
+        "tris_per_segment": c[3] / max(segs, 1),
+        "closest_per_sample": c[0] / samples,
+    }
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    scene, sky, params, (w, h) = build_workload(args.workload, args.width, args.height)
+    from oracle import oracle
+
+    p = params_struct(params)
+    threads = os.cpu_count() or 1
+    # Each step renders a band of rows sized so the whole run stays within a few minutes.
+    band = max(1, threads // 2)
+    t0 = time.perf_counter()
+    oracle.render(scene, sky, p, w, h, passes=1, precision=32, threads=threads, rows=(0, band))
+    per_row = (time.perf_counter() - t0) / band
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    band = int(min(h, max(band, budget / max(per_row, 1e-6))))
+    for i in range(args.warmup):
+        oracle.render(scene, sky, p, w, h, passes=1, precision=32, threads=threads, rows=(0, band), pass_begin=i)
+    total, samples = 0.0, 0
+    for i in range(args.steps):
+        r0 = (i * band) % max(1, h - band)
+        t0 = time.perf_counter()
+        oracle.render(scene, sky, p, w, h, passes=1, precision=32, threads=threads, rows=(r0, r0 + band), pass_begin=i)
+        total += time.perf_counter() - t0
+        samples += band * w
+    value = samples / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"{args.workload} {w}x{h}", "passes_per_step": 1, "rows_per_step": band},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{band} rows x {w} px per step, strict FP32 restatement of GPURendererKernel.run "
+                                   "(the reference's Java thread-pool path is unavailable: no JVM)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    from dfpt.kernel import RendererKernel
+
+    t_build = time.perf_counter()
+    scene, sky, params, (w, h) = build_workload(args.workload, args.width, args.height)
+    t_build = time.perf_counter() - t_build
+    k = RendererKernel(scene, sky, params)
+    k.update(w, h)
+    k.set_seed(0x5EED0000 + rank)
+    stream = torch.cuda.Stream()
+    k.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    n_pix = w * h
+
+    # Warm-up (graphs built here).
+    k.execute(args.warmup)
+    k.synchronize()
+
+    # Timed region: per-step events on the handle's stream, L2 flushed between steps, per-kernel
+    # events inside each pass for the roofline.
+    k.set_profiling(True)
+    sampler = ClockSampler(local)
+    launches0 = k.launch_count()
+    barrier()
+    sampler.start()
+    step_ms = []
+    trace_ms, trace_n, kind_ms = 0.0, 0, {}
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        k.execute(1)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        prof = k.read_profile()
+        trace_ms += prof["trace"][0]
+        trace_n += prof["trace"][1]
+        for kk, (ms, n) in prof.items():
+            a = kind_ms.setdefault(kk, [0.0, 0])
+            a[0] += ms
+            a[1] += n
+    barrier()
+    clocks = sampler.stop()
+    launches = k.launch_count() - launches0
+    total_s = sum(step_ms) / 1e3
+    if dist is not None:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * n_pix * args.steps / total_s / 1e6
+    k.set_profiling(False)
+
+    # Traversal counters over one extra pass (not timed): segments per pass.
+    k.set_counting(True)
+    k.execute(1)
+    k.synchronize()
+    cnt = k.counters().astype(float)
+    k.set_counting(False)
+
+    # End to end through the C-ABI with host buffers (camera in, BGRA8 out), the render loop of
+    # DayflowerApplication.java:832-877.
+    import ctypes as C
+
+    cam = np.ascontiguousarray(scene.camera.copy())
+    host_img = np.empty(n_pix * 4, np.uint8)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        k.update_camera(cam)
+        k.execute(1)
+        k.get(host_img)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n_pix * args.steps / e2e_s / 1e6
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, sky, params, w, h, args.cpu_seconds)
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    closest_segments = cnt[0]
+    nodes_per_seg = cpu["nodes_per_segment"] if cpu else (cnt[2] / max(cnt[0] + cnt[1], 1))
+    tris_per_seg = cpu["tris_per_segment"] if cpu else (cnt[3] / max(cnt[0] + cnt[1], 1))
+    bytes_per_seg = nodes_per_seg * 32 + tris_per_seg * 48 + 64
+    avg_trace_ms = trace_ms / max(trace_n, 1)
+    launches_per_pass = max(trace_n / args.steps, 1)
+    bytes_per_launch = closest_segments / launches_per_pass * bytes_per_seg
+    achieved = bytes_per_launch / (avg_trace_ms / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "trace_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("bytes_per_launch_full")
+        except ValueError:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"{args.workload} {w}x{h}", "triangles": int(len(scene.triangles) // 12),
+                   "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": 1,
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
+                   "scene_build_s": round(t_build, 1)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_source": peak_note,
+                     "kernel": "k_trace<closest>", "avg_launch_ms": avg_trace_ms,
+                     "bytes_per_segment": bytes_per_seg, "segments_per_launch": closest_segments / launches_per_pass},
+        "kernels_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in kind_ms.items() if v[1]},
+        "rays_per_s": (cnt[0] + cnt[1]) / (total_s / args.steps) / 1e9 * 1e3,
+        "clocks": clocks,
+    }
+    if cpu:
+        line["cpu_baseline"] = {k2: cpu[k2] for k2 in ("value", "unit", "cores", "kind", "sample")}
+    line["rays_per_s"] = (cnt[0] + cnt[1]) * world / (total_s / args.steps)
+    print(json.dumps(line), flush=True)
+    k.dispose()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -323,11 +323,18 @@ struct dfpt_handle {
     int graph_kernels = 0;
     bool use_graph = true;
     uint64_t launches = 0;
+    // Per-kernel timing (direct launches with an event between kernels).
+    bool profiling = false;
+    std::vector<cudaEvent_t> events;
+    std::vector<int> event_kind;  // kind of the kernel between events i and i+1
+    int events_used = 0;
 };
 
 namespace {
 
 void release(dfpt_handle* h) {
+    for (cudaEvent_t e : h->events) cudaEventDestroy(e);
+    h->events.clear();
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     h->graph_exec = nullptr;
     DevBuf<float>* fb[] = {&h->point2fs, &h->point3fs, &h->vector3fs, &h->spheres, &h->terrains, &h->textures, &h->surfaces, &h->o2w, &h->w2o, &h->camera, &h->hit_dist, &h->hit_normal, &h->scratch_rgb};
@@ -409,6 +416,12 @@ void fill_dev_params(dfpt_handle* h) {
     d.den_x_a = (float)(1.0 + k.perez_x[0] * std::exp(k.perez_x[1]));
     d.den_y_a = (float)(1.0 + k.perez_y[0] * std::exp(k.perez_y[1]));
     d.cos_theta0 = (float)c0;
+    const float pi_f = 3.14159274101257324219f;
+    const float pi180 = pi_f / 180.0f;
+    const float* cam = h->host.camera.data();
+    d.fov_tan_x = (float)std::tan((double)(cam[4] * 0.5f * pi180));
+    d.fov_tan_y = (float)std::tan((double)(-cam[5] * 0.5f * pi180));
+    d.wire_cos = (float)std::cos((double)(pi_f * 0.5f / 4096.0f));
     // RGBColorSpace.SRGB (breakPoint 0.00304, gamma 2.4) derived constants, float arithmetic.
     const float bp = 0.00304f, g = 2.4f;
     const float pe = powf_j(bp, 1.0f / g - 1.0f);
@@ -440,27 +453,45 @@ bool is_simple_mode(int rt) {
            rt == DFPT_RENDERER_RAY_TRACER || rt == DFPT_RENDERER_SURFACE_NORMALS;
 }
 
+// Kernel kinds reported by dfpt_read_profile.
+enum { KIND_CAMERA, KIND_TRACE, KIND_SHADE, KIND_SHADOW, KIND_FINAL, KIND_SIMPLE, KIND_WIREFRAME, KIND_FILM, KIND_END, KIND_COUNT };
+
+void mark(dfpt_handle* h, int kind) {
+    if (!h->profiling) return;
+    if (h->events_used >= (int)h->events.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) { (void)cudaGetLastError(); return; }
+        h->events.push_back(e);
+    }
+    cudaEventRecord(h->events[h->events_used], h->stream);
+    if ((int)h->event_kind.size() < h->events_used + 1) h->event_kind.resize(h->events_used + 1);
+    h->event_kind[h->events_used] = kind;
+    h->events_used++;
+}
+
 // Issues one pass on the handle's stream; returns the number of kernels launched.
 int issue_pass(dfpt_handle* h) {
     const KernelSet& K = kset(h);
     const LaunchCtx& c = h->ctx;
     int k = 0;
+    h->events_used = 0;
     cudaMemsetAsync(h->counts.p, 0, 64 * sizeof(int), h->stream);
     if (is_simple_mode(h->params.renderer_type)) {
-        K.simple(c); ++k;
+        mark(h, KIND_SIMPLE); K.simple(c); ++k;
     } else {
         const int nb = h->params.pt_ray_depth_maximum < 1 ? 1 : (h->params.pt_ray_depth_maximum > DFPT_MAX_DEPTH ? DFPT_MAX_DEPTH : h->params.pt_ray_depth_maximum);
-        K.camera(c); ++k;
+        mark(h, KIND_CAMERA); K.camera(c); ++k;
         for (int b = 0; b < nb; ++b) {
-            K.trace_closest(c, b); ++k;
-            K.shade(c, b); ++k;
-            if (h->sky.is_sun_active == 1) { K.shadow(c, b); ++k; }
+            mark(h, KIND_TRACE); K.trace_closest(c, b); ++k;
+            mark(h, KIND_SHADE); K.shade(c, b); ++k;
+            if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.shadow(c, b); ++k; }
         }
-        K.final_(c, nb); ++k;
+        mark(h, KIND_FINAL); K.final_(c, nb); ++k;
     }
-    if (h->params.wireframes == 1) { K.wireframe(c); ++k; }
-    K.film(c); ++k;
-    K.end_pass(c); ++k;
+    if (h->params.wireframes == 1) { mark(h, KIND_WIREFRAME); K.wireframe(c); ++k; }
+    mark(h, KIND_FILM); K.film(c); ++k;
+    mark(h, KIND_END); K.end_pass(c); ++k;
+    mark(h, KIND_COUNT);
     return k;
 }
 
@@ -655,7 +686,7 @@ int dfpt_set_camera(dfpt_handle* h, const float* camera19) {
     if (!h || !camera19) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
     h->host.camera.assign(camera19, camera19 + 19);
     CUDA_TRY(cudaMemcpyAsync(h->camera.p, h->host.camera.data(), 19 * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-    return DFPT_OK;
+    return push_params(h);  // the field-of-view tangents are derived from the camera
 }
 
 int dfpt_set_transforms(dfpt_handle* h, const float* o2w, const float* w2o, int32_t count) {
@@ -746,7 +777,7 @@ int dfpt_render(dfpt_handle* h, int32_t passes) {
     if (passes < 0) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "passes < 0");
     if (h->counting) CUDA_TRY(cudaMemsetAsync(h->stats.p, 0, 4 * sizeof(unsigned long long), h->stream));
     if (passes == 0) return DFPT_OK;
-    if (h->use_graph) {
+    if (h->use_graph && !h->profiling) {
         if (!h->graph_valid) {
             int r = build_graph(h);
             if (r) return r;
@@ -826,6 +857,27 @@ int dfpt_read_counters(dfpt_handle* h, uint64_t* c4) {
     CUDA_TRY(cudaMemcpyAsync(v, h->stats.p, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     for (int i = 0; i < 4; ++i) c4[i] = v[i];
+    return DFPT_OK;
+}
+
+int dfpt_set_profiling(dfpt_handle* h, int32_t enabled) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    h->profiling = enabled != 0;
+    h->events_used = 0;
+    return DFPT_OK;
+}
+
+int dfpt_read_profile(dfpt_handle* h, double* ms_by_kind, int32_t* launches_by_kind) {
+    if (!h || !ms_by_kind || !launches_by_kind) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (int i = 0; i < KIND_COUNT; ++i) { ms_by_kind[i] = 0.0; launches_by_kind[i] = 0; }
+    if (!h->profiling || h->events_used < 2) return DFPT_OK;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i + 1 < h->events_used; ++i) {
+        float ms = 0.0f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, h->events[i], h->events[i + 1]));
+        const int kind = h->event_kind[i];
+        if (kind >= 0 && kind < KIND_COUNT) { ms_by_kind[kind] += ms; launches_by_kind[kind] += 1; }
+    }
     return DFPT_OK;
 }
 

@@ -64,6 +64,11 @@ struct DevParams {
     float den_l;        // (1 + l0 e^l1)(1 + l2 e^(l3 theta0) + l4 cos^2 theta0)
     float den_x_a, den_y_a;  // 1 + x0 e^x1, 1 + y0 e^y1
     float cos_theta0;
+    // Camera constants computed once on the host with java.lang.Math semantics (double math,
+    // rounded to float): tan(fovX/2), tan(-fovY/2) (GPURendererKernel.java:603-605) and the
+    // wireframe threshold cos(PI/2/4096) (GPURendererKernel.java:2933-2934).
+    float fov_tan_x, fov_tan_y;
+    float wire_cos;
     // sRGB redo-gamma constants (RGBColorSpace.SRGB).
     float cs_break, cs_gamma, cs_slope, cs_slope_match, cs_segment;
 };

@@ -393,8 +393,8 @@ __device__ bool primary_ray(const DevScene& S, const DevParams& P, int pixel, bo
     const float ux = __ldg(C + 7), uy = __ldg(C + 8), uz = __ldg(C + 9);
     const float vx = __ldg(C + 10), vy = __ldg(C + 11), vz = __ldg(C + 12);
     const float wx = __ldg(C + 13), wy = __ldg(C + 14), wz = __ldg(C + 15);
-    const float fx = tanf(__ldg(C + 4) * 0.5f * PI_OVER_180);
-    const float fy = tanf(-__ldg(C + 5) * 0.5f * PI_OVER_180);
+    const float fx = P.fov_tan_x;
+    const float fy = P.fov_tan_y;
     const float hx = ux * fx, hy = uy * fx, hz = uz * fx;
     const float gx = vx * fy, gy = vy * fy, gz = vz * fy;
     float sx = 0.5f, sy = 0.5f;
@@ -937,7 +937,7 @@ __global__ void __launch_bounds__(128) k_wireframe(DevScene S, const DevParams* 
             TraceStats st{0, 0};
             const float4 o = B.primary_o[i], d = B.primary_d[i];
             const Hit h = trace<false>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            const float line_cos = cosf(PI_F * 0.5f / 4096.0f);
+            const float line_cos = P.wire_cos;
             if (h.t != INF && h.prim != -1 && h.shape_type == DFPT_SHAPE_TRIANGLE) {
                 const Surf s = surface(S, P, o.x, o.y, o.z, d.x, d.y, d.z, h);
                 const float* C = S.camera;

@@ -156,6 +156,17 @@ class RendererKernel:
         check(self._lib.dfpt_read_counters(self._need(), ptr(c, C.c_uint64)))
         return c
 
+    PROFILE_KINDS = ("camera", "trace", "shade", "shadow", "final", "simple", "wireframe", "film", "end")
+
+    def set_profiling(self, enabled: bool) -> None:
+        check(self._lib.dfpt_set_profiling(self._need(), 1 if enabled else 0))
+
+    def read_profile(self) -> dict:
+        ms = np.zeros(9, np.float64)
+        n = np.zeros(9, np.int32)
+        check(self._lib.dfpt_read_profile(self._need(), ptr(ms, C.c_double), ptr(n, C.c_int32)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PROFILE_KINDS)}
+
     def launch_count(self) -> int:
         c = C.c_uint64()
         check(self._lib.dfpt_launch_count(self._need(), C.byref(c)))

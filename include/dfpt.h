@@ -182,6 +182,13 @@ int dfpt_read_counters(dfpt_handle* handle, uint64_t* counters4);
 /* Enables (1) or disables (0, the default) the traversal counters; counting costs atomics. */
 int dfpt_set_counting(dfpt_handle* handle, int32_t enabled);
 
+/* Per-kernel timing of the last pass: when enabled, passes are issued as direct launches with a
+ * CUDA event between kernels (no graph), and dfpt_read_profile returns, per kernel kind
+ * (0 camera, 1 trace closest, 2 shade, 3 shadow, 4 final any-hit, 5 per-pixel modes,
+ * 6 wireframe, 7 film, 8 end of pass), the milliseconds and the launch count of the last pass. */
+int dfpt_set_profiling(dfpt_handle* handle, int32_t enabled);
+int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind9, int32_t* launches_by_kind9);
+
 /* Number of kernels the handle launched since it was created (for launch accounting). */
 int dfpt_launch_count(dfpt_handle* handle, uint64_t* launches);
 
