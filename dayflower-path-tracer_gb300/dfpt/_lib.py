@@ -106,6 +106,7 @@ SIGNATURES = {
     "dfpt_read_bgra8": (C.c_int, [C.c_void_p, u8p]),
     "dfpt_read_film": (C.c_int, [C.c_void_p, f32p, i32p]),
     "dfpt_read_film_mean": (C.c_int, [C.c_void_p, f64p]),
+    "dfpt_film_mean_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "dfpt_read_primitive_offsets": (C.c_int, [C.c_void_p, i32p]),
     "dfpt_read_hits": (C.c_int, [C.c_void_p, i32p, i32p, i32p, f32p, f32p]),
     "dfpt_read_counters": (C.c_int, [C.c_void_p, u64p]),

@@ -167,6 +167,22 @@ int dfpt_read_film(dfpt_handle* handle, float* rgb, int32_t* samples);
 /* Mean linear radiance of the film, reduced in FP64 on the device. */
 int dfpt_read_film_mean(dfpt_handle* handle, double* mean_rgb3);
 
+/* dfpt_film_mean_noalloc has no counterpart in the reference. It is the allocation-free variant of
+ * dfpt_read_film_mean for callers that cannot allocate device memory when they need the mean: a
+ * frame loop that must not call cudaMalloc/cudaFree once running (allocation can synchronise the
+ * device and stall the loop), or a host whose device memory belongs to another allocator (a
+ * JVM-side pool, an engine's frame allocator). The caller passes the film (pixel_count x 3 floats,
+ * linear RGB) and the output (3 doubles, the FP64 mean per channel), both in device memory; the
+ * result is written asynchronously on `cuda_stream` (a cudaStream_t, NULL = legacy stream).
+ * Scratch: a fixed device array of DFPT_NOALLOC_MAX_BLOCKS x 3 doubles (24 KiB) that every GPU
+ * which loads this library holds until the process exits. The first call on a device looks up
+ * that array's device address (cudaGetSymbolAddress), so make the first call on each device
+ * before any stream capture. Every call shares the array: calls that overlap on the GPU race.
+ * pixel_count outside 1..DFPT_NOALLOC_MAX_PIXELS returns DFPT_ERR_INVALID_ARGUMENT. */
+#define DFPT_NOALLOC_MAX_BLOCKS 1024
+#define DFPT_NOALLOC_MAX_PIXELS (1ll << 28)
+int dfpt_film_mean_noalloc(const float* device_rgb, int64_t pixel_count, double* device_mean3, void* cuda_stream);
+
 /* Replaces get(primitiveOffsets) of togglePrimitiveSelection (GPURendererKernel.java:351-369). */
 int dfpt_read_primitive_offsets(dfpt_handle* handle, int32_t* primitive_offsets);
 
