@@ -1292,6 +1292,14 @@ double oracle_fbm3(double frequency, double gain, double minimum, double maximum
     return Kernel<float>::fbm3((float)frequency, (float)gain, (float)minimum, (float)maximum, octaves, (float)x, (float)y, (float)z);
 }
 
+// Philox4x32-10 block for known-answer tests.
+int oracle_philox(const uint32_t* counter4, const uint32_t* key2, uint32_t* out4) {
+    uint32_t c[4] = {counter4[0], counter4[1], counter4[2], counter4[3]};
+    philox(c, key2[0], key2[1]);
+    for (int i = 0; i < 4; ++i) out4[i] = c[i];
+    return 0;
+}
+
 // The first `count` numbers of a pixel's stream (LCG from `state`, or the counter stream).
 int oracle_random(int kind, uint64_t state, uint32_t pixel, uint32_t pass, uint64_t seed, int count, float* out) {
     Random r{kind, state, pixel, pass, (uint32_t)seed, (uint32_t)(seed >> 32), 0};

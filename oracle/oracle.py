@@ -40,6 +40,7 @@ def load():
         _lib.oracle_fbm3.restype = C.c_double
         _lib.oracle_random.argtypes = [C.c_int, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int, vp]
         _lib.oracle_tonemap.argtypes = [vp, vp, C.c_int, vp]
+        _lib.oracle_philox.argtypes = [vp, vp, vp]
     return _lib
 
 
@@ -120,3 +121,11 @@ def tonemap(params, rgb, precision=32):
     v = np.asarray(rgb, np.float64)
     load().oracle_tonemap(C.addressof(params), _p(v), precision, _p(out))
     return out
+
+
+def philox(counter, key):
+    c = np.asarray(counter, np.uint32)
+    k = np.asarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    load().oracle_philox(_p(c), _p(k), _p(out))
+    return [int(x) for x in out]
