@@ -225,7 +225,13 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     n_pix = w * h
 
-    # Warm-up (graphs built here).
+    # Warm-up (graphs built here), then the traversal launch configuration is autotuned on this
+    # scene (outside the timed region).
+    k.execute(args.warmup)
+    k.synchronize()
+    from dfpt.autotune import tune_trace
+
+    tuning = tune_trace(k, passes=3, warmup=1)
     k.execute(args.warmup)
     k.synchronize()
 
@@ -332,7 +338,8 @@ def main():
         "config": {"workload": f"{args.workload} {w}x{h}", "triangles": int(len(scene.triangles) // 12),
                    "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": 1,
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                   "scene_build_s": round(t_build, 1)},
+                   "scene_build_s": round(t_build, 1), "trace_config": tuning["best"],
+                   "trace_config_ms": {str(kk): round(v, 3) for kk, v in tuning["ms_per_pass"].items()}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

@@ -313,6 +313,7 @@ struct dfpt_handle {
     DevBuf<double> mean;
     DevPass pass{};
     LaunchCtx ctx{};
+    size_t shadow_capacity = 0;  // rays the deferred shadow queue holds (pixels x bounces)
     int host_pass = 0;  // passes issued so far (mirrors the device pass counter)
     int clear_pass = 0;
     bool counting = false;
@@ -475,7 +476,7 @@ int issue_pass(dfpt_handle* h) {
     const LaunchCtx& c = h->ctx;
     int k = 0;
     h->events_used = 0;
-    cudaMemsetAsync(h->counts.p, 0, 64 * sizeof(int), h->stream);
+    cudaMemsetAsync(h->counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), h->stream);
     if (is_simple_mode(h->params.renderer_type)) {
         mark(h, KIND_SIMPLE); K.simple(c); ++k;
     } else {
@@ -484,15 +485,35 @@ int issue_pass(dfpt_handle* h) {
         for (int b = 0; b < nb; ++b) {
             mark(h, KIND_TRACE); K.trace_closest(c, b); ++k;
             mark(h, KIND_SHADE); K.shade(c, b); ++k;
-            if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.shadow(c, b); ++k; }
         }
         mark(h, KIND_FINAL); K.final_(c, nb); ++k;
+        // The sun shadow rays of all bounces, traced together.
+        if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.shadow(c, 0); ++k; }
     }
     if (h->params.wireframes == 1) { mark(h, KIND_WIREFRAME); K.wireframe(c); ++k; }
     mark(h, KIND_FILM); K.film(c); ++k;
     mark(h, KIND_END); K.end_pass(c); ++k;
     mark(h, KIND_COUNT);
     return k;
+}
+
+int bounces_of(const dfpt_handle* h) {
+    const int d = h->params.pt_ray_depth_maximum;
+    return d < 1 ? 1 : (d > DFPT_MAX_DEPTH ? DFPT_MAX_DEPTH : d);
+}
+
+// Each path emits at most one shadow ray per bounce, so pixels x bounces rays always fit.
+int ensure_shadow_capacity(dfpt_handle* h) {
+    const size_t need = (size_t)h->n_pixels * (size_t)bounces_of(h);
+    if (h->shadow_capacity >= need) return DFPT_OK;
+    h->s_o.release(); h->s_d.release(); h->s_c.release();
+    CUDA_TRY(h->s_o.alloc(need));
+    CUDA_TRY(h->s_d.alloc(need));
+    CUDA_TRY(h->s_c.alloc(need));
+    h->shadow_capacity = need;
+    h->pass.s_o = h->s_o.p; h->pass.s_d = h->s_d.p; h->pass.s_c = h->s_c.p;
+    h->graph_valid = false;
+    return DFPT_OK;
 }
 
 int build_graph(dfpt_handle* h) {
@@ -604,10 +625,10 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
 
     const size_t n = (size_t)h->n_pixels;
     TRY_R(h->q_o0.alloc(n)); TRY_R(h->q_o1.alloc(n)); TRY_R(h->q_d0.alloc(n)); TRY_R(h->q_d1.alloc(n));
-    TRY_R(h->q_hit.alloc(n)); TRY_R(h->s_o.alloc(n)); TRY_R(h->s_d.alloc(n)); TRY_R(h->s_c.alloc(n));
+    TRY_R(h->q_hit.alloc(n));
     TRY_R(h->throughput.alloc(n)); TRY_R(h->radiance.alloc(n)); TRY_R(h->rng.alloc(n)); TRY_R(h->pixel_flags.alloc(n));
     TRY_R(h->primary_o.alloc(n)); TRY_R(h->primary_d.alloc(n));
-    TRY_R(h->counts.alloc(64)); TRY_R(h->stats.alloc(4)); TRY_R(h->pass_index.alloc(1)); TRY_R(h->mean.alloc(3));
+    TRY_R(h->counts.alloc(DFPT_COUNTS_SIZE)); TRY_R(h->stats.alloc(4)); TRY_R(h->pass_index.alloc(1)); TRY_R(h->mean.alloc(3));
     TRY_R(h->film_sum.alloc(n)); TRY_R(h->film_comp.alloc(n)); TRY_R(h->film_n.alloc(n)); TRY_R(h->bgra.alloc(n * 4));
     TRY_R(h->primitive_offsets.alloc(n));
     TRY_R(h->hit_prim.alloc(n)); TRY_R(h->hit_type.alloc(n)); TRY_R(h->hit_off.alloc(n)); TRY_R(h->hit_dist.alloc(n)); TRY_R(h->hit_normal.alloc(3 * n));
@@ -744,8 +765,28 @@ int dfpt_set_strict(dfpt_handle* h, int32_t strict) {
     h->use_strict = strict != 0;
     if (h->use_strict) h->strict.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
     else h->fast.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
+    h->ctx.grid_trace = kset(h).trace_grid(h->ctx.trace_config, h->sms);
     h->graph_valid = false;
     return DFPT_OK;
+}
+
+int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
+    if (!h || !key) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (std::strcmp(key, "trace_config") == 0) {
+        if (value < 0 || value >= h->fast.trace_configs) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "trace_config %d out of range", value);
+        h->ctx.trace_config = value;
+        h->ctx.grid_trace = kset(h).trace_grid(value, h->sms);
+        h->graph_valid = false;
+        return DFPT_OK;
+    }
+    return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
+}
+
+int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
+    if (!h || !key || !value) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (std::strcmp(key, "trace_config") == 0) { *value = h->ctx.trace_config; return DFPT_OK; }
+    if (std::strcmp(key, "trace_configs") == 0) { *value = h->fast.trace_configs; return DFPT_OK; }
+    return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 
 int dfpt_set_record_hits(dfpt_handle* h, int32_t enabled) {
@@ -777,6 +818,10 @@ int dfpt_render(dfpt_handle* h, int32_t passes) {
     if (passes < 0) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "passes < 0");
     if (h->counting) CUDA_TRY(cudaMemsetAsync(h->stats.p, 0, 4 * sizeof(unsigned long long), h->stream));
     if (passes == 0) return DFPT_OK;
+    {
+        int r = ensure_shadow_capacity(h);
+        if (r) return r;
+    }
     if (h->use_graph && !h->profiling) {
         if (!h->graph_valid) {
             int r = build_graph(h);

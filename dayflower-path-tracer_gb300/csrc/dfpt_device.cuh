@@ -296,10 +296,178 @@ struct TraceStats {
     uint32_t nodes, tris;
 };
 
+// Threaded-BVH walk of one mesh (GRK:1097-1194) in the reference's preorder: a node's box is
+// tested when it is visited, with the closest distance found so far; descend to the next node
+// (its left child) or skip to `next`. Returns true when an any-hit query found its hit.
+// V selects the implementation: 0 loads each node when it is reached; 1 issues the loads of both
+// possible successors (node + 1 and next) before the current node's slab test, so the dependent
+// load of the walk overlaps the test. Both visit the same nodes in the same order.
+template <bool ANY, int V>
+__device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo, float dxo,
+                                          float dyo, float dzo, Hit& h, TraceStats& st) {
+    const float ix = 1.0f / dxo, iy = 1.0f / dyo, iz = 1.0f / dzo;
+    int node = root;
+    float4 n0 = __ldg(S.nodes + 2 * node), n1 = __ldg(S.nodes + 2 * node + 1);
+    while (node != -1) {
+        st.nodes++;
+        const int next = __float_as_int(n0.w);
+        const int leaf = __float_as_int(n1.w);
+        float4 d0, d1, s0, s1;
+        if (V == 1) {
+            // node + 1 exists for every inner node (its left child); next is -1 or a later node.
+            const int dn = leaf == -1 ? node + 1 : node;
+            const int sn = next != -1 ? next : node;
+            d0 = __ldg(S.nodes + 2 * dn);
+            d1 = __ldg(S.nodes + 2 * dn + 1);
+            s0 = __ldg(S.nodes + 2 * sn);
+            s1 = __ldg(S.nodes + 2 * sn + 1);
+        }
+        const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
+        const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
+        const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
+        const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+        const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
+        if (tb >= 0.0f && leaf != -1) {
+            // Leaf: its triangles in order (-2 marks an empty leaf).
+            for (int k = leaf; k >= 0;) {
+                const float4 a = __ldg(S.tris + 3 * k);
+                const float4 e0 = __ldg(S.tris + 3 * k + 1);
+                const float4 e1 = __ldg(S.tris + 3 * k + 2);
+                st.tris++;
+                const float t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, a, e0, e1, h.t);
+                if (t < h.t) {
+                    h.t = t;
+                    h.prim = prim;
+                    h.shape_type = DFPT_SHAPE_TRIANGLE;
+                    h.shape_offset = __float_as_int(a.w);
+                }
+                if (ANY && h.prim != -1) return true;
+                k = __float_as_int(e0.w) != 0 ? -1 : k + 1;
+            }
+        }
+        const bool descend = tb >= 0.0f && leaf == -1;
+        node = descend ? node + 1 : next;
+        if (node == -1) break;
+        if (V == 1) {
+            n0 = descend ? d0 : s0;
+            n1 = descend ? d1 : s1;
+        } else {
+            n0 = __ldg(S.nodes + 2 * node);
+            n1 = __ldg(S.nodes + 2 * node + 1);
+        }
+    }
+    return false;
+}
+
+// Warp-synchronous form of the same walk: every lane keeps its own position in the preorder
+// sequence, and the warp always serves the smallest position among its active lanes; the lanes
+// standing on that node test it (one broadcast load), the others wait. Each lane therefore
+// visits exactly the nodes, in exactly the order, of mesh_walk, with the closest distance it
+// has at that moment; only the interleaving across lanes changes. All 32 lanes must call it
+// together; `active` marks lanes with a ray that still needs this mesh.
+template <bool ANY>
+__device__ __forceinline__ bool mesh_walk_warp(const DevScene& S, int root, int prim, bool active, float oxo, float oyo, float ozo,
+                                               float dxo, float dyo, float dzo, Hit& h, TraceStats& st) {
+    const float ix = 1.0f / dxo, iy = 1.0f / dyo, iz = 1.0f / dzo;
+    int cur = active ? root : -1;
+    bool found = false;
+    for (;;) {
+        const unsigned key = cur < 0 ? 0xFFFFFFFFu : (unsigned)cur;
+        const unsigned m = __reduce_min_sync(0xFFFFFFFFu, key);
+        if (m == 0xFFFFFFFFu) break;
+        if (key == m) {
+            const int node = (int)m;
+            const float4 n0 = __ldg(S.nodes + 2 * node), n1 = __ldg(S.nodes + 2 * node + 1);
+            st.nodes++;
+            const int next = __float_as_int(n0.w);
+            const int leaf = __float_as_int(n1.w);
+            const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
+            const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
+            const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
+            const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+            const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
+            bool stop = false;
+            if (tb >= 0.0f && leaf != -1) {
+                for (int k = leaf; k >= 0;) {
+                    const float4 a = __ldg(S.tris + 3 * k);
+                    const float4 e0 = __ldg(S.tris + 3 * k + 1);
+                    const float4 e1 = __ldg(S.tris + 3 * k + 2);
+                    st.tris++;
+                    const float t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, a, e0, e1, h.t);
+                    if (t < h.t) {
+                        h.t = t;
+                        h.prim = prim;
+                        h.shape_type = DFPT_SHAPE_TRIANGLE;
+                        h.shape_offset = __float_as_int(a.w);
+                    }
+                    if (ANY && h.prim != -1) { stop = true; break; }
+                    k = __float_as_int(e0.w) != 0 ? -1 : k + 1;
+                }
+            }
+            if (stop) {
+                found = true;
+                cur = -1;
+            } else {
+                cur = (tb >= 0.0f && leaf == -1) ? node + 1 : next;
+            }
+        }
+    }
+    return found;
+}
+
+// trace() for all 32 lanes of a warp together (the warp-synchronous walk); `valid` marks lanes
+// with a ray. Same results as trace<ANY, 0> for every valid lane.
+template <bool ANY>
+__device__ Hit trace_warp(const DevScene& S, bool valid, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
+    Hit h;
+    h.t = INF;
+    h.prim = -1;
+    h.shape_type = -1;
+    h.shape_offset = -1;
+    bool done = !valid;
+    const int np = S.primitive_count;
+    for (int i = 0; i < np; ++i) {
+        const int4 info = __ldg(S.prim_info + i);
+        const float4* W = reinterpret_cast<const float4*>(S.w2o) + i * 4;
+        const float4 r0 = __ldg(W), r1 = __ldg(W + 1), r2 = __ldg(W + 2);
+        const float oxo = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
+        const float oyo = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
+        const float ozo = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
+        const float dxo = r0.x * dx + r0.y * dy + r0.z * dz;
+        const float dyo = r1.x * dx + r1.y * dy + r1.z * dz;
+        const float dzo = r2.x * dx + r2.y * dy + r2.z * dz;
+        float t = INF;
+        const int type = info.x;
+        if (type == DFPT_SHAPE_TRIANGLE_MESH) {
+            if (mesh_walk_warp<ANY>(S, info.w, i, !done, oxo, oyo, ozo, dxo, dyo, dzo, h, st)) done = true;
+        } else if (!done) {
+            if (type == DFPT_SHAPE_PLANE) {
+                t = isect_plane(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.plane_a + info.w), __ldg(S.plane_n + info.w), h.t);
+            } else if (type == DFPT_SHAPE_SPHERE) {
+                t = isect_sphere(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.sphere4 + info.w), h.t);
+            } else if (type == DFPT_SHAPE_TERRAIN) {
+                t = isect_terrain(oxo, oyo, ozo, dxo, dyo, dzo);
+            } else if (type == DFPT_SHAPE_TRIANGLE) {
+                st.tris++;
+                t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.tris + 3 * info.w), __ldg(S.tris + 3 * info.w + 1),
+                                   __ldg(S.tris + 3 * info.w + 2), h.t);
+            }
+            if (t < h.t) {
+                h.t = t;
+                h.prim = i;
+                h.shape_type = type;
+                h.shape_offset = info.y;
+            }
+            if (ANY && h.prim != -1) done = true;
+        }
+    }
+    return h;
+}
+
 // doIntersectPrimitives (GRK:1048-1256): a linear loop over primitives, each ray transformed
 // to object space; meshes walk the threaded (preorder, skip-pointer) BVH exactly as flattened.
 // ANY = isTesting: return at the first primitive with a hit.
-template <bool ANY>
+template <bool ANY, int V = 0>
 __device__ Hit trace(const DevScene& S, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
     Hit h;
     h.t = INF;
@@ -320,45 +488,8 @@ __device__ Hit trace(const DevScene& S, float ox, float oy, float oz, float dx, 
         float t = INF;
         const int type = info.x;
         if (type == DFPT_SHAPE_TRIANGLE_MESH) {
-            const float ix = 1.0f / dxo, iy = 1.0f / dyo, iz = 1.0f / dzo;
-            int node = info.w;
-            while (node != -1) {
-                const float4 n0 = __ldg(S.nodes + 2 * node);
-                const float4 n1 = __ldg(S.nodes + 2 * node + 1);
-                st.nodes++;
-                const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
-                const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
-                const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
-                const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
-                const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
-                const int next = __float_as_int(n0.w);
-                const int leaf = __float_as_int(n1.w);
-                if (tb < 0.0f) {
-                    node = next;
-                } else if (leaf == -1) {
-                    node = node + 1;
-                } else {
-                    int k = leaf;  // -2 marks an empty leaf
-                    for (; k >= 0;) {
-                        const float4 a = __ldg(S.tris + 3 * k);
-                        const float4 e0 = __ldg(S.tris + 3 * k + 1);
-                        const float4 e1 = __ldg(S.tris + 3 * k + 2);
-                        st.tris++;
-                        t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, a, e0, e1, h.t);
-                        if (t < h.t) {
-                            h.t = t;
-                            h.prim = i;
-                            h.shape_type = DFPT_SHAPE_TRIANGLE;
-                            h.shape_offset = __float_as_int(a.w);
-                        }
-                        if (ANY && h.prim != -1) return h;
-                        if (__float_as_int(e0.w) != 0) break;
-                        ++k;
-                    }
-                    node = next;
-                }
-            }
-            t = INF;  // the mesh updated the closest hit in place
+            // The mesh updates the closest hit in place; t stays INF for the check below.
+            if (mesh_walk<ANY, V>(S, info.w, i, oxo, oyo, ozo, dxo, dyo, dzo, h, st)) return h;
         } else if (type == DFPT_SHAPE_PLANE) {
             t = isect_plane(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.plane_a + info.w), __ldg(S.plane_n + info.w), h.t);
         } else if (type == DFPT_SHAPE_SPHERE) {
@@ -378,6 +509,23 @@ __device__ Hit trace(const DevScene& S, float ox, float oy, float oz, float dx, 
         }
         if (ANY && h.prim != -1) return h;
     }
+    return h;
+}
+
+// Selects the walk: V 0/1 per-lane (every lane may call it alone), V 2 warp-synchronous (all 32
+// lanes call it; invalid lanes pass valid = false).
+template <bool ANY, int V>
+__device__ __forceinline__ Hit trace_v(const DevScene& S, bool valid, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
+    if constexpr (V == 2) {
+        return trace_warp<ANY>(S, valid, ox, oy, oz, dx, dy, dz, st);
+    } else {
+        if (valid) return trace<ANY, V>(S, ox, oy, oz, dx, dy, dz, st);
+    }
+    Hit h;
+    h.t = INF;
+    h.prim = -1;
+    h.shape_type = -1;
+    h.shape_offset = -1;
     return h;
 }
 

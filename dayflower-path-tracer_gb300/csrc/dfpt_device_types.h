@@ -88,7 +88,7 @@ struct DevPass {
     int* pixel_flags;     // bit 0: film set to black this pass
     float4* primary_o;    // primary rays (wireframe overlay)
     float4* primary_d;
-    int* counts;          // [0..31] ray queue counts per bounce, [32..63] shadow counts
+    int* counts;          // [0..31] ray queue counts per bounce, [32] deferred shadow rays, [64..95] work fetch
     unsigned long long* stats;  // closest, any, nodes, triangles
     int* pass_index;      // device pass counter
     // Film (Kahan-compensated sums), image and selection buffers.
@@ -106,4 +106,6 @@ struct DevPass {
 };
 
 #define DFPT_COUNTS_SHADOW 32
+#define DFPT_COUNTS_FETCH 64  // [64..95]: work-fetch counters of the traversal launches
 #define DFPT_MAX_DEPTH 30
+#define DFPT_COUNTS_SIZE 128

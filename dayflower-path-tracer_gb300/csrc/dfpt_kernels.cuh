@@ -462,6 +462,14 @@ __device__ __forceinline__ void warp_add_stats(const DevParams& P, unsigned long
     }
 }
 
+// Warp-level dynamic work distribution: each warp takes the next 32 queue entries from a counter
+// (reset at the start of the pass), so warps that drew short rays keep taking more. All 32 lanes
+// iterate together (i >= n marks lanes without an entry).
+#define WARP_DYNAMIC(i, n, counter)                                                            \
+    for (int i##_base = 0;;)                                                                   \
+        if ((i##_base = __shfl_sync(0xFFFFFFFFu, (threadIdx.x & 31) == 0 ? atomicAdd((counter), 32) : 0, 0)) >= (n)) break; \
+        else for (int i = i##_base + (int)(threadIdx.x & 31), i##_once = 1; i##_once; i##_once = 0)
+
 #define GRID_STRIDE_UNIFORM(i, n)                                                              \
     for (int i##_base = blockIdx.x * blockDim.x; i##_base < (n); i##_base += gridDim.x * blockDim.x) \
         for (int i = i##_base + (int)threadIdx.x, i##_once = 1; i##_once; i##_once = 0)
@@ -500,20 +508,25 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S, const DevParams* __r
     }
 }
 
-template <bool ANY>
-__global__ void __launch_bounds__(256) k_trace(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce, int which_queue) {
+// Traversal kernels are instantiated per tuning configuration (walk variant, block size, resident
+// blocks per SM); see TRACE_CONFIGS.
+template <bool ANY, int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce, int which_queue) {
     const DevParams& P = *Pp;
     const int n = B.counts[bounce];
     const float4* __restrict__ qo = B.q_o[which_queue];
     const float4* __restrict__ qd = B.q_d[which_queue];
-    GRID_STRIDE_UNIFORM(i, n) {
+    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + bounce) {
         TraceStats st{0, 0};
-        if (i < n) {
-            const float4 o = qo[i], d = qd[i];
-            const Hit h = trace<ANY>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
+        const bool valid = i < n;
+        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+        if (valid) {
+            o = qo[i];
+            d = qd[i];
         }
-        warp_add_stats(P, B.stats, ANY ? 1 : 0, i < n ? 1u : 0u, st.nodes, st.tris);
+        const Hit h = trace_v<ANY, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
+        if (valid) B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
+        warp_add_stats(P, B.stats, ANY ? 1 : 0, valid ? 1u : 0u, st.nodes, st.tris);
     }
 }
 
@@ -704,7 +717,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __re
             B.q_o[qi ^ 1][slot] = no;
             B.q_d[qi ^ 1][slot] = nd;
         }
-        const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW + bounce, emit_shadow);
+        const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
         if (sslot >= 0) {
             B.s_o[sslot] = so;
             B.s_d[sslot] = sd;
@@ -713,37 +726,53 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __re
     }
 }
 
-// Sun visibility: any hit (GRK:2324-2340); unoccluded samples add their contribution.
-__global__ void __launch_bounds__(256) k_shadow(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+// Sun visibility: any hit (GRK:2324-2340); unoccluded samples add their contribution. The shadow
+// rays of every bounce of the pass wait in one queue and are traced in a single launch after the
+// last bounce (their contributions only add to the path radiance).
+template <int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
     const DevParams& P = *Pp;
-    const int n = B.counts[DFPT_COUNTS_SHADOW + bounce];
-    GRID_STRIDE_UNIFORM(i, n) {
+    const int n = B.counts[DFPT_COUNTS_SHADOW];
+    (void)bounce;
+    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1) {
         TraceStats st{0, 0};
-        if (i < n) {
-            const float4 o = B.s_o[i], d = B.s_d[i];
-            const Hit h = trace<true>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            if (h.t >= INF - 0.0001f) {
-                const int path = __float_as_int(o.w);
-                const float4 c = B.s_c[i];
-                float4 L = B.radiance[path];
-                L.x += c.x; L.y += c.y; L.z += c.z;
-                B.radiance[path] = L;
-            }
+        const bool valid = i < n;
+        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+        if (valid) {
+            o = B.s_o[i];
+            d = B.s_d[i];
         }
-        warp_add_stats(P, B.stats, 1, i < n ? 1u : 0u, st.nodes, st.tris);
+        const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
+        if (valid && h.t >= INF - 0.0001f) {
+            // A path has up to one shadow ray per bounce in this queue, so several threads may add
+            // to the same path: atomics (the sum's order, and so its last bit, may vary).
+            const int path = __float_as_int(o.w);
+            const float4 c = B.s_c[i];
+            float* L = reinterpret_cast<float*>(B.radiance + path);
+            atomicAdd(L, c.x);
+            atomicAdd(L + 1, c.y);
+            atomicAdd(L + 2, c.z);
+        }
+        warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
     }
 }
 
 // After the last bounce: any-hit test of the continuation ray, sky if it escapes (GRK:3689-3701).
-__global__ void __launch_bounds__(256) k_final(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+template <int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
     const DevParams& P = *Pp;
     const int n = B.counts[bounce];
     const int qi = bounce & 1;
-    GRID_STRIDE_UNIFORM(i, n) {
+    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + bounce) {
         TraceStats st{0, 0};
-        if (i < n) {
-            const float4 o = B.q_o[qi][i], d = B.q_d[qi][i];
-            const Hit h = trace<true>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
+        const bool valid = i < n;
+        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+        if (valid) {
+            o = B.q_o[qi][i];
+            d = B.q_d[qi][i];
+        }
+        const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
+        if (valid) {
             if (!(h.t < INF)) {
                 const int path = __float_as_int(o.w);
                 const float4 T = B.throughput[path];
@@ -755,7 +784,7 @@ __global__ void __launch_bounds__(256) k_final(DevScene S, const DevParams* __re
                 B.radiance[path] = L;
             }
         }
-        warp_add_stats(P, B.stats, 1, i < n ? 1u : 0u, st.nodes, st.tris);
+        warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
     }
 }
 
@@ -1090,13 +1119,62 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
 // ---------------------------------------------------------------------------------------------
 // Host-side launchers (the kernel set of this translation unit).
 
-static void launch_camera(const LaunchCtx& c) { k_camera<<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
+// Tuning configurations of the traversal kernels: {walk variant, block size, resident blocks}.
+#define TRACE_CONFIGS(X) X(0, 0, 256, 4) X(1, 1, 256, 4) X(2, 1, 256, 3) X(3, 0, 128, 8) X(4, 2, 256, 4) X(5, 2, 128, 8) X(6, 2, 256, 3)
+
+template <int V, int BLOCK, int MINB>
+struct TraceCfg {
+    static void closest(const LaunchCtx& c, int bounce) {
+        k_trace<false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce, bounce & 1);
+    }
+    static void shadow(const LaunchCtx& c, int bounce) {
+        k_shadow<V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+    }
+    static void final_(const LaunchCtx& c, int bounce) {
+        k_final<V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+    }
+    static int grid(int sms) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<false, V, BLOCK, MINB>, BLOCK, 0);
+        return sms * (b > 0 ? b : 1);
+    }
+};
+
 static void launch_trace_closest(const LaunchCtx& c, int bounce) {
-    k_trace<false><<<c.grid_trace, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce, bounce & 1);
+    switch (c.trace_config) {
+#define X(id, v, b, m) case id: TraceCfg<v, b, m>::closest(c, bounce); break;
+        TRACE_CONFIGS(X)
+#undef X
+        default: TraceCfg<0, 256, 4>::closest(c, bounce);
+    }
 }
+static void launch_shadow(const LaunchCtx& c, int bounce) {
+    switch (c.trace_config) {
+#define X(id, v, b, m) case id: TraceCfg<v, b, m>::shadow(c, bounce); break;
+        TRACE_CONFIGS(X)
+#undef X
+        default: TraceCfg<0, 256, 4>::shadow(c, bounce);
+    }
+}
+static void launch_final(const LaunchCtx& c, int bounce) {
+    switch (c.trace_config) {
+#define X(id, v, b, m) case id: TraceCfg<v, b, m>::final_(c, bounce); break;
+        TRACE_CONFIGS(X)
+#undef X
+        default: TraceCfg<0, 256, 4>::final_(c, bounce);
+    }
+}
+static int trace_grid(int config, int sms) {
+    switch (config) {
+#define X(id, v, b, m) case id: return TraceCfg<v, b, m>::grid(sms);
+        TRACE_CONFIGS(X)
+#undef X
+        default: return TraceCfg<0, 256, 4>::grid(sms);
+    }
+}
+
+static void launch_camera(const LaunchCtx& c) { k_camera<<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_shade(const LaunchCtx& c, int bounce) { k_shade<<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce); }
-static void launch_shadow(const LaunchCtx& c, int bounce) { k_shadow<<<c.grid_trace, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce); }
-static void launch_final(const LaunchCtx& c, int bounce) { k_final<<<c.grid_trace, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce); }
 static void launch_simple(const LaunchCtx& c) { k_simple<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_wireframe(const LaunchCtx& c) { k_wireframe<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_film(const LaunchCtx& c) { k_film<<<c.grid, 256, 0, c.stream>>>(c.params, *c.pass); }
@@ -1108,12 +1186,11 @@ static void launch_film_average(const LaunchCtx& c, float* rgb, int* samples) {
 static void launch_init_tables(cudaStream_t s, const int* perm, const float* grad) { k_init_tables<<<1, 512, 0, s>>>(perm, grad); }
 
 static void occupancy(int sms, int& grid, int& grid_trace, int& grid_simple) {
-    int b1 = 0, b2 = 0, b3 = 0;
+    int b1 = 0, b3 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_shade, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_trace<false>, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_simple, 128, 0);
     grid = sms * (b1 > 0 ? b1 : 1);
-    grid_trace = sms * (b2 > 0 ? b2 : 1);
+    grid_trace = trace_grid(0, sms);
     grid_simple = sms * (b3 > 0 ? b3 : 1);
 }
 
@@ -1132,6 +1209,8 @@ KernelSet kernel_set() {
     k.film_average = launch_film_average;
     k.init_tables = launch_init_tables;
     k.occupancy = occupancy;
+    k.trace_grid = trace_grid;
+    k.trace_configs = 7;
     return k;
 }
 

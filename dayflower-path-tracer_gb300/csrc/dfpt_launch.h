@@ -11,6 +11,7 @@ struct LaunchCtx {
     const DevPass* pass;
     cudaStream_t stream;
     int grid, grid_trace, grid_simple;
+    int trace_config;  // index into the kernel set's traversal configurations
 };
 
 struct KernelSet {
@@ -27,6 +28,8 @@ struct KernelSet {
     void (*film_average)(const LaunchCtx&, float* rgb, int* samples);
     void (*init_tables)(cudaStream_t, const int* perm256, const float* grad36);
     void (*occupancy)(int sms, int& grid, int& grid_trace, int& grid_simple);
+    int (*trace_grid)(int config, int sms);
+    int trace_configs;
 };
 
 namespace dfpt_fast { KernelSet kernel_set(); }

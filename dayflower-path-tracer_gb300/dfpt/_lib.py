@@ -113,6 +113,8 @@ SIGNATURES = {
     "dfpt_set_counting": (C.c_int, [C.c_void_p, C.c_int32]),
     "dfpt_launch_count": (C.c_int, [C.c_void_p, u64p]),
     "dfpt_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
+    "dfpt_set_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
+    "dfpt_get_tuning": (C.c_int, [C.c_void_p, C.c_char_p, i32p]),
     "dfpt_read_profile": (C.c_int, [C.c_void_p, f64p, i32p]),
     "dfpt_last_error": (C.c_char_p, []),
     "dfpt_builder_create": (C.c_int, [C.POINTER(C.c_void_p)]),

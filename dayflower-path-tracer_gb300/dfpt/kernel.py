@@ -167,6 +167,14 @@ class RendererKernel:
         check(self._lib.dfpt_read_profile(self._need(), ptr(ms, C.c_double), ptr(n, C.c_int32)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PROFILE_KINDS)}
 
+    def set_tuning(self, key: str, value: int) -> None:
+        check(self._lib.dfpt_set_tuning(self._need(), key.encode(), int(value)))
+
+    def get_tuning(self, key: str) -> int:
+        v = C.c_int32()
+        check(self._lib.dfpt_get_tuning(self._need(), key.encode(), C.byref(v)))
+        return int(v.value)
+
     def launch_count(self) -> int:
         c = C.c_uint64()
         check(self._lib.dfpt_launch_count(self._need(), C.byref(c)))

@@ -205,6 +205,12 @@ int dfpt_set_counting(dfpt_handle* handle, int32_t enabled);
 int dfpt_set_profiling(dfpt_handle* handle, int32_t enabled);
 int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind9, int32_t* launches_by_kind9);
 
+/* Launch tuning. Key "trace_config" picks the configuration of the traversal kernels (walk
+ * variant x block size x resident blocks per SM, 0..N-1, N readable as "trace_configs"); every
+ * configuration visits the same nodes in the same order, so results do not depend on it. */
+int dfpt_set_tuning(dfpt_handle* handle, const char* key, int32_t value);
+int dfpt_get_tuning(dfpt_handle* handle, const char* key, int32_t* value);
+
 /* Number of kernels the handle launched since it was created (for launch accounting). */
 int dfpt_launch_count(dfpt_handle* handle, uint64_t* launches);
 

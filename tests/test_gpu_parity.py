@@ -182,3 +182,29 @@ def test_wireframes_and_selection(scenes, oracle_mod):
         assert img[h // 2, w // 2, 1] >= 200  # green channel tinted
     assert offs[(h // 2) * w + w // 2] == (sel * 3 if sel >= 0 else -1)
     k.dispose()
+
+
+def test_trace_configs_agree(scenes):
+    """Every traversal launch configuration visits the same nodes and finds the same hits (a fresh
+    handle per configuration, so every run draws from pass 0 of the same stream)."""
+    scene, sky, params, (w, h) = scenes["meshes"]
+    ref = None
+    n = None
+    cfg = 0
+    while n is None or cfg < n:
+        k = _kernel(scene, sky, dict(params, renderer_type=2), w, h, strict=False, hits=True)
+        n = k.get_tuning("trace_configs")
+        k.set_tuning("trace_config", cfg)
+        k.set_counting(True)
+        k.execute(1)
+        film, _ = k.film()
+        got = (k.hits()[0].copy(), film.copy(), k.counters().copy())
+        k.dispose()
+        if ref is None:
+            ref = got
+        else:
+            assert np.array_equal(got[0], ref[0]), cfg
+            assert np.array_equal(got[2], ref[2]), cfg  # same segments, nodes and triangles
+            # Shadow contributions of one path are added with float atomics in any order: a few ulps.
+            assert np.allclose(got[1], ref[1], rtol=1e-5, atol=1e-6), (cfg, np.abs(got[1] - ref[1]).max())
+        cfg += 1
