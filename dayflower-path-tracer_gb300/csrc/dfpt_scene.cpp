@@ -14,6 +14,7 @@
 #include "dfpt_internal.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -64,8 +65,66 @@ struct Distinct {
     }
 };
 
-Key key3(float x, float y, float z) { return Key{{fbits(x), fbits(y), fbits(z)}}; }
-Key key2(float x, float y) { return Key{{fbits(x), fbits(y)}}; }
+// Fixed-size keys for the large sets (points, vectors, triangles): no allocation per key.
+template <size_t N>
+struct KeyN {
+    std::array<uint32_t, N> w;
+    bool operator==(const KeyN& o) const { return w == o.w; }
+};
+template <size_t N>
+struct KeyNHash {
+    size_t operator()(const KeyN<N>& k) const {
+        uint64_t h = 1469598103934665603ull;
+        for (uint32_t x : k.w) { h ^= x; h *= 1099511628211ull; }
+        h ^= h >> 29;
+        h *= 0xbf58476d1ce4e5b9ull;
+        return (size_t)(h ^ (h >> 32));
+    }
+};
+// First-occurrence-ordered set over fixed-size keys: open addressing, linear probing.
+template <size_t N>
+struct DistinctN {
+    std::vector<KeyN<N>> order;
+    std::vector<int32_t> slot;  // -1 empty, else index into order
+    size_t mask = 0;
+    void grow() {
+        const size_t cap = slot.empty() ? 1024 : slot.size() * 2;
+        slot.assign(cap, -1);
+        mask = cap - 1;
+        for (size_t i = 0; i < order.size(); ++i) {
+            size_t h = KeyNHash<N>()(order[i]) & mask;
+            while (slot[h] >= 0) h = (h + 1) & mask;
+            slot[h] = (int32_t)i;
+        }
+    }
+    int add(const KeyN<N>& k) {
+        if ((order.size() + 1) * 2 > slot.size()) grow();
+        size_t h = KeyNHash<N>()(k) & mask;
+        for (;;) {
+            const int32_t s = slot[h];
+            if (s < 0) {
+                slot[h] = (int32_t)order.size();
+                order.push_back(k);
+                return slot[h];
+            }
+            if (order[s] == k) return s;
+            h = (h + 1) & mask;
+        }
+    }
+    int find(const KeyN<N>& k) const {
+        if (slot.empty()) return -1;
+        size_t h = KeyNHash<N>()(k) & mask;
+        for (;;) {
+            const int32_t s = slot[h];
+            if (s < 0) return -1;
+            if (order[s] == k) return s;
+            h = (h + 1) & mask;
+        }
+    }
+};
+
+KeyN<3> key3(float x, float y, float z) { return KeyN<3>{{fbits(x), fbits(y), fbits(z)}}; }
+KeyN<2> key2(float x, float y) { return KeyN<2>{{fbits(x), fbits(y)}}; }
 
 struct V3 { float x, y, z; };
 
@@ -73,16 +132,16 @@ struct Vertex { float p[3], n[3], uv[2], t[3]; };
 
 struct Tri { Vertex v[3]; };
 
-Key tri_key(const Tri& t) {
-    Key k;
-    k.w.reserve(33);
+KeyN<33> tri_key(const Tri& t) {
+    KeyN<33> k;
+    int n = 0;
     for (int i = 0; i < 3; ++i) {
         const Vertex& v = t.v[i];
         // Vertex.equals compares texture coordinates, position, normal, tangent.
-        for (float f : v.uv) k.w.push_back(fbits(f));
-        for (float f : v.p) k.w.push_back(fbits(f));
-        for (float f : v.n) k.w.push_back(fbits(f));
-        for (float f : v.t) k.w.push_back(fbits(f));
+        for (float f : v.uv) k.w[n++] = fbits(f);
+        for (float f : v.p) k.w[n++] = fbits(f);
+        for (float f : v.n) k.w[n++] = fbits(f);
+        for (float f : v.t) k.w[n++] = fbits(f);
     }
     return k;
 }
@@ -155,8 +214,69 @@ SplitResult eval_split(const std::vector<BvhItem>& items, int axis, float split)
     return r;
 }
 
+// The same search restated with per-axis sorted item lists, O(n log n) per tree level instead of
+// O(candidates x n) per node. For a candidate split s on an axis, the left group is every item
+// whose centroid is < s: a prefix of the items sorted by that centroid, so its bounds are a prefix
+// max/min and its count a position in the sorted list. Max/min of non-NaN floats do not depend on
+// the order they are taken in (a NaN makes the cost NaN in either order), so every candidate's
+// count and cost - and with it the chosen split - are the ones the reference's item loop gives.
+// The chosen partition and the child bounds are still computed by the item loop in list order.
+struct SortedSweep {
+    const std::vector<BvhItem>* items = nullptr;  // all items of the mesh, by id
+    const std::vector<float>* cen[3] = {nullptr, nullptr, nullptr};
+    // prefix (k items) and suffix (items k..n-1) bounds: mx, my, mz, nx, ny, nz
+    std::vector<float> pre, suf;
+
+    void bounds_scan(const std::vector<int>& order) {
+        const size_t n = order.size();
+        pre.resize((n + 1) * 6);
+        suf.resize((n + 1) * 6);
+        float* P = pre.data();
+        P[0] = P[1] = P[2] = -FLT_MAX_F;
+        P[3] = P[4] = P[5] = FLT_MAX_F;
+        for (size_t k = 0; k < n; ++k) {
+            const BvhItem& it = (*items)[order[k]];
+            const float* a = P + k * 6;
+            float* b = P + (k + 1) * 6;
+            b[0] = jmax(a[0], it.mx); b[1] = jmax(a[1], it.my); b[2] = jmax(a[2], it.mz);
+            b[3] = jmin(a[3], it.nx); b[4] = jmin(a[4], it.ny); b[5] = jmin(a[5], it.nz);
+        }
+        float* S = suf.data();
+        float* e = S + n * 6;
+        e[0] = e[1] = e[2] = -FLT_MAX_F;
+        e[3] = e[4] = e[5] = FLT_MAX_F;
+        for (size_t k = n; k-- > 0;) {
+            const BvhItem& it = (*items)[order[k]];
+            const float* a = S + (k + 1) * 6;
+            float* b = S + k * 6;
+            b[0] = jmax(a[0], it.mx); b[1] = jmax(a[1], it.my); b[2] = jmax(a[2], it.mz);
+            b[3] = jmin(a[3], it.nx); b[4] = jmin(a[4], it.ny); b[5] = jmin(a[5], it.nz);
+        }
+    }
+
+    static float cost_of(const float* l, int cl, const float* r, int cr) {
+        const float slx = l[0] - l[3], sly = l[1] - l[4], slz = l[2] - l[5];
+        const float srx = r[0] - r[3], sry = r[1] - r[4], srz = r[2] - r[5];
+        const float sl = slx * sly + sly * slz + slz * slx;
+        const float sr = srx * sry + sry * srz + srz * srx;
+        return sl * (float)cl + sr * (float)cr;
+    }
+};
+
+// Orders item ids by one centroid coordinate, NaN last (a NaN centroid is never < a split).
+struct CentroidLess {
+    const float* v;
+    bool operator()(int a, int b) const {
+        const float x = v[a], y = v[b];
+        if (y != y) return x == x;
+        return x < y;
+    }
+};
+
 struct BvhBuilder {
     int threads = 1;
+    bool exhaustive = false;  // evaluate every candidate with the item loop (test cross-check)
+    std::atomic<int> spawned{0};
 
     std::unique_ptr<BvhNode> make_leaf(const std::vector<BvhItem>& items, int depth) {
         auto leaf = std::make_unique<BvhNode>();
@@ -164,6 +284,19 @@ struct BvhBuilder {
         leaf->depth = depth;
         for (const BvhItem& it : items) leaf->tris.push_back(it.tri);
         return leaf;
+    }
+
+    // The candidate list in loop order; float stepping exactly as the reference's for-loop.
+    static void candidates(int depth, float mx, float my, float mz, float nx, float ny, float nz,
+                           std::vector<std::pair<int, float>>& cands) {
+        cands.clear();
+        for (int axis = 0; axis < 3; ++axis) {
+            const float start = axis == 0 ? nx : axis == 1 ? ny : nz;
+            const float stop = axis == 0 ? mx : axis == 1 ? my : mz;
+            if (std::fabs(stop - start) < 1.0e-4f) continue;
+            const float step = (stop - start) / (1024.0f / ((float)depth + 1.0f));
+            for (float split = start + step; split < stop - step; split += step) cands.emplace_back(axis, split);
+        }
     }
 
     std::unique_ptr<BvhNode> build(std::vector<BvhItem>& items, int depth, float mx, float my, float mz,
@@ -174,15 +307,8 @@ struct BvhBuilder {
         float minimum_cost = (float)size0 * (sx * sy + sy * sz + sz * sx);
         float best_split = FLT_MAX_F;
         int best_axis = -1;
-        // The candidate list in loop order; float stepping exactly as the reference's for-loop.
         std::vector<std::pair<int, float>> cands;
-        for (int axis = 0; axis < 3; ++axis) {
-            const float start = axis == 0 ? nx : axis == 1 ? ny : nz;
-            const float stop = axis == 0 ? mx : axis == 1 ? my : mz;
-            if (std::fabs(stop - start) < 1.0e-4f) continue;
-            const float step = (stop - start) / (1024.0f / ((float)depth + 1.0f));
-            for (float split = start + step; split < stop - step; split += step) cands.emplace_back(axis, split);
-        }
+        candidates(depth, mx, my, mz, nx, ny, nz, cands);
         const size_t nc = cands.size();
         std::vector<SplitResult> res(nc);
         const long work = (long)nc * (long)size0;
@@ -244,6 +370,103 @@ struct BvhBuilder {
         return tree;
     }
 
+    // The sorted-list form of build(). `ids` is the node's item list in the reference's order;
+    // `by[a]` the same ids sorted by centroid a. Children get stable partitions of all four lists,
+    // which stay sorted, so the mesh is sorted once.
+    std::unique_ptr<BvhNode> build_sorted(const std::vector<BvhItem>& all, const std::vector<float>* cen,
+                                          std::vector<int>& ids, std::vector<int>* by, int depth,
+                                          float mx, float my, float mz, float nx, float ny, float nz) {
+        const int size0 = (int)ids.size();
+        if (size0 < 4) {
+            auto leaf = std::make_unique<BvhNode>();
+            leaf->leaf = true;
+            leaf->depth = depth;
+            for (int id : ids) leaf->tris.push_back(all[id].tri);
+            return leaf;
+        }
+        const float sx = mx - nx, sy = my - ny, sz = mz - nz;
+        float minimum_cost = (float)size0 * (sx * sy + sy * sz + sz * sx);
+        float best_split = FLT_MAX_F;
+        int best_axis = -1;
+        std::vector<std::pair<int, float>> cands;
+        candidates(depth, mx, my, mz, nx, ny, nz, cands);
+        SortedSweep sw;
+        sw.items = &all;
+        size_t ci = 0;
+        for (int axis = 0; axis < 3 && ci < cands.size(); ++axis) {
+            if (cands[ci].first != axis) continue;
+            const std::vector<int>& order = by[axis];
+            const float* v = cen[axis].data();
+            sw.bounds_scan(order);
+            int k = 0;  // items with centroid < split, in sorted order
+            for (; ci < cands.size() && cands[ci].first == axis; ++ci) {
+                const float split = cands[ci].second;
+                while (k < size0 && v[order[k]] < split) ++k;
+                const int cl = k, cr = size0 - k;
+                if (cl <= 1 || cr <= 1) continue;
+                const float cost = SortedSweep::cost_of(sw.pre.data() + (size_t)k * 6, cl, sw.suf.data() + (size_t)k * 6, cr);
+                if (cost < minimum_cost) {
+                    minimum_cost = cost;
+                    best_split = split;
+                    best_axis = axis;
+                }
+            }
+        }
+        if (best_axis == -1) {
+            auto leaf = std::make_unique<BvhNode>();
+            leaf->leaf = true;
+            leaf->depth = depth;
+            for (int id : ids) leaf->tris.push_back(all[id].tri);
+            return leaf;
+        }
+        float mlx = -FLT_MAX_F, mly = -FLT_MAX_F, mlz = -FLT_MAX_F, nlx = FLT_MAX_F, nly = FLT_MAX_F, nlz = FLT_MAX_F;
+        float mrx = -FLT_MAX_F, mry = -FLT_MAX_F, mrz = -FLT_MAX_F, nrx = FLT_MAX_F, nry = FLT_MAX_F, nrz = FLT_MAX_F;
+        const float* vb = cen[best_axis].data();
+        std::vector<int> lid, rid;
+        lid.reserve(size0);
+        rid.reserve(size0);
+        for (int id : ids) {
+            const BvhItem& it = all[id];
+            if (vb[id] < best_split) {
+                lid.push_back(id);
+                mlx = jmax(mlx, it.mx); mly = jmax(mly, it.my); mlz = jmax(mlz, it.mz);
+                nlx = jmin(nlx, it.nx); nly = jmin(nly, it.ny); nlz = jmin(nlz, it.nz);
+            } else {
+                rid.push_back(id);
+                mrx = jmax(mrx, it.mx); mry = jmax(mry, it.my); mrz = jmax(mrz, it.mz);
+                nrx = jmin(nrx, it.nx); nry = jmin(nry, it.ny); nrz = jmin(nrz, it.nz);
+            }
+        }
+        std::vector<int> lby[3], rby[3];
+        for (int a = 0; a < 3; ++a) {
+            lby[a].reserve(lid.size());
+            rby[a].reserve(rid.size());
+            for (int id : by[a]) (vb[id] < best_split ? lby[a] : rby[a]).push_back(id);
+            std::vector<int>().swap(by[a]);
+        }
+        std::vector<int>().swap(ids);
+        std::unique_ptr<BvhNode> node_left, node_right;
+        auto run_left = [&]() { node_left = build_sorted(all, cen, lid, lby, depth + 1, mlx, mly, mlz, nlx, nly, nlz); };
+        // Large subtrees build on their own thread (the tree does not depend on the schedule).
+        if (size0 > 20000 && spawned.fetch_add(1) < threads - 1) {
+            std::thread t(run_left);
+            node_right = build_sorted(all, cen, rid, rby, depth + 1, mrx, mry, mrz, nrx, nry, nrz);
+            t.join();
+        } else {
+            run_left();
+            node_right = build_sorted(all, cen, rid, rby, depth + 1, mrx, mry, mrz, nrx, nry, nrz);
+        }
+        node_left->mx = mlx; node_left->my = mly; node_left->mz = mlz;
+        node_left->nx = nlx; node_left->ny = nly; node_left->nz = nlz;
+        node_right->mx = mrx; node_right->my = mry; node_right->mz = mrz;
+        node_right->nx = nrx; node_right->ny = nry; node_right->nz = nrz;
+        auto tree = std::make_unique<BvhNode>();
+        tree->depth = depth;
+        tree->left = std::move(node_left);
+        tree->right = std::move(node_right);
+        return tree;
+    }
+
     std::unique_ptr<BvhNode> create(const std::vector<Tri>& tris) {
         std::vector<BvhItem> items;
         items.reserve(tris.size());
@@ -264,7 +487,30 @@ struct BvhBuilder {
             mx = jmax(mx, it.mx); my = jmax(my, it.my); mz = jmax(mz, it.mz);
             nx = jmin(nx, it.nx); ny = jmin(ny, it.ny); nz = jmin(nz, it.nz);
         }
-        auto root = build(items, 0, mx, my, mz, nx, ny, nz);
+        std::unique_ptr<BvhNode> root;
+        if (exhaustive) {
+            std::vector<BvhItem> work = items;
+            root = build(work, 0, mx, my, mz, nx, ny, nz);
+        } else {
+            const int n = (int)items.size();
+            std::vector<float> cen[3];
+            std::vector<int> ids(n), by[3];
+            for (int a = 0; a < 3; ++a) cen[a].resize(n);
+            for (int i = 0; i < n; ++i) {
+                ids[i] = i;
+                cen[0][i] = items[i].cx();
+                cen[1][i] = items[i].cy();
+                cen[2][i] = items[i].cz();
+            }
+            std::thread sorters[3];
+            for (int a = 0; a < 3; ++a) {
+                by[a] = ids;
+                sorters[a] = std::thread([&, a]() { std::sort(by[a].begin(), by[a].end(), CentroidLess{cen[a].data()}); });
+            }
+            for (auto& t : sorters) t.join();
+            spawned = 0;
+            root = build_sorted(items, cen, ids, by, 0, mx, my, mz, nx, ny, nz);
+        }
         root->mx = mx; root->my = my; root->mz = mz;
         root->nx = nx; root->ny = ny; root->nz = nz;
         return root;
@@ -277,7 +523,7 @@ int bvh_size(const BvhNode* n) {
 }
 
 // Node.addBounds: maximum, minimum, then the left and right subtrees (preorder).
-void bvh_add_bounds(const BvhNode* n, Distinct& points) {
+void bvh_add_bounds(const BvhNode* n, DistinctN<3>& points) {
     points.add(key3(n->mx, n->my, n->mz));
     points.add(key3(n->nx, n->ny, n->nz));
     if (!n->leaf) {
@@ -302,7 +548,7 @@ bool bvh_equal(const BvhNode* a, const BvhNode* b, const std::vector<Tri>& ta, c
 
 // doCompileBoundingVolumeHierarchy: preorder list, relative offsets, skip ("next") pointers.
 void bvh_flatten(const BvhNode* n, int next_after, std::vector<int32_t>& out, int base,
-                 const std::vector<int>& tri_offsets, const Distinct& points, const std::vector<int>& point_index) {
+                 const std::vector<int>& tri_offsets, const DistinctN<3>& points, const std::vector<int>& point_index) {
     const int here = (int)out.size() - base;
     (void)here;
     const int max_off = point_index[points.find(key3(n->mx, n->my, n->mz))] * 3;
@@ -417,6 +663,7 @@ struct dfpt_scene_builder {
     std::vector<Primitive> primitives;
     float camera[19];
     bool camera_set = false;
+    bool exhaustive_bvh = false;
 };
 
 struct dfpt_compiled {
@@ -547,6 +794,14 @@ int dfpt_builder_set_camera(dfpt_scene_builder* b, const float* eye, const float
     return DFPT_OK;
 }
 
+// Selects the builder's split search: 0 = sorted sweep (default), 1 = the reference's loop over
+// every item for every candidate. Both give the same tree; the second is kept to check that.
+int dfpt_builder_set_exhaustive(dfpt_scene_builder* b, int32_t on) {
+    if (!b) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "null builder");
+    b->exhaustive_bvh = on != 0;
+    return DFPT_OK;
+}
+
 int dfpt_builder_compile(dfpt_scene_builder* b, int32_t threads, dfpt_compiled** out) {
     if (!b || !out) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "bad compile arguments");
     if (!b->camera_set) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "camera not set");
@@ -562,6 +817,7 @@ int dfpt_builder_compile(dfpt_scene_builder* b, int32_t threads, dfpt_compiled**
     // several primitives are built once since the builder is deterministic.
     BvhBuilder builder;
     builder.threads = threads;
+    builder.exhaustive = b->exhaustive_bvh;
     std::unordered_map<int, std::shared_ptr<BvhNode>> bvh_of_shape;
     std::vector<int> mesh_shapes_in_order;
     for (int pi : mesh_prims) {
@@ -573,16 +829,19 @@ int dfpt_builder_compile(dfpt_scene_builder* b, int32_t threads, dfpt_compiled**
     // Unique triangle meshes (TriangleMesh.equals compares the triangle lists).
     std::vector<int> unique_mesh_shapes;
     {
-        Distinct dm;
+        auto same_mesh = [&](int a, int c) {
+            const auto& ta = b->shapes[a].tris;
+            const auto& tc = b->shapes[c].tris;
+            if (ta.size() != tc.size()) return false;
+            for (size_t i = 0; i < ta.size(); ++i)
+                if (!(tri_key(ta[i]) == tri_key(tc[i]))) return false;
+            return true;
+        };
         for (int si : mesh_shapes_in_order) {
-            Key k;
-            for (const Tri& t : b->shapes[si].tris) {
-                Key kt = tri_key(t);
-                k.w.insert(k.w.end(), kt.w.begin(), kt.w.end());
-            }
-            const size_t before = dm.order.size();
-            dm.add(k);
-            if (dm.order.size() != before) unique_mesh_shapes.push_back(si);
+            bool dup = false;
+            for (int u : unique_mesh_shapes)
+                if (u == si || same_mesh(u, si)) { dup = true; break; }
+            if (!dup) unique_mesh_shapes.push_back(si);
         }
     }
     // Unique BVH roots (distinct over Node.equals), aligned with the unique meshes.
@@ -665,7 +924,8 @@ int dfpt_builder_compile(dfpt_scene_builder* b, int32_t threads, dfpt_compiled**
     }
 
     // Points (BVH bounds first), texture coordinates, vectors.
-    Distinct p3, p2, v3;
+    DistinctN<3> p3, v3;
+    DistinctN<2> p2;
     for (int si : mesh_shapes_in_order) bvh_add_bounds(bvh_of_shape[si].get(), p3);
     auto add_tri_points = [&](const Tri& t) {
         for (int k = 0; k < 3; ++k) p3.add(key3(t.v[k].p[0], t.v[k].p[1], t.v[k].p[2]));
@@ -697,8 +957,8 @@ int dfpt_builder_compile(dfpt_scene_builder* b, int32_t threads, dfpt_compiled**
             }
         }
     }
-    auto unpack = [](const Distinct& d, std::vector<float>& out) {
-        for (const Key& k : d.order)
+    auto unpack = [](const auto& d, std::vector<float>& out) {
+        for (const auto& k : d.order)
             for (uint32_t w : k.w) {
                 float f;
                 std::memcpy(&f, &w, 4);
@@ -713,7 +973,8 @@ int dfpt_builder_compile(dfpt_scene_builder* b, int32_t threads, dfpt_compiled**
     for (size_t i = 0; i < identity_index.size(); ++i) identity_index[i] = (int)i;
 
     // Shapes: unique planes, spheres, terrains, triangles (primitive order).
-    Distinct dplane, dsphere, dterrain, dtri;
+    Distinct dplane, dsphere, dterrain;
+    DistinctN<33> dtri;
     std::vector<int> plane_off(b->shapes.size(), -1), sphere_off(b->shapes.size(), -1), terrain_off(b->shapes.size(), -1);
     std::vector<std::vector<int>> tri_off(b->shapes.size());
     for (const Primitive& p : b->primitives) {

@@ -126,6 +126,7 @@ SIGNATURES = {
     "dfpt_builder_add_primitive": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, f32p]),
     "dfpt_builder_set_camera": (C.c_int, [C.c_void_p, f32p, f32p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32]),
     "dfpt_builder_compile": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "dfpt_builder_set_exhaustive": (C.c_int, [C.c_void_p, C.c_int32]),
     "dfpt_compiled_destroy": (C.c_int, [C.c_void_p]),
     "dfpt_compiled_describe": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
     "dfpt_sky_set": (C.c_int, [C.POINTER(Sky), f32p, C.c_float]),

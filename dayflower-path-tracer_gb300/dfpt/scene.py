@@ -242,8 +242,11 @@ class SceneBuilder:
                                                float(resolution[0]), float(resolution[1]), float(aperture_radius),
                                                float(focal_distance), 2 if fisheye else 1))
 
-    def compile(self, name: str = "scene", threads: int = 0) -> CompiledScene:
+    def compile(self, name: str = "scene", threads: int = 0, exhaustive_bvh: bool = False) -> CompiledScene:
+        """SceneCompiler.compile. `exhaustive_bvh` runs the builder's split search as the reference's
+        loop over every item for every candidate (slow; the default sorted sweep gives the same tree)."""
         out = C.c_void_p()
+        check(self._lib.dfpt_builder_set_exhaustive(self._h, 1 if exhaustive_bvh else 0))
         check(self._lib.dfpt_builder_compile(self._h, int(threads), C.byref(out)))
         try:
             d = _lib.SceneDesc()

@@ -144,3 +144,27 @@ def test_sky_set_matches_formulas():
                                                                0.12064 * t - 2.57705, -0.06696 * t + 0.37027], rel=1e-15)
     assert list(s.sun_origin) == pytest.approx([float(x) * 10000.0 for x in dw], rel=1e-7)
     assert list(s.sun_direction) == pytest.approx([float(dw[0]), float(dw[2]), float(dw[1])], rel=1e-7)
+
+
+@pytest.mark.parametrize("kind", ["icosphere", "heightfield"])
+def test_sorted_sweep_matches_exhaustive_split_search(kind):
+    """The builder's sorted-list split search (prefix bounds over centroid order) picks the same
+    splits as the reference's loop over every item per candidate: identical arrays. The grid
+    heightfield has many equal centroids (ties at split positions)."""
+    from dfpt import scene as sc, synthetic
+
+    def compile_(exhaustive):
+        b = sc.SceneBuilder()
+        t = b.constant(0.5, 0.5, 0.5)
+        if kind == "icosphere":
+            pos, idx, _, nrm, uv = synthetic.displaced_icosphere(20, 0.1, 3)
+            b.primitive(b.mesh(pos, idx, nrm, uv), b.surface(3, t, t, t))
+        else:
+            pos, idx = synthetic.heightfield(64, 6.0, 1.0, 3)[:2]
+            b.primitive(b.mesh(pos, idx), b.surface(3, t, t, t))
+        b.camera((0, 0, 5), (0, 0, 0))
+        return b.compile(exhaustive_bvh=exhaustive)
+
+    fast, slow = compile_(False), compile_(True)
+    for k, v in fast.arrays().items():
+        assert np.array_equal(v, getattr(slow, k)), k
