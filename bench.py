@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-scenes leg")
+    ap.add_argument("--batch-scenes", type=int, default=64)
     return ap.parse_args()
 
 
@@ -189,6 +191,98 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(args, stream, torch, barrier, dist, world):
+    """Batched rendering: `--batch-scenes` seeded scenes (triangles log-uniform in [1k, 500k],
+    resolutions {256^2, 512^2, 1024^2}, spp {16, 64, 256}) rendered to their full sample counts
+    (a) by one BatchRenderer - one launch per stage per wave, a replayed CUDA graph, wave capacity
+    and traversal configuration picked by the autotuner - and (b) as sequential single-scene
+    renders (one RendererKernel per scene, spp passes each, one stream). Scenes are uploaded and
+    graphs built before either timed region; each region is bracketed by CUDA events."""
+    import numpy as np
+    from dfpt import synthetic
+    from dfpt.autotune import tune_batch
+    from dfpt.batch import BatchRenderer
+    from dfpt.kernel import RendererKernel
+
+    t0 = time.perf_counter()
+    work = synthetic.batch_workload(seed=5, count=args.batch_scenes)
+    build_s = time.perf_counter() - t0
+    samples = sum(x["width"] * x["height"] * x["spp"] for x in work)
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        fn()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    b = BatchRenderer()
+    b.set_stream(stream.cuda_stream)
+    for x in work:
+        b.add(x["scene"], x["width"], x["height"], x["spp"], x["sky"], x["params"])
+    tuning = tune_batch(b)
+    launches0 = b.launch_count()
+    barrier()
+    batch_s = timed(b.render)
+    barrier()
+    batch_launches = b.launch_count() - launches0
+
+    handles = []
+    for x in work:
+        k = RendererKernel(x["scene"], x["sky"], x["params"])
+        k.update(x["width"], x["height"])
+        k.set_stream(stream.cuda_stream)
+        k.set_tuning("trace_config", tuning["best"]["trace_config"])
+        k.execute(1)  # builds the pass graph
+        handles.append(k)
+    torch.cuda.synchronize()
+
+    def sequential():
+        for k, x in zip(handles, work):
+            k.clear()
+            k.execute(x["spp"])
+
+    barrier()
+    seq_s = timed(sequential)
+    barrier()
+    for k in handles:
+        k.dispose()
+    # The batch reproduces the single-scene films (same paths, same Kahan order per pixel): fresh
+    # handles (pass index from 0, as the batch's sample index) on a sample of the scenes.
+    worst = 0.0
+    for i in range(0, len(work), max(1, len(work) // 8)):
+        x = work[i]
+        k = RendererKernel(x["scene"], x["sky"], x["params"])
+        k.update(x["width"], x["height"])
+        k.execute(x["spp"])
+        fs, ns = k.film()
+        k.dispose()
+        fb, nb = b.film(i)
+        if not np.array_equal(nb, ns):
+            worst = float("inf")
+            break
+        worst = max(worst, float(np.max(np.abs(fb - fs) / (np.abs(fs) + 1e-3))))
+    b.dispose()
+    if dist is not None:
+        t = torch.tensor([batch_s, seq_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        batch_s, seq_s = (float(v) for v in t.tolist())
+    n = len(work)
+    return {
+        "metric": "scenes/s", "value": world * n / batch_s, "sequential_value": world * n / seq_s,
+        "speedup_vs_sequential": seq_s / batch_s, "samples": samples,
+        "m_samples_per_s": world * samples / batch_s / 1e6, "sequential_m_samples_per_s": world * samples / seq_s / 1e6,
+        "batch_s": batch_s, "sequential_s": seq_s, "gpu_launches": int(batch_launches),
+        "triangles_total": sum(x["triangles"] for x in work), "scenes": n, "scene_build_s": round(build_s, 1),
+        "tuning": tuning["best"], "film_max_rel_diff_vs_sequential": worst,
+        "workload": "batch_workload seed 5: tris log-uniform [1k,500k], res {256,512,1024}^2, spp {16,64,256}, depth 5",
+    }
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -235,15 +329,13 @@ def main():
     k.execute(args.warmup)
     k.synchronize()
 
-    # Timed region: per-step events on the handle's stream, L2 flushed between steps, per-kernel
-    # events inside each pass for the roofline.
-    k.set_profiling(True)
+    # Timed region: the pass graph replayed once per step, per-step events on the handle's stream,
+    # L2 flushed between steps.
     sampler = ClockSampler(local)
     launches0 = k.launch_count()
     barrier()
     sampler.start()
     step_ms = []
-    trace_ms, trace_n, kind_ms = 0.0, 0, {}
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
@@ -255,13 +347,6 @@ def main():
             e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
-        prof = k.read_profile()
-        trace_ms += prof["trace"][0]
-        trace_n += prof["trace"][1]
-        for kk, (ms, n) in prof.items():
-            a = kind_ms.setdefault(kk, [0.0, 0])
-            a[0] += ms
-            a[1] += n
     barrier()
     clocks = sampler.stop()
     launches = k.launch_count() - launches0
@@ -271,6 +356,29 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_s = float(t.item())
     value = world * n_pix * args.steps / total_s / 1e6
+
+    # The same steps with an event between kernels (direct launches): per-kernel times, and the
+    # average duration of the closest-hit traversal launch for the roofline.
+    k.set_profiling(True)
+    trace_ms, trace_n, kind_ms, prof_ms = 0.0, 0, {}, []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        k.execute(1)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        prof_ms.append(e0.elapsed_time(e1))
+        prof = k.read_profile()
+        trace_ms += prof["trace"][0]
+        trace_n += prof["trace"][1]
+        for kk, (ms, n) in prof.items():
+            a = kind_ms.setdefault(kk, [0.0, 0])
+            a[0] += ms
+            a[1] += n
     k.set_profiling(False)
 
     # Traversal counters over one extra pass (not timed): segments per pass.
@@ -299,6 +407,10 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = world * n_pix * args.steps / e2e_s / 1e6
+
+    batched = None
+    if not args.no_batch:
+        batched = batch_leg(args, stream, torch, barrier, dist, world)
 
     if rank != 0:
         if dist is not None:
@@ -347,11 +459,14 @@ def main():
                      "kernel": "k_trace<closest>", "avg_launch_ms": avg_trace_ms,
                      "bytes_per_segment": bytes_per_seg, "segments_per_launch": closest_segments / launches_per_pass},
         "kernels_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in kind_ms.items() if v[1]},
+        "ms_per_step_profiled": sum(prof_ms) / len(prof_ms),
         "rays_per_s": (cnt[0] + cnt[1]) / (total_s / args.steps) / 1e9 * 1e3,
         "clocks": clocks,
     }
     if cpu:
         line["cpu_baseline"] = {k2: cpu[k2] for k2 in ("value", "unit", "cores", "kind", "sample")}
+    if batched:
+        line["batched"] = batched
     line["rays_per_s"] = (cnt[0] + cnt[1]) * world / (total_s / args.steps)
     print(json.dumps(line), flush=True)
     k.dispose()

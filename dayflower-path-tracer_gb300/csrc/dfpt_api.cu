@@ -16,6 +16,7 @@
 #include "dfpt_internal.h"
 #include "dfpt_launch.h"
 #include "dfpt_noise_tables.h"
+#include "dfpt_store.h"
 
 namespace {
 thread_local std::string g_last_error;
@@ -31,41 +32,11 @@ int dfpt_fail(int code, const char* fmt, ...) {
     return code;
 }
 
-#define CUDA_TRY(expr)                                                                          \
-    do {                                                                                        \
-        cudaError_t e_ = (expr);                                                                \
-        if (e_ != cudaSuccess) {                                                                \
-            (void)cudaGetLastError();                                                           \
-            return dfpt_fail(e_ == cudaErrorMemoryAllocation ? DFPT_ERR_OUT_OF_MEMORY : DFPT_ERR_CUDA, \
-                             "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
-        }                                                                                       \
-    } while (0)
-
 namespace {
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    cudaError_t alloc(size_t count) {
-        n = count;
-        return cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-};
 
 // ---------------------------------------------------------------------------------------------
 // Validation of the compiled scene: every offset the kernels will follow is checked here so no
 // device access can leave its array.
-
-struct HostScene {
-    std::vector<float> point2fs, point3fs, vector3fs, spheres, terrains, textures, surfaces, o2w, w2o, camera;
-    std::vector<int> planes, triangles, bvh, primitives;
-};
 
 bool in_range(int64_t off, int64_t len, int64_t count) { return off >= 0 && len >= 0 && off + len <= count; }
 
@@ -129,11 +100,6 @@ int check_surface(const HostScene& s, int so) {
     }
     return DFPT_OK;
 }
-
-struct Derived {
-    std::vector<int4> prim_info;
-    std::vector<float4> nodes, tris, sphere4, plane_a, plane_n;
-};
 
 float int_bits(int i) {
     float f;
@@ -284,19 +250,13 @@ float powf_j(float a, float b) { return (float)std::pow((double)a, (double)b); }
 }  // namespace
 
 struct dfpt_handle {
-    HostScene host;
+    SceneStore sc;  // the compiled scene, host copy + device arrays
     int width = 0, height = 0, n_pixels = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int sms = 0;
     KernelSet fast{}, strict{};
     bool use_strict = false;
-    // Scene on the device.
-    DevBuf<float> point2fs, point3fs, vector3fs, spheres, terrains, textures, surfaces, o2w, w2o, camera;
-    DevBuf<int> planes, triangles, primitives;
-    DevBuf<int4> prim_info;
-    DevBuf<float4> nodes, tris, sphere4, plane_a, plane_n;
-    DevScene scene{};
     // Parameters.
     dfpt_params params{};
     dfpt_sky sky{};
@@ -338,13 +298,13 @@ void release(dfpt_handle* h) {
     h->events.clear();
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     h->graph_exec = nullptr;
-    DevBuf<float>* fb[] = {&h->point2fs, &h->point3fs, &h->vector3fs, &h->spheres, &h->terrains, &h->textures, &h->surfaces, &h->o2w, &h->w2o, &h->camera, &h->hit_dist, &h->hit_normal, &h->scratch_rgb};
+    h->sc.release();
+    DevBuf<float>* fb[] = {&h->hit_dist, &h->hit_normal, &h->scratch_rgb};
     for (auto* b : fb) b->release();
-    DevBuf<int>* ib[] = {&h->planes, &h->triangles, &h->primitives, &h->pixel_flags, &h->counts, &h->pass_index, &h->film_n, &h->primitive_offsets, &h->hit_prim, &h->hit_type, &h->hit_off};
+    DevBuf<int>* ib[] = {&h->pixel_flags, &h->counts, &h->pass_index, &h->film_n, &h->primitive_offsets, &h->hit_prim, &h->hit_type, &h->hit_off};
     for (auto* b : ib) b->release();
-    DevBuf<float4>* f4[] = {&h->nodes, &h->tris, &h->sphere4, &h->plane_a, &h->plane_n, &h->q_o0, &h->q_o1, &h->q_d0, &h->q_d1, &h->s_o, &h->s_d, &h->s_c, &h->throughput, &h->radiance, &h->primary_o, &h->primary_d, &h->film_sum, &h->film_comp};
+    DevBuf<float4>* f4[] = {&h->q_o0, &h->q_o1, &h->q_d0, &h->q_d1, &h->s_o, &h->s_d, &h->s_c, &h->throughput, &h->radiance, &h->primary_o, &h->primary_d, &h->film_sum, &h->film_comp};
     for (auto* b : f4) b->release();
-    h->prim_info.release();
     h->rng.release();
     h->bgra.release();
     h->stats.release();
@@ -354,20 +314,9 @@ void release(dfpt_handle* h) {
     h->stream = nullptr;
 }
 
-template <typename T>
-cudaError_t upload(DevBuf<T>& b, const std::vector<T>& v, cudaStream_t s) {
-    if (!b.p || b.n != v.size()) {
-        b.release();
-        cudaError_t e = b.alloc(v.size());
-        if (e != cudaSuccess) return e;
-    }
-    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
-}
+}  // namespace
 
-void fill_dev_params(dfpt_handle* h) {
-    DevParams& d = h->dev_params_host;
-    const dfpt_params& p = h->params;
-    const dfpt_sky& k = h->sky;
+void dev_params_fill(DevParams& d, const dfpt_params& p, const dfpt_sky& k, const float* cam, int width, int height) {
     std::memset(&d, 0, sizeof(d));
     d.renderer_type = p.renderer_type;
     d.tone_mapper_type = p.tone_mapper_type;
@@ -387,11 +336,8 @@ void fill_dev_params(dfpt_handle* h) {
     d.rng_kind = p.rng_kind;
     d.seed_lo = (uint32_t)p.seed;
     d.seed_hi = (uint32_t)(p.seed >> 32);
-    d.width = h->width;
-    d.height = h->height;
-    d.record_hits = h->record_hits ? 1 : 0;
-    d.counting = h->counting ? 1 : 0;
-    d.clear_pass = h->clear_pass;
+    d.width = width;
+    d.height = height;
     for (int i = 0; i < 3; ++i) {
         d.sky_u[i] = k.orthonormal_basis_u[i];
         d.sky_v[i] = k.orthonormal_basis_v[i];
@@ -419,7 +365,6 @@ void fill_dev_params(dfpt_handle* h) {
     d.cos_theta0 = (float)c0;
     const float pi_f = 3.14159274101257324219f;
     const float pi180 = pi_f / 180.0f;
-    const float* cam = h->host.camera.data();
     d.fov_tan_x = (float)std::tan((double)(cam[4] * 0.5f * pi180));
     d.fov_tan_y = (float)std::tan((double)(-cam[5] * 0.5f * pi180));
     d.wire_cos = (float)std::cos((double)(pi_f * 0.5f / 4096.0f));
@@ -431,6 +376,16 @@ void fill_dev_params(dfpt_handle* h) {
     d.cs_slope = 1.0f / (g / pe - g * bp + bp);
     d.cs_slope_match = g * d.cs_slope / pe;
     d.cs_segment = d.cs_slope_match * powf_j(bp, 1.0f / g) - d.cs_slope * bp;
+}
+
+namespace {
+
+void fill_dev_params(dfpt_handle* h) {
+    DevParams& d = h->dev_params_host;
+    dev_params_fill(d, h->params, h->sky, h->sc.host.camera.data(), h->width, h->height);
+    d.record_hits = h->record_hits ? 1 : 0;
+    d.counting = h->counting ? 1 : 0;
+    d.clear_pass = h->clear_pass;
 }
 
 int push_params(dfpt_handle* h) {
@@ -542,22 +497,27 @@ int build_graph(dfpt_handle* h) {
 
 }  // namespace
 
-extern "C" {
+// ---------------------------------------------------------------------------------------------
+// SceneStore: validation and upload of one compiled scene.
 
-const char* dfpt_last_error(void) { return g_last_error.c_str(); }
+void SceneStore::release() {
+    DevBuf<float>* fb[] = {&point2fs, &point3fs, &vector3fs, &spheres, &terrains, &textures, &surfaces, &o2w, &w2o, &camera};
+    for (auto* b : fb) b->release();
+    DevBuf<int>* ib[] = {&planes, &triangles, &primitives};
+    for (auto* b : ib) b->release();
+    DevBuf<float4>* f4[] = {&nodes, &tris, &sphere4, &plane_a, &plane_n};
+    for (auto* b : f4) b->release();
+    prim_info.release();
+}
 
-int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, int32_t height, dfpt_handle** out) {
-    if (!sd || !sky || !out) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
-    *out = nullptr;
-    if (width <= 0 || height <= 0 || (int64_t)width * (int64_t)height > (1ll << 28))
-        return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "resolution %d x %d is not supported", width, height);
+int scene_load(const dfpt_scene_desc* sd, SceneStore& st) {
+    if (!sd) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL scene");
     if (sd->camera_count < 19 || !sd->camera) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "camera needs 19 floats");
     if (sd->primitives_count % 3 != 0) return dfpt_fail(DFPT_ERR_INVALID_SCENE, "primitives count %lld is not a multiple of 3", (long long)sd->primitives_count);
     const int64_t np = sd->primitives_count / 3;
     if (sd->primitives_object_to_world_count < np * 16 || sd->primitives_world_to_object_count < np * 16)
         return dfpt_fail(DFPT_ERR_INVALID_SCENE, "primitive matrices need 16 floats per primitive");
-    auto h = new dfpt_handle();
-    HostScene& s = h->host;
+    HostScene& s = st.host;
     copy_array(s.point2fs, sd->point2fs, sd->point2fs_count);
     copy_array(s.point3fs, sd->point3fs, sd->point3fs_count);
     copy_array(s.vector3fs, sd->vector3fs, sd->vector3fs_count);
@@ -573,10 +533,82 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     s.w2o.assign(sd->primitives_world_to_object, sd->primitives_world_to_object + np * 16);
     if (s.o2w.empty()) { s.o2w.assign(16, 0.0f); s.w2o.assign(16, 0.0f); }
     s.camera.assign(sd->camera, sd->camera + 19);
-    Derived d;
+    Derived& d = st.derived;
     int r = build_derived(s, d);
+    if (r) return r;
+    if (d.nodes.size() / 2 > (size_t)INT32_MAX / 4 || d.tris.size() / 3 > (size_t)INT32_MAX / 4) return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "scene too large");
+    st.scene.primitive_count = (int)np;
+    st.scene.textures_count = (int)s.textures.size();
+    return DFPT_OK;
+}
+
+int scene_upload(SceneStore& st, cudaStream_t s) {
+    const HostScene& h = st.host;
+    Derived& d = st.derived;
+    CUDA_TRY(upload(st.point2fs, h.point2fs, s));
+    CUDA_TRY(upload(st.point3fs, h.point3fs, s));
+    CUDA_TRY(upload(st.vector3fs, h.vector3fs, s));
+    CUDA_TRY(upload(st.planes, h.planes, s));
+    CUDA_TRY(upload(st.spheres, h.spheres, s));
+    CUDA_TRY(upload(st.terrains, h.terrains, s));
+    CUDA_TRY(upload(st.triangles, h.triangles, s));
+    CUDA_TRY(upload(st.textures, h.textures, s));
+    CUDA_TRY(upload(st.surfaces, h.surfaces, s));
+    CUDA_TRY(upload(st.primitives, h.primitives, s));
+    CUDA_TRY(upload(st.o2w, h.o2w, s));
+    CUDA_TRY(upload(st.w2o, h.w2o, s));
+    CUDA_TRY(upload(st.camera, h.camera, s));
+    CUDA_TRY(upload(st.prim_info, d.prim_info, s));
+    CUDA_TRY(upload(st.nodes, d.nodes, s));
+    CUDA_TRY(upload(st.tris, d.tris, s));
+    CUDA_TRY(upload(st.sphere4, d.sphere4, s));
+    CUDA_TRY(upload(st.plane_a, d.plane_a, s));
+    CUDA_TRY(upload(st.plane_n, d.plane_n, s));
+    CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors below are freed
+    DevScene& S = st.scene;
+    S.point2fs = st.point2fs.p; S.point3fs = st.point3fs.p; S.vector3fs = st.vector3fs.p;
+    S.planes = st.planes.p; S.spheres = st.spheres.p; S.terrains = st.terrains.p; S.triangles = st.triangles.p;
+    S.textures = st.textures.p; S.surfaces = st.surfaces.p; S.primitives = st.primitives.p;
+    S.o2w = st.o2w.p; S.w2o = st.w2o.p; S.camera = st.camera.p;
+    S.prim_info = st.prim_info.p; S.nodes = st.nodes.p; S.tris = st.tris.p; S.sphere4 = st.sphere4.p;
+    S.plane_a = st.plane_a.p; S.plane_n = st.plane_n.p;
+    st.derived = Derived();
+    return DFPT_OK;
+}
+
+int noise_tables_init(const KernelSet& ks, cudaStream_t st) {
+    std::vector<int> perm(DFPT_PERMUTATION, DFPT_PERMUTATION + 256);
+    std::vector<float> grad(DFPT_GRADIENT3, DFPT_GRADIENT3 + 36);
+    DevBuf<int> dperm;
+    DevBuf<float> dgrad;
+    cudaError_t e = upload(dperm, perm, st);
+    if (e == cudaSuccess) e = upload(dgrad, grad, st);
+    if (e == cudaSuccess) {
+        ks.init_tables(st, dperm.p, dgrad.p);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dperm.release();
+    dgrad.release();
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return dfpt_fail(DFPT_ERR_CUDA, "noise tables: %s", cudaGetErrorString(e));
+    }
+    return DFPT_OK;
+}
+
+extern "C" {
+
+const char* dfpt_last_error(void) { return g_last_error.c_str(); }
+
+int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, int32_t height, dfpt_handle** out) {
+    if (!sd || !sky || !out) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (width <= 0 || height <= 0 || (int64_t)width * (int64_t)height > (1ll << 28))
+        return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "resolution %d x %d is not supported", width, height);
+    auto h = new dfpt_handle();
+    int r = scene_load(sd, h->sc);
     if (r) { delete h; return r; }
-    if (d.nodes.size() / 2 > (size_t)INT32_MAX / 4 || d.tris.size() / 3 > (size_t)INT32_MAX / 4) { delete h; return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "scene too large"); }
 
     h->width = width;
     h->height = height;
@@ -591,38 +623,11 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { (void)cudaGetLastError(); delete h; return dfpt_fail(DFPT_ERR_CUDA, "CUDA device unavailable: %s", cudaGetErrorString(ce)); }
     h->own_stream = true;
+    cudaStream_t st = h->stream;
+    r = scene_upload(h->sc, st);
+    if (r) { release(h); delete h; return r; }
 
 #define TRY_R(expr) do { cudaError_t e_ = (expr); if (e_ != cudaSuccess) { (void)cudaGetLastError(); int code = e_ == cudaErrorMemoryAllocation ? DFPT_ERR_OUT_OF_MEMORY : DFPT_ERR_CUDA; dfpt_fail(code, "%s: %s", #expr, cudaGetErrorString(e_)); release(h); delete h; return code; } } while (0)
-    cudaStream_t st = h->stream;
-    TRY_R(upload(h->point2fs, s.point2fs, st));
-    TRY_R(upload(h->point3fs, s.point3fs, st));
-    TRY_R(upload(h->vector3fs, s.vector3fs, st));
-    TRY_R(upload(h->planes, s.planes, st));
-    TRY_R(upload(h->spheres, s.spheres, st));
-    TRY_R(upload(h->terrains, s.terrains, st));
-    TRY_R(upload(h->triangles, s.triangles, st));
-    TRY_R(upload(h->textures, s.textures, st));
-    TRY_R(upload(h->surfaces, s.surfaces, st));
-    TRY_R(upload(h->primitives, s.primitives, st));
-    TRY_R(upload(h->o2w, s.o2w, st));
-    TRY_R(upload(h->w2o, s.w2o, st));
-    TRY_R(upload(h->camera, s.camera, st));
-    TRY_R(upload(h->prim_info, d.prim_info, st));
-    TRY_R(upload(h->nodes, d.nodes, st));
-    TRY_R(upload(h->tris, d.tris, st));
-    TRY_R(upload(h->sphere4, d.sphere4, st));
-    TRY_R(upload(h->plane_a, d.plane_a, st));
-    TRY_R(upload(h->plane_n, d.plane_n, st));
-    DevScene& S = h->scene;
-    S.point2fs = h->point2fs.p; S.point3fs = h->point3fs.p; S.vector3fs = h->vector3fs.p;
-    S.planes = h->planes.p; S.spheres = h->spheres.p; S.terrains = h->terrains.p; S.triangles = h->triangles.p;
-    S.textures = h->textures.p; S.surfaces = h->surfaces.p; S.primitives = h->primitives.p;
-    S.o2w = h->o2w.p; S.w2o = h->w2o.p; S.camera = h->camera.p;
-    S.primitive_count = (int)np;
-    S.textures_count = (int)s.textures.size();
-    S.prim_info = h->prim_info.p; S.nodes = h->nodes.p; S.tris = h->tris.p; S.sphere4 = h->sphere4.p;
-    S.plane_a = h->plane_a.p; S.plane_n = h->plane_n.p;
-
     const size_t n = (size_t)h->n_pixels;
     TRY_R(h->q_o0.alloc(n)); TRY_R(h->q_o1.alloc(n)); TRY_R(h->q_d0.alloc(n)); TRY_R(h->q_d1.alloc(n));
     TRY_R(h->q_hit.alloc(n));
@@ -654,21 +659,13 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     B.hit_distance = h->hit_dist.p; B.hit_normal = h->hit_normal.p;
 
     // Noise tables (both kernel sets own a copy).
-    std::vector<int> perm(DFPT_PERMUTATION, DFPT_PERMUTATION + 256);
-    std::vector<float> grad(DFPT_GRADIENT3, DFPT_GRADIENT3 + 36);
-    DevBuf<int> dperm;
-    DevBuf<float> dgrad;
-    TRY_R(upload(dperm, perm, st));
-    TRY_R(upload(dgrad, grad, st));
-    h->fast.init_tables(st, dperm.p, dgrad.p);
-    h->strict.init_tables(st, dperm.p, dgrad.p);
-    TRY_R(cudaGetLastError());
+    r = noise_tables_init(h->fast, st);
+    if (!r) r = noise_tables_init(h->strict, st);
+    if (r) { release(h); delete h; return r; }
     TRY_R(cudaStreamSynchronize(st));
-    dperm.release();
-    dgrad.release();
 #undef TRY_R
 
-    h->ctx.scene = &h->scene;
+    h->ctx.scene = &h->sc.scene;
     h->ctx.params = h->dev_params.p;
     h->ctx.pass = &h->pass;
     h->ctx.stream = h->stream;
@@ -705,33 +702,33 @@ int dfpt_set_stream(dfpt_handle* h, void* stream) {
 
 int dfpt_set_camera(dfpt_handle* h, const float* camera19) {
     if (!h || !camera19) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
-    h->host.camera.assign(camera19, camera19 + 19);
-    CUDA_TRY(cudaMemcpyAsync(h->camera.p, h->host.camera.data(), 19 * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    h->sc.host.camera.assign(camera19, camera19 + 19);
+    CUDA_TRY(cudaMemcpyAsync(h->sc.camera.p, h->sc.host.camera.data(), 19 * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     return push_params(h);  // the field-of-view tangents are derived from the camera
 }
 
 int dfpt_set_transforms(dfpt_handle* h, const float* o2w, const float* w2o, int32_t count) {
     if (!h || !o2w || !w2o) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (count != h->scene.primitive_count) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive count %d != %d", count, h->scene.primitive_count);
-    h->host.o2w.assign(o2w, o2w + (size_t)count * 16);
-    h->host.w2o.assign(w2o, w2o + (size_t)count * 16);
+    if (count != h->sc.scene.primitive_count) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive count %d != %d", count, h->sc.scene.primitive_count);
+    h->sc.host.o2w.assign(o2w, o2w + (size_t)count * 16);
+    h->sc.host.w2o.assign(w2o, w2o + (size_t)count * 16);
     if (count == 0) return DFPT_OK;
-    CUDA_TRY(cudaMemcpyAsync(h->o2w.p, h->host.o2w.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(cudaMemcpyAsync(h->w2o.p, h->host.w2o.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->sc.o2w.p, h->sc.host.o2w.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->sc.w2o.p, h->sc.host.w2o.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return DFPT_OK;
 }
 
 int dfpt_set_surfaces(dfpt_handle* h, const float* surfaces, int64_t count) {
     if (!h || !surfaces) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (count != (int64_t)h->host.surfaces.size()) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "surfaces count %lld != %zu", (long long)count, h->host.surfaces.size());
-    std::vector<float> old = h->host.surfaces;
-    h->host.surfaces.assign(surfaces, surfaces + count);
-    for (int i = 0; i < h->scene.primitive_count; ++i) {
-        int r = check_surface(h->host, h->host.primitives[3 * i + 2]);
-        if (r) { h->host.surfaces.swap(old); return r; }
+    if (count != (int64_t)h->sc.host.surfaces.size()) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "surfaces count %lld != %zu", (long long)count, h->sc.host.surfaces.size());
+    std::vector<float> old = h->sc.host.surfaces;
+    h->sc.host.surfaces.assign(surfaces, surfaces + count);
+    for (int i = 0; i < h->sc.scene.primitive_count; ++i) {
+        int r = check_surface(h->sc.host, h->sc.host.primitives[3 * i + 2]);
+        if (r) { h->sc.host.surfaces.swap(old); return r; }
     }
-    CUDA_TRY(cudaMemcpyAsync(h->surfaces.p, h->host.surfaces.data(), (size_t)count * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->sc.surfaces.p, h->sc.host.surfaces.data(), (size_t)count * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return DFPT_OK;
 }

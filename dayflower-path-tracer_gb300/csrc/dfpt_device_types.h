@@ -105,6 +105,24 @@ struct DevPass {
     float* hit_normal;
 };
 
+// Many scenes rendered by one set of launches. Every scene's samples form one global sequence
+// (scene-major, then sample, then pixel); a wave takes `capacity` consecutive samples of it, one
+// path slot each. Queue entries carry their scene in the direction's w.
+struct DevBatch {
+    const DevScene* scenes;           // [n_scenes]
+    const DevParams* params;          // [n_scenes]
+    const long long* sample_begin;    // [n_scenes + 1] first global sample of each scene
+    const long long* film_begin;      // [n_scenes + 1] first film pixel of each scene
+    int n_scenes;
+    int capacity;                     // path slots per wave
+    long long total;                  // samples of all scenes
+    long long* wave_base;             // device: [0] global sample of slot 0 of the current wave,
+                                      //         [1] end of the sample range being rendered
+    int4* slot_key;                   // per slot {scene, pixel, sample, 0}
+    long long* wave_tab;              // per scene in the wave {scene, local begin, local end, film-task prefix}
+    int* wave_entries;                // entries in wave_tab
+};
+
 #define DFPT_COUNTS_SHADOW 32
 #define DFPT_COUNTS_FETCH 64  // [64..95]: work-fetch counters of the traversal launches
 #define DFPT_MAX_DEPTH 30

@@ -474,27 +474,75 @@ __device__ __forceinline__ void warp_add_stats(const DevParams& P, unsigned long
     for (int i##_base = blockIdx.x * blockDim.x; i##_base < (n); i##_base += gridDim.x * blockDim.x) \
         for (int i = i##_base + (int)threadIdx.x, i##_once = 1; i##_once; i##_once = 0)
 
-// ---------------------------------------------------------------------------------------------
-// Path tracer wavefront (doRenderWithPathTracer, GRK:3151-3705).
+// Scene and parameters of a work item: the kernel's own (one scene) or the item's scene of a batch.
+template <bool BATCH>
+__device__ __forceinline__ const DevScene& scene_of(const DevScene& S0, const DevBatch& Q, int sid) {
+    if constexpr (BATCH) return Q.scenes[sid];
+    else { (void)Q; (void)sid; return S0; }
+}
+template <bool BATCH>
+__device__ __forceinline__ const DevParams& params_of(const DevParams* P0, const DevBatch& Q, int sid) {
+    if constexpr (BATCH) return Q.params[sid];
+    else { (void)Q; (void)sid; return *P0; }
+}
+// The scene holding global sample g: the last scene whose first sample is <= g.
+__device__ __forceinline__ int batch_scene_of(const DevBatch& Q, long long g) {
+    int lo = 0, hi = Q.n_scenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (Q.sample_begin[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
-__global__ void __launch_bounds__(256) k_camera(DevScene S, const DevParams* __restrict__ Pp, DevPass B) {
-    const DevParams& P = *Pp;
-    const int n = B.n_pixels;
-    const uint32_t pass = (uint32_t)*B.pass_index;
-    const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
-                    (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
+// ---------------------------------------------------------------------------------------------
+// Path tracer wavefront (doRenderWithPathTracer, GRK:3151-3705). Every stage is written once for
+// both forms: one scene (BATCH = false; a path is a pixel, the pass index keys the RNG) and a batch
+// of scenes (BATCH = true; a path is a wave slot, {scene, pixel, sample} come from the slot key).
+
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q) {
+    const int n = BATCH ? Q.capacity : B.n_pixels;
+    const uint32_t pass = BATCH ? 0u : (uint32_t)*B.pass_index;
+    long long base = 0, end = 0;
+    if constexpr (BATCH) {
+        base = Q.wave_base[0];
+        end = Q.wave_base[1];
+    }
     GRID_STRIDE_UNIFORM(i, n) {
-        const bool valid = i < n;
+        bool valid = i < n;
+        int sid = 0, pixel = i;
+        uint32_t sample = pass;
+        if constexpr (BATCH) {
+            if (valid) {
+                const long long g = base + i;
+                if (g >= end) {
+                    valid = false;
+                } else {
+                    sid = batch_scene_of(Q, g);
+                    const long long local = g - Q.sample_begin[sid];
+                    const long long np = (long long)Q.params[sid].width * Q.params[sid].height;
+                    sample = (uint32_t)(local / np);
+                    pixel = (int)(local - (long long)sample * np);
+                    Q.slot_key[i] = make_int4(sid, pixel, (int)sample, 0);
+                }
+            }
+        }
+        const DevScene& S = scene_of<BATCH>(S0, Q, sid);
+        const DevParams& P = params_of<BATCH>(Pp, Q, sid);
         float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 0, 0);
         bool live = false;
         if (valid) {
-            Rng rng = make_rng(P, (uint32_t)i, pass, P.rng_kind == DFPT_RNG_LCG ? B.rng[i] : 0ull);
-            live = primary_ray(S, P, i, pt, rng, o, d);
+            const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
+                            (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
+            Rng rng = make_rng(P, (uint32_t)pixel, sample, (!BATCH && P.rng_kind == DFPT_RNG_LCG) ? B.rng[i] : 0ull);
+            live = primary_ray(S, P, pixel, pt, rng, o, d);
             B.rng[i] = rng.state;
             B.pixel_flags[i] = live ? 0 : 1;
             B.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
             B.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (P.wireframes == 1) {
+            if (!BATCH && P.wireframes == 1) {
                 B.primary_o[i] = o;
                 B.primary_d[i] = d;
             }
@@ -502,6 +550,7 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S, const DevParams* __r
         const int slot = warp_push(B.counts + 0, live);
         if (slot >= 0) {
             o.w = __int_as_float(i);
+            d.w = BATCH ? __int_as_float(sid) : 0.0f;
             B.q_o[0][slot] = o;
             B.q_d[0][slot] = d;
         }
@@ -510,9 +559,9 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S, const DevParams* __r
 
 // Traversal kernels are instantiated per tuning configuration (walk variant, block size, resident
 // blocks per SM); see TRACE_CONFIGS.
-template <bool ANY, int V, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce, int which_queue) {
-    const DevParams& P = *Pp;
+template <bool BATCH, bool ANY, int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce, int which_queue) {
+    const DevParams& P = *Pp;  // run-wide flags (statistics counting)
     const int n = B.counts[bounce];
     const float4* __restrict__ qo = B.q_o[which_queue];
     const float4* __restrict__ qd = B.q_d[which_queue];
@@ -524,6 +573,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S, const DevPara
             o = qo[i];
             d = qd[i];
         }
+        const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
         const Hit h = trace_v<ANY, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
         if (valid) B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
         warp_add_stats(P, B.stats, ANY ? 1 : 0, valid ? 1u : 0u, st.nodes, st.tris);
@@ -532,12 +582,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S, const DevPara
 
 // One bounce of shading: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
 // roulette, material sampling and the next ray (GRK:3185-3686).
-__global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
-    const DevParams& P = *Pp;
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     const int n = B.counts[bounce];
     const int qi = bounce & 1;
-    const uint32_t pass = (uint32_t)*B.pass_index;
-    const int depth_max = P.depth_max;
+    const uint32_t pass = BATCH ? 0u : (uint32_t)*B.pass_index;
     GRID_STRIDE_UNIFORM(i, n) {
         bool emit_next = false, emit_shadow = false;
         float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
@@ -546,6 +595,16 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __re
         if (i < n) {
             const float4 o4 = B.q_o[qi][i], d4 = B.q_d[qi][i];
             path = __float_as_int(o4.w);
+            const int sid = BATCH ? __float_as_int(d4.w) : 0;
+            const float sid_bits = BATCH ? d4.w : 0.0f;
+            const DevScene& S = scene_of<BATCH>(S0, Q, sid);
+            const DevParams& P = params_of<BATCH>(Pp, Q, sid);
+            uint32_t rng_pixel = (uint32_t)path, rng_pass = pass;
+            if constexpr (BATCH) {
+                const int4 key = Q.slot_key[path];
+                rng_pixel = (uint32_t)key.y;
+                rng_pass = (uint32_t)key.z;
+            }
             const int4 hr = B.q_hit[i];
             Hit h;
             h.t = __int_as_float(hr.x);
@@ -554,21 +613,21 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __re
             h.shape_offset = hr.w;
             float4 T = B.throughput[path];
             float4 L = B.radiance[path];
-            if (bounce == 0) B.primitive_offsets[path] = h.prim >= 0 ? h.prim * 3 : -1;
+            if (!BATCH && bounce == 0) B.primitive_offsets[path] = h.prim >= 0 ? h.prim * 3 : -1;
             if (h.t == INF || h.prim == -1) {
                 const float3 sky = sky_color(P, d4.x, d4.y, d4.z);
                 L.x += T.x * sky.x * INV_PI;
                 L.y += T.y * sky.y * INV_PI;
                 L.z += T.z * sky.z * INV_PI;
                 B.radiance[path] = L;
-                if (bounce == 0 && P.record_hits) {
+                if (!BATCH && bounce == 0 && P.record_hits) {
                     B.hit_prim_offset[path] = -1; B.hit_shape_type[path] = -1; B.hit_shape_offset[path] = -1;
                     B.hit_distance[path] = INF;
                 }
             } else {
-                Rng rng = make_rng(P, (uint32_t)path, pass, B.rng[path]);
+                Rng rng = make_rng(P, rng_pixel, rng_pass, B.rng[path]);
                 const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
-                if (bounce == 0 && P.record_hits) {
+                if (!BATCH && bounce == 0 && P.record_hits) {
                     B.hit_prim_offset[path] = h.prim * 3; B.hit_shape_type[path] = h.shape_type; B.hit_shape_offset[path] = h.shape_offset;
                     B.hit_distance[path] = h.t;
                     B.hit_normal[3 * path] = s.nx; B.hit_normal[3 * path + 1] = s.ny; B.hit_normal[3 * path + 2] = s.nz;
@@ -590,7 +649,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __re
                     if (sun_sample(P, s.px, s.py, s.pz, wx, wy, wz, u, v, lx, ly, lz, dot1)) {
                         emit_shadow = true;
                         so = make_float4(s.px, s.py, s.pz, __int_as_float(path));
-                        sd = make_float4(lx, ly, lz, 0.0f);
+                        sd = make_float4(lx, ly, lz, sid_bits);
                         sc = make_float4(T.x * (ar * 1.0f * dot1 * INV_PI), T.y * (ag * 1.0f * dot1 * INV_PI), T.z * (ab * 1.0f * dot1 * INV_PI), 0.0f);
                     }
                 }
@@ -704,8 +763,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __re
                     }
                     emit_next = true;
                     no = make_float4(ox, oy, oz, __int_as_float(path));
-                    nd = make_float4(dx, dy, dz, 0.0f);
-                    (void)depth_max;
+                    nd = make_float4(dx, dy, dz, sid_bits);
                 }
                 B.throughput[path] = T;
                 B.radiance[path] = L;
@@ -729,8 +787,8 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, const DevParams* __re
 // Sun visibility: any hit (GRK:2324-2340); unoccluded samples add their contribution. The shadow
 // rays of every bounce of the pass wait in one queue and are traced in a single launch after the
 // last bounce (their contributions only add to the path radiance).
-template <int V, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+template <bool BATCH, int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     const DevParams& P = *Pp;
     const int n = B.counts[DFPT_COUNTS_SHADOW];
     (void)bounce;
@@ -742,6 +800,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S, const DevPar
             o = B.s_o[i];
             d = B.s_d[i];
         }
+        const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
         const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
         if (valid && h.t >= INF - 0.0001f) {
             // A path has up to one shadow ray per bounce in this queue, so several threads may add
@@ -758,9 +817,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S, const DevPar
 }
 
 // After the last bounce: any-hit test of the continuation ray, sky if it escapes (GRK:3689-3701).
-template <int V, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
-    const DevParams& P = *Pp;
+template <bool BATCH, int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
+    const DevParams& P0 = *Pp;  // run-wide flags (statistics counting)
     const int n = B.counts[bounce];
     const int qi = bounce & 1;
     WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + bounce) {
@@ -771,8 +830,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S, const DevPara
             o = B.q_o[qi][i];
             d = B.q_d[qi][i];
         }
+        const int sid = BATCH ? __float_as_int(d.w) : 0;
+        const DevScene& S = scene_of<BATCH>(S0, Q, sid);
         const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
         if (valid) {
+            const DevParams& P = params_of<BATCH>(Pp, Q, sid);
             if (!(h.t < INF)) {
                 const int path = __float_as_int(o.w);
                 const float4 T = B.throughput[path];
@@ -784,7 +846,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S, const DevPara
                 B.radiance[path] = L;
             }
         }
-        warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
+        warp_add_stats(P0, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
     }
 }
 
@@ -1018,63 +1080,148 @@ __device__ __forceinline__ float filmic(float v, float exposure, float a, float 
     return saturate_j((m * (a * m + b)) / (m * (c * m + d) + e), 0.0f, 1.0f);
 }
 
+// One sample into a pixel's Kahan-compensated sum (filmAddColor / filmSetColor, AIK:333-378):
+// a rejected primary ray sets the pixel black; the first sample after a clear sets it.
+__device__ __forceinline__ void film_add(float4 L, int flags, bool clear, float4& sum, float4& comp, int& cnt) {
+    if (flags & 1) {
+        sum = make_float4(0, 0, 0, 0); comp = make_float4(0, 0, 0, 0); cnt = 1;
+    } else if (clear || cnt == 0) {
+        sum = make_float4(L.x, L.y, L.z, 0); comp = make_float4(0, 0, 0, 0); cnt = 1;
+    } else {
+        float y, t;
+        y = L.x - comp.x; t = sum.x + y; comp.x = (t - sum.x) - y; sum.x = t;
+        y = L.y - comp.y; t = sum.y + y; comp.y = (t - sum.y) - y; sum.y = t;
+        y = L.z - comp.z; t = sum.z + y; comp.z = (t - sum.z) - y; sum.z = t;
+        cnt += 1;
+    }
+}
+
+// Film average -> tone map -> sRGB -> BGRA8 (AIK:333-378, 410-534, 702-774), with the selection
+// highlight on the green channel (GRK:282-290).
+__device__ __forceinline__ uchar4 tone_map_bgra(const DevParams& P, float4 sum, int cnt, int po) {
+    const float inv = 1.0f / (float)cnt;
+    float r = sum.x * inv, g = sum.y * inv, b = sum.z * inv;
+    g += (po > -1 && po == P.selected_primitive_offset) ? 1.0f : 0.0f;
+    const float ex = P.exposure;
+    switch (P.tone_mapper_type) {
+        case DFPT_TONE_MAPPER_REINHARD:
+            r = (r * ex) / (1.0f + r * ex); g = (g * ex) / (1.0f + g * ex); b = (b * ex) / (1.0f + b * ex);
+            break;
+        case DFPT_TONE_MAPPER_REINHARD_MODIFIED_1:
+            r = 1.0f - expf(-r * ex); g = 1.0f - expf(-g * ex); b = 1.0f - expf(-b * ex);
+            break;
+        case DFPT_TONE_MAPPER_REINHARD_MODIFIED_2: {
+            const float lw2r = 1.0f / (4.0f * 4.0f);
+            const float rm = r * ex, gm = g * ex, bm = b * ex;
+            r = rm * (1.0f + rm * lw2r) / (1.0f + rm); g = gm * (1.0f + gm * lw2r) / (1.0f + gm); b = bm * (1.0f + bm * lw2r) / (1.0f + bm);
+            break;
+        }
+        case DFPT_TONE_MAPPER_FILMIC_CURVE_ACES_MODIFIED:
+            r = filmic(r, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
+            g = filmic(g, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
+            b = filmic(b, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
+            break;
+        default:
+            break;
+    }
+    r = redo_gamma(P, r); g = redo_gamma(P, g); b = redo_gamma(P, b);
+    const int ri = f2i(jmax(jmin(r * 255.0f + 0.5f, 255.0f), 0.0f));
+    const int gi = f2i(jmax(jmin(g * 255.0f + 0.5f, 255.0f), 0.0f));
+    const int bi = f2i(jmax(jmin(b * 255.0f + 0.5f, 255.0f), 0.0f));
+    return make_uchar4((unsigned char)bi, (unsigned char)gi, (unsigned char)ri, 255);
+}
+
 __global__ void __launch_bounds__(256) k_film(const DevParams* __restrict__ Pp, DevPass B) {
     const DevParams& P = *Pp;
     const int n = B.n_pixels;
     const int pass = *B.pass_index;
     const bool clear = pass == P.clear_pass;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 L = B.radiance[i];
         float4 sum = B.film_sum[i], comp = B.film_comp[i];
         int cnt = B.film_n[i];
-        if (B.pixel_flags[i] & 1) {
-            sum = make_float4(0, 0, 0, 0); comp = make_float4(0, 0, 0, 0); cnt = 1;
-        } else if (clear || cnt == 0) {
-            sum = make_float4(L.x, L.y, L.z, 0); comp = make_float4(0, 0, 0, 0); cnt = 1;
-        } else {
-            float y, t;
-            y = L.x - comp.x; t = sum.x + y; comp.x = (t - sum.x) - y; sum.x = t;
-            y = L.y - comp.y; t = sum.y + y; comp.y = (t - sum.y) - y; sum.y = t;
-            y = L.z - comp.z; t = sum.z + y; comp.z = (t - sum.z) - y; sum.z = t;
-            cnt += 1;
-        }
+        film_add(B.radiance[i], B.pixel_flags[i], clear, sum, comp, cnt);
         B.film_sum[i] = sum; B.film_comp[i] = comp; B.film_n[i] = cnt;
-        const float inv = 1.0f / (float)cnt;
-        float r = sum.x * inv, g = sum.y * inv, b = sum.z * inv;
-        const int po = B.primitive_offsets[i];
-        g += (po > -1 && po == P.selected_primitive_offset) ? 1.0f : 0.0f;
-        const float ex = P.exposure;
-        switch (P.tone_mapper_type) {
-            case DFPT_TONE_MAPPER_REINHARD:
-                r = (r * ex) / (1.0f + r * ex); g = (g * ex) / (1.0f + g * ex); b = (b * ex) / (1.0f + b * ex);
-                break;
-            case DFPT_TONE_MAPPER_REINHARD_MODIFIED_1:
-                r = 1.0f - expf(-r * ex); g = 1.0f - expf(-g * ex); b = 1.0f - expf(-b * ex);
-                break;
-            case DFPT_TONE_MAPPER_REINHARD_MODIFIED_2: {
-                const float lw2r = 1.0f / (4.0f * 4.0f);
-                const float rm = r * ex, gm = g * ex, bm = b * ex;
-                r = rm * (1.0f + rm * lw2r) / (1.0f + rm); g = gm * (1.0f + gm * lw2r) / (1.0f + gm); b = bm * (1.0f + bm * lw2r) / (1.0f + bm);
-                break;
-            }
-            case DFPT_TONE_MAPPER_FILMIC_CURVE_ACES_MODIFIED:
-                r = filmic(r, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
-                g = filmic(g, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
-                b = filmic(b, ex, 2.51f, 0.03f, 2.43f, 0.59f, 0.14f, 0.0f, -FLT_MAX_F);
-                break;
-            default:
-                break;
-        }
-        r = redo_gamma(P, r); g = redo_gamma(P, g); b = redo_gamma(P, b);
-        const int ri = f2i(jmax(jmin(r * 255.0f + 0.5f, 255.0f), 0.0f));
-        const int gi = f2i(jmax(jmin(g * 255.0f + 0.5f, 255.0f), 0.0f));
-        const int bi = f2i(jmax(jmin(b * 255.0f + 0.5f, 255.0f), 0.0f));
-        reinterpret_cast<uchar4*>(B.bgra)[i] = make_uchar4((unsigned char)bi, (unsigned char)gi, (unsigned char)ri, 255);
+        reinterpret_cast<uchar4*>(B.bgra)[i] = tone_map_bgra(P, sum, cnt, B.primitive_offsets[i]);
     }
 }
 
 __global__ void k_end_pass(DevPass B) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *B.pass_index += 1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batch-only stages: the wave's film tasks, the film update, the final resolve, the wave advance.
+
+// The scenes a wave touches, in order: {scene, local begin, local end, first film task}. A film task
+// is one pixel of one scene that has at least one sample in the wave; a scene whose range in the
+// wave covers fewer samples than pixels touches only that many pixels. Entry `E` holds the total.
+__global__ void k_bwave(DevBatch Q) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const long long base = Q.wave_base[0];
+    const long long end = base + Q.capacity < Q.wave_base[1] ? base + Q.capacity : Q.wave_base[1];
+    int e = 0;
+    long long tasks = 0;
+    if (base < end) {
+        for (int s = batch_scene_of(Q, base); s < Q.n_scenes && Q.sample_begin[s] < end; ++s) {
+            const long long b0 = Q.sample_begin[s], b1 = Q.sample_begin[s + 1];
+            const long long a = (base > b0 ? base : b0) - b0;
+            const long long b = (end < b1 ? end : b1) - b0;
+            const long long np = (long long)Q.params[s].width * Q.params[s].height;
+            Q.wave_tab[4 * e + 0] = s;
+            Q.wave_tab[4 * e + 1] = a;
+            Q.wave_tab[4 * e + 2] = b;
+            Q.wave_tab[4 * e + 3] = tasks;
+            tasks += (b - a) < np ? (b - a) : np;
+            ++e;
+        }
+    }
+    Q.wave_tab[4 * e + 3] = tasks;
+    *Q.wave_entries = e;
+}
+
+// One thread per film task: adds the pixel's samples of this wave in sample order, so each pixel
+// sees the same Kahan sequence as one-scene rendering, pass after pass.
+__global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
+    const int E = *Q.wave_entries;
+    const long long tasks = Q.wave_tab[4 * E + 3];
+    const long long base = Q.wave_base[0];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tasks; t += (long long)gridDim.x * blockDim.x) {
+        int e = 0;
+        while (e + 1 < E && Q.wave_tab[4 * (e + 1) + 3] <= t) ++e;
+        const int s = (int)Q.wave_tab[4 * e + 0];
+        const long long a = Q.wave_tab[4 * e + 1], b = Q.wave_tab[4 * e + 2];
+        const long long np = (long long)Q.params[s].width * Q.params[s].height;
+        const long long first = a + (t - Q.wave_tab[4 * e + 3]);
+        const long long pixel = first % np;
+        const long long f = Q.film_begin[s] + pixel;
+        const long long slot0 = Q.sample_begin[s] - base;
+        float4 sum = B.film_sum[f], comp = B.film_comp[f];
+        int cnt = B.film_n[f];
+        for (long long loc = first; loc < b; loc += np) {
+            const int slot = (int)(slot0 + loc);
+            film_add(B.radiance[slot], B.pixel_flags[slot], false, sum, comp, cnt);
+        }
+        B.film_sum[f] = sum; B.film_comp[f] = comp; B.film_n[f] = cnt;
+    }
+}
+
+// Tone maps every scene's film into its BGRA8 image (once, after the last wave).
+__global__ void __launch_bounds__(256) k_bresolve(DevBatch Q, DevPass B) {
+    const long long n = Q.film_begin[Q.n_scenes];
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = Q.n_scenes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (Q.film_begin[mid] <= f) lo = mid;
+            else hi = mid - 1;
+        }
+        const int cnt = B.film_n[f];
+        reinterpret_cast<uchar4*>(B.bgra)[f] = cnt > 0 ? tone_map_bgra(Q.params[lo], B.film_sum[f], cnt, -1) : make_uchar4(0, 0, 0, 255);
+    }
+}
+
+__global__ void k_bend_wave(DevBatch Q) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) Q.wave_base[0] += Q.capacity;
 }
 
 // FP64 mean of the film average (AIK film semantics: sum / samples per pixel).
@@ -1125,19 +1272,32 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
 template <int V, int BLOCK, int MINB>
 struct TraceCfg {
     static void closest(const LaunchCtx& c, int bounce) {
-        k_trace<false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce, bounce & 1);
+        k_trace<false, false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce, bounce & 1);
     }
     static void shadow(const LaunchCtx& c, int bounce) {
-        k_shadow<V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+        k_shadow<false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce);
     }
     static void final_(const LaunchCtx& c, int bounce) {
-        k_final<V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+        k_final<false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce);
     }
     static int grid(int sms) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<false, V, BLOCK, MINB>, BLOCK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<false, false, V, BLOCK, MINB>, BLOCK, 0);
         return sms * (b > 0 ? b : 1);
     }
+#ifdef DFPT_BATCH_KERNELS
+    // Batch traversal: per-lane walks only (a warp may hold rays of several scenes).
+    static constexpr int BV = V == 2 ? 1 : V;
+    static void b_closest(const LaunchCtx& c, int bounce) {
+        k_trace<true, false, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce, bounce & 1);
+    }
+    static void b_shadow(const LaunchCtx& c, int bounce) {
+        k_shadow<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce);
+    }
+    static void b_final(const LaunchCtx& c, int bounce) {
+        k_final<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce);
+    }
+#endif
 };
 
 static void launch_trace_closest(const LaunchCtx& c, int bounce) {
@@ -1173,8 +1333,34 @@ static int trace_grid(int config, int sms) {
     }
 }
 
-static void launch_camera(const LaunchCtx& c) { k_camera<<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
-static void launch_shade(const LaunchCtx& c, int bounce) { k_shade<<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce); }
+static void launch_camera(const LaunchCtx& c) { k_camera<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}); }
+static void launch_shade(const LaunchCtx& c, int bounce) { k_shade<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce); }
+
+#ifdef DFPT_BATCH_KERNELS
+#define BATCH_DISPATCH(fn)                                                                     \
+    static void launch_b_##fn(const LaunchCtx& c, int bounce) {                                \
+        switch (c.trace_config) {                                                              \
+            TRACE_CONFIGS(BATCH_CASE_##fn)                                                     \
+            default: TraceCfg<0, 256, 4>::b_##fn(c, bounce);                                   \
+        }                                                                                      \
+    }
+#define BATCH_CASE_closest(id, v, b, m) case id: TraceCfg<v, b, m>::b_closest(c, bounce); break;
+#define BATCH_CASE_shadow(id, v, b, m) case id: TraceCfg<v, b, m>::b_shadow(c, bounce); break;
+#define BATCH_CASE_final(id, v, b, m) case id: TraceCfg<v, b, m>::b_final(c, bounce); break;
+BATCH_DISPATCH(closest)
+BATCH_DISPATCH(shadow)
+BATCH_DISPATCH(final)
+#undef BATCH_DISPATCH
+#undef BATCH_CASE_closest
+#undef BATCH_CASE_shadow
+#undef BATCH_CASE_final
+static void launch_b_camera(const LaunchCtx& c, int) { k_camera<true><<<c.grid, 256, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch); }
+static void launch_b_shade(const LaunchCtx& c, int bounce) { k_shade<true><<<c.grid, 256, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce); }
+static void launch_b_wave(const LaunchCtx& c, int) { k_bwave<<<1, 32, 0, c.stream>>>(*c.batch); }
+static void launch_b_film(const LaunchCtx& c, int) { k_bfilm<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
+static void launch_b_resolve(const LaunchCtx& c, int) { k_bresolve<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
+static void launch_b_end(const LaunchCtx& c, int) { k_bend_wave<<<1, 32, 0, c.stream>>>(*c.batch); }
+#endif
 static void launch_simple(const LaunchCtx& c) { k_simple<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_wireframe(const LaunchCtx& c) { k_wireframe<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_film(const LaunchCtx& c) { k_film<<<c.grid, 256, 0, c.stream>>>(c.params, *c.pass); }
@@ -1187,7 +1373,7 @@ static void launch_init_tables(cudaStream_t s, const int* perm, const float* gra
 
 static void occupancy(int sms, int& grid, int& grid_trace, int& grid_simple) {
     int b1 = 0, b3 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_shade, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_shade<false>, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_simple, 128, 0);
     grid = sms * (b1 > 0 ? b1 : 1);
     grid_trace = trace_grid(0, sms);
@@ -1211,6 +1397,17 @@ KernelSet kernel_set() {
     k.occupancy = occupancy;
     k.trace_grid = trace_grid;
     k.trace_configs = 7;
+#ifdef DFPT_BATCH_KERNELS
+    k.b_camera = launch_b_camera;
+    k.b_trace_closest = launch_b_closest;
+    k.b_shade = launch_b_shade;
+    k.b_shadow = launch_b_shadow;
+    k.b_final = launch_b_final;
+    k.b_wave = launch_b_wave;
+    k.b_film = launch_b_film;
+    k.b_resolve = launch_b_resolve;
+    k.b_end = launch_b_end;
+#endif
     return k;
 }
 

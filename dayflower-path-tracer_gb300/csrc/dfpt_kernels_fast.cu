@@ -1,3 +1,5 @@
-// dfpt_kernels_fast.cu - the kernel set with FMA contraction (the path tracer's fast path).
+// dfpt_kernels_fast.cu - the kernel set with FMA contraction (the path tracer's fast path), with
+// the batch stages.
 #define DFPT_NS dfpt_fast
+#define DFPT_BATCH_KERNELS
 #include "dfpt_kernels.cuh"

@@ -12,6 +12,7 @@ struct LaunchCtx {
     cudaStream_t stream;
     int grid, grid_trace, grid_simple;
     int trace_config;  // index into the kernel set's traversal configurations
+    const DevBatch* batch = nullptr;  // batch launches only
 };
 
 struct KernelSet {
@@ -30,6 +31,16 @@ struct KernelSet {
     void (*occupancy)(int sms, int& grid, int& grid_trace, int& grid_simple);
     int (*trace_grid)(int config, int sms);
     int trace_configs;
+    // Batch stages (the fast kernel set only; null elsewhere). The int is the bounce where it applies.
+    void (*b_camera)(const LaunchCtx&, int) = nullptr;
+    void (*b_trace_closest)(const LaunchCtx&, int) = nullptr;
+    void (*b_shade)(const LaunchCtx&, int) = nullptr;
+    void (*b_shadow)(const LaunchCtx&, int) = nullptr;
+    void (*b_final)(const LaunchCtx&, int) = nullptr;
+    void (*b_wave)(const LaunchCtx&, int) = nullptr;
+    void (*b_film)(const LaunchCtx&, int) = nullptr;
+    void (*b_resolve)(const LaunchCtx&, int) = nullptr;
+    void (*b_end)(const LaunchCtx&, int) = nullptr;
 };
 
 namespace dfpt_fast { KernelSet kernel_set(); }

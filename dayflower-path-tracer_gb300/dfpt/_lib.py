@@ -130,6 +130,21 @@ SIGNATURES = {
     "dfpt_compiled_destroy": (C.c_int, [C.c_void_p]),
     "dfpt_compiled_describe": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
     "dfpt_sky_set": (C.c_int, [C.POINTER(Sky), f32p, C.c_float]),
+    "dfpt_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "dfpt_batch_destroy": (C.c_int, [C.c_void_p]),
+    "dfpt_batch_add": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(Sky), C.POINTER(Params), C.c_int32, C.c_int32,
+                                 C.c_int32, i32p]),
+    "dfpt_batch_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dfpt_batch_set_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
+    "dfpt_batch_get_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int64)]),
+    "dfpt_batch_render": (C.c_int, [C.c_void_p]),
+    "dfpt_batch_clear": (C.c_int, [C.c_void_p]),
+    "dfpt_batch_render_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
+    "dfpt_batch_resolve": (C.c_int, [C.c_void_p]),
+    "dfpt_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "dfpt_batch_read_film": (C.c_int, [C.c_void_p, C.c_int32, f32p, i32p]),
+    "dfpt_batch_read_bgra8": (C.c_int, [C.c_void_p, C.c_int32, u8p]),
+    "dfpt_batch_launch_count": (C.c_int, [C.c_void_p, u64p]),
     # Extensions outside the public header (test and measurement hooks).
     "dfpt_set_strict": (C.c_int, [C.c_void_p, C.c_int32]),
     "dfpt_set_record_hits": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -27,3 +27,42 @@ def tune_trace(kernel, passes: int = 4, warmup: int = 1, verbose: bool = False) 
     best = min(results, key=results.get)
     kernel.set_tuning("trace_config", best)
     return {"best": best, "ms_per_pass": results}
+
+
+def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=None, window: int | None = None,
+               verbose: bool = False) -> dict:
+    """Picks the batch's wave capacity (queue depth) and traversal configuration (block size x
+    resident blocks x walk variant) by timing the same window of the batch's own samples with
+    each candidate. The traversal is stackless (threaded BVH with skip pointers), so there is no
+    stack depth to choose. Leaves the films cleared and the best candidate set."""
+    total = batch.total_samples
+    if configs is None:
+        # Walk variant 2 (warp-synchronous) maps to the per-lane walk in a batch; skip duplicates.
+        configs = [c for c in range(batch.get_tuning("trace_configs")) if c not in (4, 5, 6)]
+    results = {}
+    # One window of the batch's sample sequence for every candidate, so the rates compare.
+    span = int(min(total, window if window is not None else 2 * max(capacities)))
+    first = max(0, (total - span) // 2)
+    for cap in capacities:
+        cap = int(min(cap, total))
+        batch.set_tuning("wave_capacity", max(cap, 1024))
+        for cfg in configs:
+            batch.set_tuning("trace_config", cfg)
+            batch.clear()
+            batch.render_range(first, min(span, cap))  # warm-up (graph build, caches)
+            batch.synchronize()
+            t0 = time.perf_counter()
+            batch.render_range(first, span)
+            batch.synchronize()
+            dt = time.perf_counter() - t0
+            results[(cap, cfg)] = span / dt / 1e6
+            if verbose:
+                print(f"wave_capacity {cap} trace_config {cfg}: {results[(cap, cfg)]:.1f} M samples/s", flush=True)
+        if cap >= total:
+            break
+    best = max(results, key=results.get)
+    batch.set_tuning("wave_capacity", max(best[0], 1024))
+    batch.set_tuning("trace_config", best[1])
+    batch.clear()
+    return {"best": {"wave_capacity": best[0], "trace_config": best[1]},
+            "m_samples_per_s": {f"{k[0]}/{k[1]}": round(v, 2) for k, v in results.items()}}

@@ -9,6 +9,8 @@ The reference publishes no benchmark scenes, so each workload is generated from 
   instances_scene   - 40 displaced icospheres of 50,000 triangles each (2M), scale U(0.5,3) in a
                       100^3 box, Glass/Reflection/Lambertian, 500 emissive triangles.
   spheres_on_plane  - 256 spheres on a plane under a Perez sky (the inverse-rendering scene).
+  batch_workload    - 64 scenes (displaced icosphere on a plane) with log-uniform triangle counts in
+                      [1k, 500k], resolutions {256^2, 512^2, 1024^2}, spp {16, 64, 256}.
 Geometry uses only IEEE arithmetic (+, -, *, /, sqrt, floor) so a seed gives the same arrays on
 every host; noise is the reference's simplex fBm (AbstractKernel.java:695-716, 762-900).
 """
@@ -317,3 +319,49 @@ def spheres_on_plane(seed: int = 4, width: int = 512, height: int = 512, count: 
     params = dict(renderer_type=2, pt_ray_depth_maximum=5, pt_ray_depth_russian_roulette=3, tone_mapper_type=2,
                   tone_mapper_exposure=1.0)
     return b.compile("spheres_on_plane"), sc.SkyState(SUN_45, 3.0), params, (width, height)
+
+
+def batch_scene(seed: int, triangles: int, width: int, height: int, threads: int = 0):
+    """One scene of the batched workload: an fBm-displaced icosphere with about `triangles`
+    triangles (20 f^2 for frequency f) in Lambertian/Phong/Glass regions on a checkerboard plane,
+    Perez sky with a seeded turbidity and sun; depth 5, Russian roulette from 3, Reinhard."""
+    rng = np.random.default_rng(1000 + seed)
+    f = max(1, int(round(np.sqrt(triangles / 20.0))))
+    b = sc.SceneBuilder()
+    black = b.constant(0, 0, 0)
+    checker = b.checkerboard((0.5, 0.5, 0.5), (0.2, 0.2, 0.2), 0.0, 5.0, 5.0)
+    b.primitive(b.plane((0, 0, 0), (0, 0, 1), (1, 0, 0)), b.surface(sc.LAMBERTIAN, checker, black, black))
+    pos, idx, region, nrm, uv = displaced_icosphere(f, 0.1, seed, radius=1.5)
+    pos = pos + np.array([0.0, 1.6, 0.0])
+    tng = tangents_for(nrm)
+    mats = (sc.LAMBERTIAN, sc.PHONG, sc.GLASS)
+    for q in range(3):
+        sel = idx[region % 3 == q]
+        if len(sel) == 0:
+            continue
+        tex = b.constant(1, 1, 1) if mats[q] == sc.GLASS else b.constant(*rng.uniform(0.2, 0.9, 3))
+        b.primitive(b.mesh(pos, sel, nrm, uv, tng), b.surface(mats[q], tex, black, black))
+    az = float(rng.uniform(0, 2 * np.pi))
+    el = float(rng.uniform(0.35, 1.2))
+    sun = (float(np.cos(el) * np.cos(az)), float(np.sin(el)), float(np.cos(el) * np.sin(az)))
+    b.camera((0, 2.5, 6), (0, 1.4, 0), 70.0, (width, height))
+    params = dict(renderer_type=2, pt_ray_depth_maximum=5, pt_ray_depth_russian_roulette=3, tone_mapper_type=2,
+                  tone_mapper_exposure=1.0, seed=seed)
+    return b.compile(f"batch_scene_{seed}", threads=threads), sc.SkyState(sun, float(rng.uniform(2.0, 4.0))), params
+
+
+def batch_workload(seed: int = 5, count: int = 64, tri_range=(1000, 500000), resolutions=(256, 512, 1024),
+                   spps=(16, 64, 256)):
+    """The batched-rendering workload: `count` seeded scenes, triangle counts log-uniform in
+    `tri_range`, square resolutions and samples per pixel drawn uniformly from the lists.
+    Returns a list of dicts {scene, sky, params, width, height, spp, triangles}."""
+    rng = np.random.default_rng(seed)
+    tris = np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1]), count))
+    res = rng.choice(resolutions, count)
+    spp = rng.choice(spps, count)
+    out = []
+    for i in range(count):
+        cs, sky, params = batch_scene(seed * 1000 + i, int(tris[i]), int(res[i]), int(res[i]))
+        out.append(dict(scene=cs, sky=sky, params=params, width=int(res[i]), height=int(res[i]), spp=int(spp[i]),
+                        triangles=int(cs.triangles.size // 12)))
+    return out

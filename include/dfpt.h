@@ -275,6 +275,40 @@ int dfpt_compiled_describe(const dfpt_compiled* compiled, dfpt_scene_desc* desc)
 /* Sky.set(sunDirectionWorld, turbidity) (Sky.java:295-333). */
 int dfpt_sky_set(dfpt_sky* sky, const float* sun_direction_world3, float turbidity);
 
+/* ---------------------------------------------------------------------------------------------
+ * Batched rendering. No counterpart in the reference, which renders one scene per
+ * GPURendererKernel (one AbstractRendererKernel per DayflowerApplication window). A batch holds
+ * many compiled scenes resident at once, each with its own resolution, samples per pixel, camera,
+ * sky and dfpt_params (path tracer only, counter-based RNG, no wireframes, one maximum depth for
+ * the whole batch). dfpt_batch_render renders every scene to its sample count in waves of
+ * `wave_capacity` samples, one launch per stage per wave (a replayed CUDA graph); each scene's
+ * film then equals what dfpt_create + dfpt_render(spp) gives for that scene with the same seed. */
+typedef struct dfpt_batch dfpt_batch;
+
+int dfpt_batch_create(dfpt_batch** out);
+int dfpt_batch_destroy(dfpt_batch* batch);
+/* Validates and uploads one scene (the checks of dfpt_create); *index receives its index. */
+int dfpt_batch_add(dfpt_batch* batch, const dfpt_scene_desc* scene, const dfpt_sky* sky,
+                   const dfpt_params* params, int32_t width, int32_t height, int32_t spp, int32_t* index);
+int dfpt_batch_set_stream(dfpt_batch* batch, void* cuda_stream);
+/* Keys: "wave_capacity" (path slots per wave, 1024..2^27), "trace_config" (traversal launch
+ * configuration, as dfpt_set_tuning), "graphs" (0/1). Read-only for get: "trace_configs",
+ * "scenes", "total_samples", "depth". */
+int dfpt_batch_set_tuning(dfpt_batch* batch, const char* key, int64_t value);
+int dfpt_batch_get_tuning(dfpt_batch* batch, const char* key, int64_t* value);
+/* Clears every film, renders all samples of all scenes, tone maps the images (asynchronous). */
+int dfpt_batch_render(dfpt_batch* batch);
+/* Pieces of dfpt_batch_render: zero the films; render the waves covering global samples
+ * [first_sample, first_sample + count) (scene-major order); tone map the films. */
+int dfpt_batch_clear(dfpt_batch* batch);
+int dfpt_batch_render_range(dfpt_batch* batch, int64_t first_sample, int64_t count);
+int dfpt_batch_resolve(dfpt_batch* batch);
+int dfpt_batch_synchronize(dfpt_batch* batch);
+/* One scene's film average (rgb, 3 floats per pixel) and sample counts, as dfpt_read_film. */
+int dfpt_batch_read_film(dfpt_batch* batch, int32_t index, float* rgb, int32_t* samples);
+int dfpt_batch_read_bgra8(dfpt_batch* batch, int32_t index, uint8_t* bgra);
+int dfpt_batch_launch_count(dfpt_batch* batch, uint64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif
