@@ -5,6 +5,7 @@
 // film, the wavefront form of GPURendererKernel.run (GPURendererKernel.java:252-308).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -278,6 +279,16 @@ struct dfpt_handle {
     int clear_pass = 0;
     bool counting = false;
     bool record_hits = false;
+    // Differentiable rendering (dfpt_diff_*): parameters, the forward's per-sample records, the
+    // backward's gradient rows.
+    bool diff_on = false;     // shading reads the per-primitive parameters
+    bool diff_ready = false;  // the last forward's samples are stored for a backward
+    int diff_pass0 = 0, diff_spp = 0;
+    size_t diff_capacity = 0;  // samples x pixels the per-sample records hold
+    DevBuf<float4> diff_albedo, diff_emission, diff_L, diff_dldi;
+    DevBuf<float> diff_exponent, diff_sky_tan;
+    DevBuf<int> vis, diff_vis;
+    DevBuf<double> diff_rows, diff_out;
     // Graph of one pass.
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -299,6 +310,9 @@ void release(dfpt_handle* h) {
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     h->graph_exec = nullptr;
     h->sc.release();
+    h->diff_albedo.release(); h->diff_emission.release(); h->diff_L.release(); h->diff_dldi.release();
+    h->diff_exponent.release(); h->diff_sky_tan.release(); h->vis.release(); h->diff_vis.release();
+    h->diff_rows.release(); h->diff_out.release();
     DevBuf<float>* fb[] = {&h->hit_dist, &h->hit_normal, &h->scratch_rgb};
     for (auto* b : fb) b->release();
     DevBuf<int>* ib[] = {&h->pixel_flags, &h->counts, &h->pass_index, &h->film_n, &h->primitive_offsets, &h->hit_prim, &h->hit_type, &h->hit_off};
@@ -386,7 +400,71 @@ void fill_dev_params(dfpt_handle* h) {
     d.record_hits = h->record_hits ? 1 : 0;
     d.counting = h->counting ? 1 : 0;
     d.clear_pass = h->clear_pass;
+    if (h->diff_on) {
+        d.diff = 1;
+        d.diff_pass0 = h->diff_pass0;
+        d.diff_spp = h->diff_spp;
+        d.diff_albedo = h->diff_albedo.p;
+        d.diff_emission = h->diff_emission.p;
+        d.diff_exponent = h->diff_exponent.p;
+        d.diff_sky_tan = h->diff_sky_tan.p;
+    }
 }
+
+// The sky fields the kernels read (DevParams, SKY_* order) as functions of turbidity and the world
+// sun direction: Sky.set (Sky.java:295-333) and the derived Perez denominators, in double without
+// the float narrowing, for the tangent table.
+void sky_fields(double t, const double* dir, double* f) {
+    const double len = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    const double wx = dir[0] / len, wy = dir[1] / len, wz = dir[2] / len;
+    // Sky basis u = X, v = Z, w = Y: the sky-frame sun direction is (x, z, y), already unit.
+    const double sx = wx, sy = wz, sz = wy;
+    f[SKY_SUN_DIR] = sx; f[SKY_SUN_DIR + 1] = sy; f[SKY_SUN_DIR + 2] = sz;
+    const double theta = std::acos(std::max(-1.0, std::min(1.0, sz)));
+    const double th2 = theta * theta, th3 = th2 * theta, t2 = t * t;
+    const double pi_f = (double)3.14159274101257324219f;
+    const double chi = (4.0 / 9.0 - t / 120.0) * (pi_f - 2.0 * theta);
+    const double L[5] = {0.17872 * t - 1.46303, -0.35540 * t + 0.42749, -0.02266 * t + 5.32505, 0.12064 * t - 2.57705, -0.06696 * t + 0.37027};
+    const double X[5] = {-0.01925 * t - 0.25922, -0.06651 * t + 0.00081, -0.00041 * t + 0.21247, -0.06409 * t - 0.89887, -0.00325 * t + 0.04517};
+    const double Y[5] = {-0.01669 * t - 0.26078, -0.09495 * t + 0.00921, -0.00792 * t + 0.21023, -0.04405 * t - 1.65369, -0.01092 * t + 0.05291};
+    for (int i = 0; i < 5; ++i) {
+        f[SKY_PEREZ_L + i] = L[i];
+        f[SKY_PEREZ_X + i] = X[i];
+        f[SKY_PEREZ_Y + i] = Y[i];
+    }
+    f[SKY_ZENITH_L] = ((4.0453 * t - 4.9710) * std::tan(chi) - 0.2155 * t + 2.4192) * 1000.0;
+    f[SKY_ZENITH_X] = (0.00165 * th3 - 0.00374 * th2 + 0.00208 * theta + 0.0) * t2 +
+                      (-0.02902 * th3 + 0.06377 * th2 - 0.03202 * theta + 0.00394) * t +
+                      (0.11693 * th3 - 0.21196 * th2 + 0.06052 * theta + 0.25885);
+    f[SKY_ZENITH_Y] = (0.00275 * th3 - 0.00610 * th2 + 0.00316 * theta + 0.0) * t2 +
+                      (-0.04212 * th3 + 0.08970 * th2 - 0.04153 * theta + 0.00515) * t +
+                      (0.15346 * th3 - 0.26756 * th2 + 0.06669 * theta + 0.26688);
+    const double c0 = std::cos(theta);
+    f[SKY_DEN_L] = (1.0 + L[0] * std::exp(L[1])) * (1.0 + L[2] * std::exp(L[3] * theta) + L[4] * c0 * c0);
+    f[SKY_DEN_X_A] = 1.0 + X[0] * std::exp(X[1]);
+    f[SKY_DEN_Y_A] = 1.0 + Y[0] * std::exp(Y[1]);
+    f[SKY_COS_THETA0] = c0;
+    for (int i = 0; i < 3; ++i) {
+        f[SKY_SUN_ORIGIN + i] = (i == 0 ? wx : i == 1 ? wy : wz) * 10000.0;
+        f[SKY_SUN_DIR_WORLD + i] = i == 0 ? wx : i == 1 ? wy : wz;
+    }
+}
+
+// d(field)/d(turbidity, sun x, sun y, sun z) by central differences of sky_fields in double
+// (smooth closed forms: step 1e-6 leaves ~1e-10 relative error).
+void sky_tangents(double t, const double* dir, float* out) {
+    const double h = 1.0e-6;
+    double fp[DFPT_SKY_FIELDS], fm[DFPT_SKY_FIELDS];
+    for (int j = 0; j < 4; ++j) {
+        double tp = t, tm = t, dp[3] = {dir[0], dir[1], dir[2]}, dm[3] = {dir[0], dir[1], dir[2]};
+        if (j == 0) { tp += h; tm -= h; }
+        else { dp[j - 1] += h; dm[j - 1] -= h; }
+        sky_fields(tp, dp, fp);
+        sky_fields(tm, dm, fm);
+        for (int k = 0; k < DFPT_SKY_FIELDS; ++k) out[4 * k + j] = (float)((fp[k] - fm[k]) / (2.0 * h));
+    }
+}
+
 
 int push_params(dfpt_handle* h) {
     fill_dev_params(h);
@@ -449,6 +527,24 @@ int issue_pass(dfpt_handle* h) {
     mark(h, KIND_FILM); K.film(c); ++k;
     mark(h, KIND_END); K.end_pass(c); ++k;
     mark(h, KIND_COUNT);
+    return k;
+}
+
+// The replay of the last forward's samples (k_shade_adj / k_final_adj) for one pass; returns the
+// number of kernels launched.
+int issue_replay_pass(dfpt_handle* h) {
+    const KernelSet& K = h->fast;
+    const LaunchCtx& c = h->ctx;
+    int k = 0;
+    cudaMemsetAsync(h->counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), h->stream);
+    const int nb = h->params.pt_ray_depth_maximum < 1 ? 1 : (h->params.pt_ray_depth_maximum > DFPT_MAX_DEPTH ? DFPT_MAX_DEPTH : h->params.pt_ray_depth_maximum);
+    K.camera(c); ++k;
+    for (int b = 0; b < nb; ++b) {
+        K.trace_closest(c, b); ++k;
+        K.shade_adj(c, b); ++k;
+    }
+    K.final_adj(c, nb); ++k;
+    K.end_pass(c); ++k;
     return k;
 }
 
@@ -891,6 +987,128 @@ int dfpt_read_hits(dfpt_handle* h, int32_t* prim, int32_t* type, int32_t* off, f
     if (normal3) CUDA_TRY(cudaMemcpyAsync(normal3, h->hit_normal.p, n * 12, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return DFPT_OK;
+}
+
+int dfpt_diff_forward(dfpt_handle* h, const dfpt_diff_params* dp, int32_t spp, float* image_rgb) {
+    if (!h || !dp) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (spp < 1) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "spp %d < 1", spp);
+    if (h->params.renderer_type != DFPT_RENDERER_PATH_TRACER) return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "differentiable rendering needs the path tracer");
+    if (h->params.rng_kind != DFPT_RNG_COUNTER) return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "the replay needs the counter-based RNG");
+    if (h->use_strict) return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "differentiable rendering runs on the fast kernel set");
+    if (!h->fast.shade_adj) return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "kernel set has no adjoint");
+    if (!(dp->turbidity > 0.0f) || !std::isfinite(dp->turbidity)) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "turbidity must be positive");
+    const double sl = (double)dp->sun_direction[0] * dp->sun_direction[0] + (double)dp->sun_direction[1] * dp->sun_direction[1] +
+                      (double)dp->sun_direction[2] * dp->sun_direction[2];
+    if (!(sl > 0.0) || !std::isfinite(sl)) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "sun direction must be a nonzero finite vector");
+    const int np = h->sc.scene.primitive_count;
+    const size_t n = (size_t)h->n_pixels;
+    // Per-primitive parameters.
+    std::vector<float4> alb((size_t)std::max(np, 1), make_float4(1, 1, 1, 0)), emi((size_t)std::max(np, 1), make_float4(0, 0, 0, 0));
+    std::vector<float> ex((size_t)std::max(np, 1), 50.0f);
+    for (int i = 0; i < np; ++i) {
+        if (dp->albedo) alb[i] = make_float4(dp->albedo[3 * i], dp->albedo[3 * i + 1], dp->albedo[3 * i + 2], 0.0f);
+        if (dp->emission) emi[i] = make_float4(dp->emission[3 * i], dp->emission[3 * i + 1], dp->emission[3 * i + 2], 0.0f);
+        if (dp->phong_exponent) {
+            ex[i] = dp->phong_exponent[i];
+            if (!(ex[i] > -1.0f) || !std::isfinite(ex[i])) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "Phong exponent %g of primitive %d must exceed -1", ex[i], i);
+        }
+    }
+    CUDA_TRY(h->stream ? cudaStreamSynchronize(h->stream) : cudaSuccess);
+    CUDA_TRY(upload(h->diff_albedo, alb, h->stream));
+    CUDA_TRY(upload(h->diff_emission, emi, h->stream));
+    CUDA_TRY(upload(h->diff_exponent, ex, h->stream));
+    // Sky from (turbidity, sun direction), keeping the sky/sun switches.
+    dfpt_sky sky;
+    const int sky_on = h->sky.is_sky_active, sun_on = h->sky.is_sun_active;
+    int r = dfpt_sky_set(&sky, dp->sun_direction, dp->turbidity);
+    if (r) return r;
+    sky.is_sky_active = sky_on;
+    sky.is_sun_active = sun_on;
+    if ((h->sky.is_sun_active == 1) != (sky.is_sun_active == 1)) h->graph_valid = false;
+    h->sky = sky;
+    std::vector<float> tan(4 * DFPT_SKY_FIELDS);
+    const double dir[3] = {dp->sun_direction[0], dp->sun_direction[1], dp->sun_direction[2]};
+    sky_tangents((double)dp->turbidity, dir, tan.data());
+    CUDA_TRY(upload(h->diff_sky_tan, tan, h->stream));
+    // Per-sample records of this forward.
+    if (!h->vis.p) {
+        CUDA_TRY(h->vis.alloc(n));
+        CUDA_TRY(cudaMemsetAsync(h->vis.p, 0, n * sizeof(int), h->stream));
+    }
+    if (h->diff_capacity < (size_t)spp * n) {
+        h->diff_L.release();
+        h->diff_vis.release();
+        CUDA_TRY(h->diff_L.alloc((size_t)spp * n));
+        CUDA_TRY(h->diff_vis.alloc((size_t)spp * n));
+        h->diff_capacity = (size_t)spp * n;
+    }
+    if (!h->diff_dldi.p) CUDA_TRY(h->diff_dldi.alloc(n));
+    const int rows = std::max(h->ctx.grid, 1), row_len = np * DFPT_DIFF_PER_PRIM + DFPT_DIFF_GLOBAL;
+    if (h->diff_rows.n != (size_t)rows * row_len) {
+        h->diff_rows.release();
+        h->diff_out.release();
+        CUDA_TRY(h->diff_rows.alloc((size_t)rows * row_len));
+        CUDA_TRY(h->diff_out.alloc((size_t)row_len));
+    }
+    DevPass& B = h->pass;
+    B.vis = h->vis.p; B.diff_L = h->diff_L.p; B.diff_vis = h->diff_vis.p; B.diff_dldi = h->diff_dldi.p;
+    B.diff_rows = h->diff_rows.p; B.diff_row_len = row_len;
+    h->graph_valid = false;  // the pass record changed
+    h->diff_on = true;
+    h->diff_pass0 = h->host_pass;
+    h->diff_spp = spp;
+    h->clear_pass = h->host_pass;  // the forward starts a fresh film
+    r = push_params(h);
+    if (!r) r = dfpt_render(h, spp);
+    if (r) return r;
+    h->diff_ready = true;
+    if (image_rgb) return dfpt_read_film(h, image_rgb, nullptr);
+    return DFPT_OK;
+}
+
+int dfpt_diff_backward(dfpt_handle* h, const float* dloss_dimage, double* grad_albedo, double* grad_emission,
+                       double* grad_phong_exponent, double* grad_sky) {
+    if (!h || !dloss_dimage) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!h->diff_ready) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "dfpt_diff_backward needs a dfpt_diff_forward first");
+    const size_t n = (size_t)h->n_pixels;
+    const int np = h->sc.scene.primitive_count;
+    const int row_len = np * DFPT_DIFF_PER_PRIM + DFPT_DIFF_GLOBAL;
+    const int rows = (int)(h->diff_rows.n / (size_t)row_len);
+    std::vector<float4> w(n);
+    for (size_t i = 0; i < n; ++i) w[i] = make_float4(dloss_dimage[3 * i], dloss_dimage[3 * i + 1], dloss_dimage[3 * i + 2], 0.0f);
+    CUDA_TRY(upload(h->diff_dldi, w, h->stream));
+    CUDA_TRY(cudaMemsetAsync(h->diff_rows.p, 0, h->diff_rows.n * sizeof(double), h->stream));
+    // Replay the forward's passes: same pass indices, so the same RNG streams.
+    const int pass0 = h->diff_pass0;
+    CUDA_TRY(cudaMemcpyAsync(h->pass_index.p, &pass0, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    for (int j = 0; j < h->diff_spp; ++j) h->launches += (uint64_t)issue_replay_pass(h);
+    h->fast.diff_reduce(h->ctx, h->diff_rows.p, rows, row_len, h->diff_out.p);
+    h->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    std::vector<double> out((size_t)row_len);
+    CUDA_TRY(cudaMemcpyAsync(out.data(), h->diff_out.p, (size_t)row_len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));  // also keeps pass0 alive for its copy
+    for (int i = 0; i < np; ++i) {
+        const double* g = out.data() + (size_t)i * DFPT_DIFF_PER_PRIM;
+        if (grad_albedo) for (int c = 0; c < 3; ++c) grad_albedo[3 * i + c] = g[c];
+        if (grad_emission) for (int c = 0; c < 3; ++c) grad_emission[3 * i + c] = g[3 + c];
+        if (grad_phong_exponent) grad_phong_exponent[i] = g[6];
+    }
+    if (grad_sky) for (int j = 0; j < DFPT_DIFF_GLOBAL; ++j) grad_sky[j] = out[(size_t)np * DFPT_DIFF_PER_PRIM + j];
+    return DFPT_OK;
+}
+
+int dfpt_diff_end(dfpt_handle* h) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->diff_on = false;
+    h->diff_ready = false;
+    h->diff_L.release(); h->diff_vis.release(); h->diff_capacity = 0;
+    h->diff_rows.release(); h->diff_out.release();
+    DevPass& B = h->pass;
+    B.diff_L = nullptr; B.diff_vis = nullptr; B.diff_rows = nullptr;
+    h->graph_valid = false;
+    return push_params(h);
 }
 
 int dfpt_read_counters(dfpt_handle* h, uint64_t* c4) {

@@ -71,7 +71,23 @@ struct DevParams {
     float wire_cos;
     // sRGB redo-gamma constants (RGBColorSpace.SRGB).
     float cs_break, cs_gamma, cs_slope, cs_slope_match, cs_segment;
+    // Differentiable rendering (dfpt_diff_*): per-primitive parameters and replay bookkeeping.
+    int diff;                     // 1: shading reads the per-primitive parameters below
+    int diff_pass0, diff_spp;     // the forward's first pass index and sample count
+    const float4* diff_albedo;    // per primitive {r, g, b, 0}: multiplies the albedo texture color
+    const float4* diff_emission;  // per primitive: added to the emission texture color
+    const float* diff_exponent;   // per primitive Phong exponent (the reference fixes 50)
+    const float* diff_sky_tan;    // [DFPT_SKY_FIELDS][4]: d(field)/d(turbidity, sun x, sun y, sun z)
 };
+
+// Sky fields the sky and sun code reads, in the order of the tangent table above.
+enum {
+    SKY_SUN_DIR = 0, SKY_PEREZ_L = 3, SKY_PEREZ_X = 8, SKY_PEREZ_Y = 13, SKY_ZENITH_L = 18, SKY_ZENITH_X = 19,
+    SKY_ZENITH_Y = 20, SKY_DEN_L = 21, SKY_DEN_X_A = 22, SKY_DEN_Y_A = 23, SKY_COS_THETA0 = 24, SKY_SUN_ORIGIN = 25,
+    SKY_SUN_DIR_WORLD = 28, DFPT_SKY_FIELDS = 31
+};
+#define DFPT_DIFF_PER_PRIM 7  // gradient entries per primitive: albedo rgb, emission rgb, exponent
+#define DFPT_DIFF_GLOBAL 4    // turbidity, sun direction x, y, z
 
 // Wavefront buffers of one handle. Queue entries are SoA float4 records.
 struct DevPass {
@@ -103,6 +119,13 @@ struct DevPass {
     int* hit_shape_offset;
     float* hit_distance;
     float* hit_normal;
+    // Differentiable rendering.
+    int* vis;                  // per path: bit b = the sun shadow ray of bounce b was unoccluded
+    float4* diff_L;            // [sample][pixel] path radiance of the forward's samples
+    int* diff_vis;             // [sample][pixel] the forward's visibility bits
+    const float4* diff_dldi;   // per pixel dLoss/dImage (rgb)
+    double* diff_rows;         // per block of the adjoint kernels: gradient partials
+    int diff_row_len;          // primitives x 7 + 4
 };
 
 // Many scenes rendered by one set of launches. Every scene's samples form one global sequence

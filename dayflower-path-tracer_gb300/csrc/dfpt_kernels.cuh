@@ -542,6 +542,7 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
             B.pixel_flags[i] = live ? 0 : 1;
             B.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
             B.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (!BATCH && P.diff) B.vis[i] = 0;
             if (!BATCH && P.wireframes == 1) {
                 B.primary_o[i] = o;
                 B.primary_d[i] = d;
@@ -578,6 +579,130 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S0, const DevPar
         if (valid) B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
         warp_add_stats(P, B.stats, ANY ? 1 : 0, valid ? 1u : 0u, st.nodes, st.tris);
     }
+}
+
+// Differentiable mode: the primitive's parameters applied to its texture colors.
+__device__ __forceinline__ void diff_surface(const DevParams& P, int prim, float& ar, float& ag, float& ab, float& er, float& eg,
+                                             float& eb, float& exponent) {
+    const float4 a = P.diff_albedo[prim], e = P.diff_emission[prim];
+    ar *= a.x; ag *= a.y; ab *= a.z;
+    er += e.x; eg += e.y; eb += e.z;
+    exponent = P.diff_exponent[prim];
+}
+
+// Material sampling at one vertex (GRK:3323-3686): the next ray, and the throughput T multiplied
+// by the vertex's factors. Reports whether the albedo was one of them and, for a Phong lobe, the
+// sampled cosine (the path-replay adjoint differentiates through both).
+struct Scatter {
+    float4 o, d;       // next ray origin / direction (w unset)
+    bool albedo;       // T was multiplied by the albedo
+    float phong_ct;    // Phong: cosine to the lobe axis drawn from (n + 1) cos^n; else 0
+};
+
+__device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx, float wy, float wz, float4 o, float4 d, float dp2,
+                                           float ar, float ag, float ab, float exponent, Rng& rng, float4& T) {
+    Scatter out;
+    out.albedo = false;
+    out.phong_ct = 0.0f;
+    float ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+    const float rx = dx - s.nx * dp2, ry = dy - s.ny * dp2, rz = dz - s.nz * dp2;
+    if (material == DFPT_MATERIAL_CLEAR_COAT) {
+        const float a = 1.5f - 1.0f, b = 1.5f + 1.0f, c = 1.0f / 1.5f;
+        const float e = (a * a) / (b * b);
+        const float d0 = wx * dx + wy * dy + wz * dz;
+        const float tir = 1.0f - c * c * (1.0f - d0 * d0);
+        if (tir < 0.0f) {
+            ox = s.px + wx * 0.02f; oy = s.py + wy * 0.02f; oz = s.pz + wz * 0.02f;
+            dx = rx; dy = ry; dz = rz;
+        } else {
+            const float a2 = 1.0f - (-d0);
+            const float refl = e + (1.0f - e) * a2 * a2 * a2 * a2 * a2;
+            const float trans = 1.0f - refl;
+            const float pr = 0.25f + 0.5f * refl;
+            const float rp = refl / pr, tp = trans / (1.0f - pr);
+            const bool is_refl = rng.next() < pr;
+            const float m = is_refl ? rp : tp;
+            T.x *= m; T.y *= m; T.z *= m;
+            if (is_refl) {
+                ox = s.px + wx * 0.02f; oy = s.py + wy * 0.02f; oz = s.pz + wz * 0.02f;
+                dx = rx; dy = ry; dz = rz;
+            } else {
+                const float u = rng.next(), v = rng.next();
+                cosine_dir(wx, wy, wz, u, v, dx, dy, dz);
+                ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
+                T.x *= ar; T.y *= ag; T.z *= ab;
+                out.albedo = true;
+            }
+        }
+    } else if (material == DFPT_MATERIAL_LAMBERTIAN) {
+        const float u = rng.next(), v = rng.next();
+        cosine_dir(wx, wy, wz, u, v, dx, dy, dz);
+        ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
+        T.x *= ar; T.y *= ag; T.z *= ab;
+        out.albedo = true;
+    } else if (material == DFPT_MATERIAL_PHONG) {
+        const float u = rng.next(), v = rng.next();
+        const float phi = TWO_PI * u;
+        const float ct = powf(1.0f - v, 1.0f / (exponent + 1.0f));
+        out.phong_ct = ct;
+        const float st = sqrtf(jmax(0.0f, 1.0f - ct * ct));
+        const float x = cosf(phi) * st, y = sinf(phi) * st, z = ct;
+        const float rwr = rsqrt_j(rx * rx + ry * ry + rz * rz);
+        const float rnx = rx * rwr, rny = ry * rwr, rnz = rz * rwr;
+        const bool isY = fabsf(rnx) > 0.1f;
+        const float ux = (isY ? 1.0f : 0.0f) * rnz;
+        const float uy = -((isY ? 0.0f : 1.0f) * rnz);
+        const float uz = (isY ? 0.0f : 1.0f) * rny - (isY ? 1.0f : 0.0f) * rnx;
+        const float ur = rsqrt_j(ux * ux + uy * uy + uz * uz);
+        const float unx = ux * ur, uny = uy * ur, unz = uz * ur;
+        const float vnx = rny * unz - rnz * uny, vny = rnz * unx - rnx * unz, vnz = rnx * uny - rny * unx;
+        // The reference mixes the unnormalised reflection vector in here (GRK:3555-3557).
+        const float px = unx * x + vnx * y + rx * z;
+        const float py = uny * x + vny * y + ry * z;
+        const float pz = unz * x + vnz * y + rz * z;
+        const float pr = rsqrt_j(px * px + py * py + pz * pz);
+        ox = s.px + rnx * 0.01f; oy = s.py + rny * 0.01f; oz = s.pz + rnz * 0.01f;
+        dx = px * pr; dy = py * pr; dz = pz * pr;
+        T.x *= ar; T.y *= ag; T.z *= ab;
+        out.albedo = true;
+    } else if (material == DFPT_MATERIAL_GLASS) {
+        const float a = 1.5f - 1.0f, b = 1.5f + 1.0f, c = 1.0f / 1.5f, dd = 1.5f / 1.0f;
+        const float e = (a * a) / (b * b);
+        const bool going_in = s.nx * wx + s.ny * wy + s.nz * wz > 0.0f;
+        const float nnt = going_in ? c : dd;
+        const float dw = wx * dx + wy * dy + wz * dz;
+        const float tir = 1.0f - nnt * nnt * (1.0f - dw * dw);
+        if (tir < 0.0f) {
+            ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
+            dx = rx; dy = ry; dz = rz;
+        } else {
+            const float st = sqrtf(tir);
+            const float scl = going_in ? dw * nnt + st : -(dw * nnt + st);
+            const float t0x = dx * nnt - s.nx * scl, t0y = dy * nnt - s.ny * scl, t0z = dz * nnt - s.nz * scl;
+            const float tr = rsqrt_j(t0x * t0x + t0y * t0y + t0z * t0z);
+            const float tdx = t0x * tr, tdy = t0y * tr, tdz = t0z * tr;
+            const float a1 = going_in ? -dw : tdx * s.nx + tdy * s.ny + tdz * s.nz;
+            const float a2 = 1.0f - a1;
+            const float refl = e + (1.0f - e) * a2 * a2 * a2 * a2 * a2;
+            const float trans = 1.0f - refl;
+            const float pr = 0.25f + 0.5f * refl;
+            const float rp = refl / pr, tp = trans / (1.0f - pr);
+            const bool is_refl = rng.next() < pr;
+            const float m = is_refl ? rp : tp;
+            T.x *= m; T.y *= m; T.z *= m;
+            const float eps = is_refl ? 0.01f : 0.000001f;
+            ox = s.px + wx * eps; oy = s.py + wy * eps; oz = s.pz + wz * eps;
+            dx = is_refl ? rx : tdx; dy = is_refl ? ry : tdy; dz = is_refl ? rz : tdz;
+        }
+    } else if (material == DFPT_MATERIAL_REFLECTION) {
+        ox = s.px + s.nx * 0.000001f; oy = s.py + s.ny * 0.000001f; oz = s.pz + s.nz * 0.000001f;
+        dx = rx; dy = ry; dz = rz;
+        T.x *= ar; T.y *= ag; T.z *= ab;
+        out.albedo = true;
+    }
+    out.o = make_float4(ox, oy, oz, 0.0f);
+    out.d = make_float4(dx, dy, dz, 0.0f);
+    return out;
 }
 
 // One bounce of shading: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
@@ -640,8 +765,10 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __r
                 const int albedo = texture_color(S, f2i(__ldg(S.surfaces + so_off + 1)), s);
                 const int emission = texture_color(S, f2i(__ldg(S.surfaces + so_off + 2)), s);
                 float ar = cr(albedo), ag = cg(albedo), ab = cb(albedo);
-                const float er = cr(emission), eg = cg(emission), eb = cb(emission);
+                float er = cr(emission), eg = cg(emission), eb = cb(emission);
                 const int material = f2i(__ldg(S.surfaces + so_off + 0));
+                float exponent = 50.0f;  // the reference's fixed Phong exponent (GRK:3524)
+                if (!BATCH && P.diff) diff_surface(P, h.prim, ar, ag, ab, er, eg, eb, exponent);
                 if ((material == DFPT_MATERIAL_CLEAR_COAT || material == DFPT_MATERIAL_LAMBERTIAN || material == DFPT_MATERIAL_PHONG) &&
                     P.sun_active == 1) {
                     const float u = rng.next(), v = rng.next();
@@ -650,7 +777,8 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __r
                         emit_shadow = true;
                         so = make_float4(s.px, s.py, s.pz, __int_as_float(path));
                         sd = make_float4(lx, ly, lz, sid_bits);
-                        sc = make_float4(T.x * (ar * 1.0f * dot1 * INV_PI), T.y * (ag * 1.0f * dot1 * INV_PI), T.z * (ab * 1.0f * dot1 * INV_PI), 0.0f);
+                        sc = make_float4(T.x * (ar * 1.0f * dot1 * INV_PI), T.y * (ag * 1.0f * dot1 * INV_PI), T.z * (ab * 1.0f * dot1 * INV_PI),
+                                         __int_as_float(bounce));
                     }
                 }
                 L.x += T.x * er;
@@ -670,100 +798,10 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __r
                     }
                 }
                 if (alive) {
-                    float ox = o4.x, oy = o4.y, oz = o4.z, dx = d4.x, dy = d4.y, dz = d4.z;
-                    const float rx = dx - s.nx * dp2, ry = dy - s.ny * dp2, rz = dz - s.nz * dp2;
-                    if (material == DFPT_MATERIAL_CLEAR_COAT) {
-                        const float a = 1.5f - 1.0f, b = 1.5f + 1.0f, c = 1.0f / 1.5f;
-                        const float e = (a * a) / (b * b);
-                        const float d0 = wx * dx + wy * dy + wz * dz;
-                        const float tir = 1.0f - c * c * (1.0f - d0 * d0);
-                        if (tir < 0.0f) {
-                            ox = s.px + wx * 0.02f; oy = s.py + wy * 0.02f; oz = s.pz + wz * 0.02f;
-                            dx = rx; dy = ry; dz = rz;
-                        } else {
-                            const float a2 = 1.0f - (-d0);
-                            const float refl = e + (1.0f - e) * a2 * a2 * a2 * a2 * a2;
-                            const float trans = 1.0f - refl;
-                            const float pr = 0.25f + 0.5f * refl;
-                            const float rp = refl / pr, tp = trans / (1.0f - pr);
-                            const bool is_refl = rng.next() < pr;
-                            const float m = is_refl ? rp : tp;
-                            T.x *= m; T.y *= m; T.z *= m;
-                            if (is_refl) {
-                                ox = s.px + wx * 0.02f; oy = s.py + wy * 0.02f; oz = s.pz + wz * 0.02f;
-                                dx = rx; dy = ry; dz = rz;
-                            } else {
-                                const float u = rng.next(), v = rng.next();
-                                cosine_dir(wx, wy, wz, u, v, dx, dy, dz);
-                                ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
-                                T.x *= ar; T.y *= ag; T.z *= ab;
-                            }
-                        }
-                    } else if (material == DFPT_MATERIAL_LAMBERTIAN) {
-                        const float u = rng.next(), v = rng.next();
-                        cosine_dir(wx, wy, wz, u, v, dx, dy, dz);
-                        ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
-                        T.x *= ar; T.y *= ag; T.z *= ab;
-                    } else if (material == DFPT_MATERIAL_PHONG) {
-                        const float u = rng.next(), v = rng.next();
-                        const float phi = TWO_PI * u;
-                        const float ct = powf(1.0f - v, 1.0f / (50.0f + 1.0f));
-                        const float st = sqrtf(jmax(0.0f, 1.0f - ct * ct));
-                        const float x = cosf(phi) * st, y = sinf(phi) * st, z = ct;
-                        const float rwr = rsqrt_j(rx * rx + ry * ry + rz * rz);
-                        const float rnx = rx * rwr, rny = ry * rwr, rnz = rz * rwr;
-                        const bool isY = fabsf(rnx) > 0.1f;
-                        const float ux = (isY ? 1.0f : 0.0f) * rnz;
-                        const float uy = -((isY ? 0.0f : 1.0f) * rnz);
-                        const float uz = (isY ? 0.0f : 1.0f) * rny - (isY ? 1.0f : 0.0f) * rnx;
-                        const float ur = rsqrt_j(ux * ux + uy * uy + uz * uz);
-                        const float unx = ux * ur, uny = uy * ur, unz = uz * ur;
-                        const float vnx = rny * unz - rnz * uny, vny = rnz * unx - rnx * unz, vnz = rnx * uny - rny * unx;
-                        // The reference mixes the unnormalised reflection vector in here (GRK:3555-3557).
-                        const float px = unx * x + vnx * y + rx * z;
-                        const float py = uny * x + vny * y + ry * z;
-                        const float pz = unz * x + vnz * y + rz * z;
-                        const float pr = rsqrt_j(px * px + py * py + pz * pz);
-                        ox = s.px + rnx * 0.01f; oy = s.py + rny * 0.01f; oz = s.pz + rnz * 0.01f;
-                        dx = px * pr; dy = py * pr; dz = pz * pr;
-                        T.x *= ar; T.y *= ag; T.z *= ab;
-                    } else if (material == DFPT_MATERIAL_GLASS) {
-                        const float a = 1.5f - 1.0f, b = 1.5f + 1.0f, c = 1.0f / 1.5f, dd = 1.5f / 1.0f;
-                        const float e = (a * a) / (b * b);
-                        const bool going_in = s.nx * wx + s.ny * wy + s.nz * wz > 0.0f;
-                        const float nnt = going_in ? c : dd;
-                        const float dw = wx * dx + wy * dy + wz * dz;
-                        const float tir = 1.0f - nnt * nnt * (1.0f - dw * dw);
-                        if (tir < 0.0f) {
-                            ox = s.px + wx * 0.01f; oy = s.py + wy * 0.01f; oz = s.pz + wz * 0.01f;
-                            dx = rx; dy = ry; dz = rz;
-                        } else {
-                            const float st = sqrtf(tir);
-                            const float scl = going_in ? dw * nnt + st : -(dw * nnt + st);
-                            const float t0x = dx * nnt - s.nx * scl, t0y = dy * nnt - s.ny * scl, t0z = dz * nnt - s.nz * scl;
-                            const float tr = rsqrt_j(t0x * t0x + t0y * t0y + t0z * t0z);
-                            const float tdx = t0x * tr, tdy = t0y * tr, tdz = t0z * tr;
-                            const float a1 = going_in ? -dw : tdx * s.nx + tdy * s.ny + tdz * s.nz;
-                            const float a2 = 1.0f - a1;
-                            const float refl = e + (1.0f - e) * a2 * a2 * a2 * a2 * a2;
-                            const float trans = 1.0f - refl;
-                            const float pr = 0.25f + 0.5f * refl;
-                            const float rp = refl / pr, tp = trans / (1.0f - pr);
-                            const bool is_refl = rng.next() < pr;
-                            const float m = is_refl ? rp : tp;
-                            T.x *= m; T.y *= m; T.z *= m;
-                            const float eps = is_refl ? 0.01f : 0.000001f;
-                            ox = s.px + wx * eps; oy = s.py + wy * eps; oz = s.pz + wz * eps;
-                            dx = is_refl ? rx : tdx; dy = is_refl ? ry : tdy; dz = is_refl ? rz : tdz;
-                        }
-                    } else if (material == DFPT_MATERIAL_REFLECTION) {
-                        ox = s.px + s.nx * 0.000001f; oy = s.py + s.ny * 0.000001f; oz = s.pz + s.nz * 0.000001f;
-                        dx = rx; dy = ry; dz = rz;
-                        T.x *= ar; T.y *= ag; T.z *= ab;
-                    }
+                    const Scatter sct = scatter(s, material, wx, wy, wz, o4, d4, dp2, ar, ag, ab, exponent, rng, T);
                     emit_next = true;
-                    no = make_float4(ox, oy, oz, __int_as_float(path));
-                    nd = make_float4(dx, dy, dz, sid_bits);
+                    no = make_float4(sct.o.x, sct.o.y, sct.o.z, __int_as_float(path));
+                    nd = make_float4(sct.d.x, sct.d.y, sct.d.z, sid_bits);
                 }
                 B.throughput[path] = T;
                 B.radiance[path] = L;
@@ -811,6 +849,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevPa
             atomicAdd(L, c.x);
             atomicAdd(L + 1, c.y);
             atomicAdd(L + 2, c.z);
+            if (!BATCH && P.diff) atomicOr(B.vis + path, 1 << __float_as_int(c.w));
         }
         warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
     }
@@ -1140,6 +1179,13 @@ __global__ void __launch_bounds__(256) k_film(const DevParams* __restrict__ Pp, 
         float4 sum = B.film_sum[i], comp = B.film_comp[i];
         int cnt = B.film_n[i];
         film_add(B.radiance[i], B.pixel_flags[i], clear, sum, comp, cnt);
+        if (P.diff) {
+            const int k = pass - P.diff_pass0;
+            if (k >= 0 && k < P.diff_spp) {
+                B.diff_L[(size_t)k * n + i] = B.radiance[i];
+                B.diff_vis[(size_t)k * n + i] = (B.pixel_flags[i] & 1) ? 0 : B.vis[i];
+            }
+        }
         B.film_sum[i] = sum; B.film_comp[i] = comp; B.film_n[i] = cnt;
         reinterpret_cast<uchar4*>(B.bgra)[i] = tone_map_bgra(P, sum, cnt, B.primitive_offsets[i]);
     }
@@ -1263,6 +1309,10 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
     if (i < 36) g_grad3[i] = grad36[i];
 }
 
+#ifdef DFPT_EXTENDED_KERNELS
+#include "dfpt_adjoint.cuh"
+#endif
+
 // ---------------------------------------------------------------------------------------------
 // Host-side launchers (the kernel set of this translation unit).
 
@@ -1285,7 +1335,7 @@ struct TraceCfg {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<false, false, V, BLOCK, MINB>, BLOCK, 0);
         return sms * (b > 0 ? b : 1);
     }
-#ifdef DFPT_BATCH_KERNELS
+#ifdef DFPT_EXTENDED_KERNELS
     // Batch traversal: per-lane walks only (a warp may hold rays of several scenes).
     static constexpr int BV = V == 2 ? 1 : V;
     static void b_closest(const LaunchCtx& c, int bounce) {
@@ -1336,7 +1386,7 @@ static int trace_grid(int config, int sms) {
 static void launch_camera(const LaunchCtx& c) { k_camera<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}); }
 static void launch_shade(const LaunchCtx& c, int bounce) { k_shade<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce); }
 
-#ifdef DFPT_BATCH_KERNELS
+#ifdef DFPT_EXTENDED_KERNELS
 #define BATCH_DISPATCH(fn)                                                                     \
     static void launch_b_##fn(const LaunchCtx& c, int bounce) {                                \
         switch (c.trace_config) {                                                              \
@@ -1360,6 +1410,20 @@ static void launch_b_wave(const LaunchCtx& c, int) { k_bwave<<<1, 32, 0, c.strea
 static void launch_b_film(const LaunchCtx& c, int) { k_bfilm<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_resolve(const LaunchCtx& c, int) { k_bresolve<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_end(const LaunchCtx& c, int) { k_bend_wave<<<1, 32, 0, c.stream>>>(*c.batch); }
+
+// Path-replay adjoint. Per-primitive partials live in shared memory when they fit in 44 KB.
+static void launch_shade_adj(const LaunchCtx& c, int bounce) {
+    const size_t bytes = (size_t)c.scene->primitive_count * DFPT_DIFF_PER_PRIM * sizeof(float);
+    if (bytes <= 44 * 1024) k_shade_adj<true><<<c.grid, 256, bytes, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+    else k_shade_adj<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+}
+static void launch_final_adj(const LaunchCtx& c, int bounce) {
+    // Per-lane walks (variant 1 prefetches); one block per gradient row.
+    k_final_adj<1><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+}
+static void launch_diff_reduce(const LaunchCtx& c, const double* rows, int n_rows, int row_len, double* out) {
+    k_diff_reduce<<<(row_len + 255) / 256, 256, 0, c.stream>>>(rows, n_rows, row_len, out);
+}
 #endif
 static void launch_simple(const LaunchCtx& c) { k_simple<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_wireframe(const LaunchCtx& c) { k_wireframe<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
@@ -1397,7 +1461,7 @@ KernelSet kernel_set() {
     k.occupancy = occupancy;
     k.trace_grid = trace_grid;
     k.trace_configs = 7;
-#ifdef DFPT_BATCH_KERNELS
+#ifdef DFPT_EXTENDED_KERNELS
     k.b_camera = launch_b_camera;
     k.b_trace_closest = launch_b_closest;
     k.b_shade = launch_b_shade;
@@ -1407,6 +1471,9 @@ KernelSet kernel_set() {
     k.b_film = launch_b_film;
     k.b_resolve = launch_b_resolve;
     k.b_end = launch_b_end;
+    k.shade_adj = launch_shade_adj;
+    k.final_adj = launch_final_adj;
+    k.diff_reduce = launch_diff_reduce;
 #endif
     return k;
 }

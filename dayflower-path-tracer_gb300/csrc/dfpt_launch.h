@@ -41,6 +41,10 @@ struct KernelSet {
     void (*b_film)(const LaunchCtx&, int) = nullptr;
     void (*b_resolve)(const LaunchCtx&, int) = nullptr;
     void (*b_end)(const LaunchCtx&, int) = nullptr;
+    // Path-replay adjoint (the fast kernel set only).
+    void (*shade_adj)(const LaunchCtx&, int bounce) = nullptr;
+    void (*final_adj)(const LaunchCtx&, int bounce) = nullptr;
+    void (*diff_reduce)(const LaunchCtx&, const double* rows, int n_rows, int row_len, double* out) = nullptr;
 };
 
 namespace dfpt_fast { KernelSet kernel_set(); }

@@ -89,6 +89,16 @@ class Params(C.Structure):
     ]
 
 
+class DiffParams(C.Structure):
+    _fields_ = [
+        ("albedo", f32p),
+        ("emission", f32p),
+        ("phong_exponent", f32p),
+        ("turbidity", C.c_float),
+        ("sun_direction", C.c_float * 3),
+    ]
+
+
 # Symbol -> (restype, argtypes). Every entry point of include/dfpt.h is listed here.
 SIGNATURES = {
     "dfpt_params_default": (None, [C.POINTER(Params)]),
@@ -130,6 +140,9 @@ SIGNATURES = {
     "dfpt_compiled_destroy": (C.c_int, [C.c_void_p]),
     "dfpt_compiled_describe": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
     "dfpt_sky_set": (C.c_int, [C.POINTER(Sky), f32p, C.c_float]),
+    "dfpt_diff_forward": (C.c_int, [C.c_void_p, C.POINTER(DiffParams), C.c_int32, f32p]),
+    "dfpt_diff_backward": (C.c_int, [C.c_void_p, f32p, f64p, f64p, f64p, f64p]),
+    "dfpt_diff_end": (C.c_int, [C.c_void_p]),
     "dfpt_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "dfpt_batch_destroy": (C.c_int, [C.c_void_p]),
     "dfpt_batch_add": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(Sky), C.POINTER(Params), C.c_int32, C.c_int32,

@@ -365,3 +365,44 @@ def batch_workload(seed: int = 5, count: int = 64, tri_range=(1000, 500000), res
         out.append(dict(scene=cs, sky=sky, params=params, width=int(res[i]), height=int(res[i]), spp=int(spp[i]),
                         triangles=int(cs.triangles.size // 12)))
     return out
+
+
+def inverse_scene(seed: int = 6, width: int = 512, height: int = 512, count: int = 256, phong_every: int = 4,
+                  plane: bool = True):
+    """The inverse-rendering workload: `count` spheres (radius 0.4) on a grid over a Lambertian
+    plane under a Perez sky, every `phong_every`-th sphere Phong, the rest Lambertian. Sphere
+    albedo textures are white, so the per-primitive albedo parameter is the albedo. Returns
+    (scene, params, (width, height), truth, start): truth/start hold per-primitive albedo (P, 3),
+    Phong exponents (P,), turbidity and sun direction - ground truth albedo U(0.1, 0.9)^3 and
+    turbidity 3, start albedo 0.5 and turbidity 2 (the plane, primitive 0, keeps multiplier 1)."""
+    rng = np.random.default_rng(seed)
+    b = sc.SceneBuilder()
+    black = b.constant(0, 0, 0)
+    white = b.constant(1, 1, 1)
+    if plane:
+        b.primitive(b.plane((0, 0, 0), (0, 0, 1), (1, 0, 0)), b.surface(sc.LAMBERTIAN, b.constant(0.5, 0.5, 0.5), black, black))
+    sphere = b.sphere((0, 0, 0), 0.4)
+    side = int(np.ceil(np.sqrt(count)))
+    lam = b.surface(sc.LAMBERTIAN, white, black, black)
+    pho = b.surface(sc.PHONG, white, black, black)
+    spacing = 1.0 if count > 16 else 1.6
+    for k in range(count):
+        x = (k % side - (side - 1) / 2) * spacing
+        z = (k // side - (side - 1) / 2) * spacing
+        b.primitive(sphere, pho if phong_every and k % phong_every == phong_every - 1 else lam, position=(x, 0.4, z))
+    dist = 1.1 * side * spacing
+    b.camera((0, 0.65 * dist, dist), (0, 0, 0), 60.0, (width, height))
+    params = dict(renderer_type=2, pt_ray_depth_maximum=5, pt_ray_depth_russian_roulette=3, tone_mapper_type=2,
+                  tone_mapper_exposure=1.0)
+    n = count + (1 if plane else 0)
+    off = 1 if plane else 0
+    truth_albedo = np.ones((n, 3), np.float32)
+    truth_albedo[off:] = rng.uniform(0.1, 0.9, (count, 3))
+    exponent = np.full(n, 50.0, np.float32)
+    exponent[off:] = rng.uniform(10.0, 200.0, count)
+    sun = tuple(float(v) for v in SUN_45)
+    truth = dict(albedo=truth_albedo, phong_exponent=exponent, turbidity=3.0, sun_direction=sun)
+    start_albedo = np.ones((n, 3), np.float32)
+    start_albedo[off:] = 0.5
+    start = dict(albedo=start_albedo, phong_exponent=exponent.copy(), turbidity=2.0, sun_direction=sun)
+    return b.compile("inverse_scene"), params, (width, height), truth, start

@@ -276,6 +276,34 @@ int dfpt_compiled_describe(const dfpt_compiled* compiled, dfpt_scene_desc* desc)
 int dfpt_sky_set(dfpt_sky* sky, const float* sun_direction_world3, float turbidity);
 
 /* ---------------------------------------------------------------------------------------------
+ * Differentiable rendering. No counterpart in the reference (its kernel only renders). A forward /
+ * backward pair over one handle: dfpt_diff_forward renders `spp` path-traced samples per pixel
+ * with per-primitive parameters and a sky given by (turbidity, sun direction) - Sky.set
+ * (Sky.java:295-333) - and keeps per sample only the path radiance and its sun-visibility bits;
+ * dfpt_diff_backward replays every path from its RNG key (path-replay backpropagation) and
+ * returns d(loss)/d(parameters) for a given d(loss)/d(image). Needs the path tracer and the
+ * counter-based RNG. Gradients hold Russian roulette's survival probability and the sun shadow
+ * rays' visibility fixed (no derivative of shadow boundaries); the Phong exponent's gradient is the
+ * score of the lobe density (n+1) cos^n the sample was drawn from. */
+typedef struct dfpt_diff_params {
+    const float* albedo;         /* 3 per primitive: multiplies the albedo texture color (NULL: 1) */
+    const float* emission;       /* 3 per primitive: added to the emission texture color (NULL: 0) */
+    const float* phong_exponent; /* 1 per primitive, > -1 (NULL: 50, the reference's constant) */
+    float turbidity;             /* Perez turbidity, > 0 */
+    float sun_direction[3];      /* world-space sun direction (normalised inside, as Sky.set) */
+} dfpt_diff_params;
+
+/* Clears the film, renders spp passes with the parameters (the handle keeps using them until
+ * dfpt_diff_end) and, if image_rgb != NULL, writes the film average (3 floats per pixel). */
+int dfpt_diff_forward(dfpt_handle* handle, const dfpt_diff_params* params, int32_t spp, float* image_rgb);
+/* dloss_dimage: 3 floats per pixel. Outputs (each may be NULL): grad_albedo and grad_emission
+ * 3 per primitive, grad_phong_exponent 1 per primitive, grad_sky 4 = d/d(turbidity, sun x, y, z). */
+int dfpt_diff_backward(dfpt_handle* handle, const float* dloss_dimage, double* grad_albedo, double* grad_emission,
+                       double* grad_phong_exponent, double* grad_sky);
+/* Leaves differentiable mode: shading uses the textures alone again; the records are freed. */
+int dfpt_diff_end(dfpt_handle* handle);
+
+/* ---------------------------------------------------------------------------------------------
  * Batched rendering. No counterpart in the reference, which renders one scene per
  * GPURendererKernel (one AbstractRendererKernel per DayflowerApplication window). A batch holds
  * many compiled scenes resident at once, each with its own resolution, samples per pixel, camera,

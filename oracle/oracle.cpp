@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -124,10 +125,42 @@ template <typename R> struct Isect {
 
 struct Counters { uint64_t closest = 0, any = 0, nodes = 0, tris = 0; };
 
+// Differentiable-rendering inputs (per primitive: albedo multiplier, added emission, Phong
+// exponent) and the record of one path, for the FP64 host adjoint.
+struct DiffIn {
+    const double* albedo;    // 3 per primitive
+    const double* emission;  // 3 per primitive
+    const double* exponent;  // 1 per primitive
+};
+struct TapeVertex {
+    int prim, material;
+    double T[3];              // throughput arriving at the vertex
+    double tex[3], a0[3];     // albedo texture color, albedo used (before Russian roulette)
+    bool sun, sun_vis;        // a sun sample was drawn / its shadow ray was unoccluded
+    double sun_u, sun_v, sun_dot, p[3], w[3];
+    bool albedo_mult;         // the vertex multiplied the throughput by the albedo
+    double phong_ct, exponent;
+    bool alive;
+};
+struct TapeEscape {
+    int after;                // number of vertices before the escape
+    double T[3], d[3];
+};
+struct Tape {
+    std::vector<TapeVertex> v;
+    std::vector<TapeEscape> esc;
+    std::vector<std::pair<int, std::array<double, 3>>> contrib;  // (vertex index or depth, rgb)
+    void clear() { v.clear(); esc.clear(); contrib.clear(); }
+};
+
 template <typename R> struct Kernel {
     const Scene& S;
     Random rng;
     Counters cnt;
+    const DiffIn* diff = nullptr;  // per-primitive parameters (FP64 host adjoint)
+    Tape* tape = nullptr;          // path record (FP64 host adjoint)
+    R sun_u = 0, sun_v = 0, sun_dot = 0;
+    bool sun_drawn = false, sun_seen = false;
     R ray[6];
     R color[3];  // colorTemporarySamples
     Isect<R> is;
@@ -717,6 +750,8 @@ template <typename R> struct Kernel {
             const R tX = (R)k->sun_origin[0] - pX, tY = (R)k->sun_origin[1] - pY, tZ = (R)k->sun_origin[2] - pZ;
             const R tl2 = tX * tX + tY * tY + tZ * tZ;
             const R u = nextf(), v = nextf();
+            sun_drawn = true;
+            sun_u = u; sun_v = v;
             const R sin2 = rad2 / tl2;
             const R cosMax = jsqrt(jmax((R)0, (R)1 - sin2));
             const R cosT = u * (cosMax - (R)1) + (R)1;
@@ -735,8 +770,10 @@ template <typename R> struct Kernel {
             const R dX = rX * rl, dY = rY * rl, dZ = rZ * rl;
             const R dp0 = dX * sWX + dY * sWY + dZ * sWZ;
             const R dp1 = dX * nX + dY * nY + dZ * nZ;
+            sun_dot = dp1;
             if (dp0 > (R)0 && dp1 > (R)0) {
                 const R t = intersect(pX, pY, pZ, dX, dY, dZ, true);
+                sun_seen = t >= K<R>::INF() - (R)0.0001f;
                 if (t >= K<R>::INF() - (R)0.0001f) {
                     r = aR * (R)1 * dp1 * K<R>::INV_PI();
                     g = aG * (R)1 * dp1 * K<R>::INV_PI();
@@ -762,6 +799,11 @@ template <typename R> struct Kernel {
             if (distance == K<R>::INF() || po == -1) {
                 sky_color(dX, dY, dZ);
                 pR += mR * color[0] * K<R>::INV_PI(); pG += mG * color[1] * K<R>::INV_PI(); pB += mB * color[2] * K<R>::INV_PI();
+                if (tape) {
+                    tape->esc.push_back({depth, {(double)mR, (double)mG, (double)mB}, {(double)dX, (double)dY, (double)dZ}});
+                    tape->contrib.push_back({depth, {(double)(mR * color[0] * K<R>::INV_PI()), (double)(mG * color[1] * K<R>::INV_PI()),
+                                                     (double)(mB * color[2] * K<R>::INV_PI())}});
+                }
                 out[0] = pR; out[1] = pG; out[2] = pB;
                 return;
             }
@@ -774,14 +816,42 @@ template <typename R> struct Kernel {
             const int aRGB = texture(jint(S.d->surfaces[so + 1]));
             R aR = cr(aRGB), aG = cg(aRGB), aB = cb(aRGB);
             const int eRGB = texture(jint(S.d->surfaces[so + 2]));
-            const R eR = cr(eRGB), eG = cg(eRGB), eB = cb(eRGB);
+            R eR = cr(eRGB), eG = cg(eRGB), eB = cb(eRGB);
             const int material = jint(S.d->surfaces[so]);
+            const R tR = aR, tG = aG, tB = aB;
+            R exponent = (R)50;
+            const int prim = po / 3;
+            if (diff) {
+                aR *= (R)diff->albedo[3 * prim]; aG *= (R)diff->albedo[3 * prim + 1]; aB *= (R)diff->albedo[3 * prim + 2];
+                eR += (R)diff->emission[3 * prim]; eG += (R)diff->emission[3 * prim + 1]; eB += (R)diff->emission[3 * prim + 2];
+                exponent = (R)diff->exponent[prim];
+            }
+            sun_drawn = sun_seen = false;
             if (material == DFPT_MATERIAL_CLEAR_COAT || material == DFPT_MATERIAL_LAMBERTIAN || material == DFPT_MATERIAL_PHONG) {
                 sun_color(sunA, sX, sY, sZ, wX, wY, wZ, aR, aG, aB);
             } else {
                 color[0] = color[1] = color[2] = 0;
             }
             pR += mR * (eR + color[0]); pG += mG * (eG + color[1]); pB += mB * (eB + color[2]);
+            TapeVertex* tv = nullptr;
+            if (tape) {
+                TapeVertex x{};
+                x.prim = prim;
+                x.material = material;
+                x.T[0] = (double)mR; x.T[1] = (double)mG; x.T[2] = (double)mB;
+                x.tex[0] = (double)tR; x.tex[1] = (double)tG; x.tex[2] = (double)tB;
+                x.a0[0] = (double)aR; x.a0[1] = (double)aG; x.a0[2] = (double)aB;
+                x.sun = sun_drawn;
+                x.sun_vis = sun_drawn && sun_seen && sun_dot > (R)0;
+                x.sun_u = (double)sun_u; x.sun_v = (double)sun_v; x.sun_dot = (double)sun_dot;
+                x.p[0] = (double)sX; x.p[1] = (double)sY; x.p[2] = (double)sZ;
+                x.w[0] = (double)wX; x.w[1] = (double)wY; x.w[2] = (double)wZ;
+                x.exponent = (double)exponent;
+                x.alive = true;
+                tape->v.push_back(x);
+                tv = &tape->v.back();
+                tape->contrib.push_back({depth, {(double)(mR * (eR + color[0])), (double)(mG * (eG + color[1])), (double)(mB * (eB + color[2]))}});
+            }
             depth++;
             if (depth >= depthRR) {
                 const R pdf = jmax(aR, jmax(aG, aB));
@@ -792,6 +862,7 @@ template <typename R> struct Kernel {
                         sky_color(dX, dY, dZ);
                         pR += mR * color[0] * K<R>::INV_PI(); pG += mG * color[1] * K<R>::INV_PI(); pB += mB * color[2] * K<R>::INV_PI();
                     }
+                    if (tv) tv->alive = false;
                     out[0] = pR; out[1] = pG; out[2] = pB;
                     return;
                 }
@@ -822,16 +893,19 @@ template <typename R> struct Kernel {
                         cosine(wX, wY, wZ, dX, dY, dZ);
                         oX = sX + wX * (R)0.01f; oY = sY + wY * (R)0.01f; oZ = sZ + wZ * (R)0.01f;
                         mR *= aR; mG *= aG; mB *= aB;
+                if (tv) tv->albedo_mult = true;
                     }
                 }
             } else if (material == DFPT_MATERIAL_LAMBERTIAN) {
                 cosine(wX, wY, wZ, dX, dY, dZ);
                 oX = sX + wX * (R)0.01f; oY = sY + wY * (R)0.01f; oZ = sZ + wZ * (R)0.01f;
                 mR *= aR; mG *= aG; mB *= aB;
+                if (tv) tv->albedo_mult = true;
             } else if (material == DFPT_MATERIAL_PHONG) {
                 const R u = nextf(), v = nextf();
                 const R phi = K<R>::TWO_PI() * u;
-                const R cosT = jpow((R)1 - v, (R)1 / ((R)50 + (R)1));
+                const R cosT = jpow((R)1 - v, (R)1 / (exponent + (R)1));
+                if (tv) tv->phong_ct = (double)cosT;
                 const R sinT = jsqrt(jmax((R)0, (R)1 - cosT * cosT));
                 const R x = jcos(phi) * sinT, y = jsin(phi) * sinT, z = cosT;
                 const R rl = jrsqrt(rX * rX + rY * rY + rZ * rZ);
@@ -846,6 +920,7 @@ template <typename R> struct Kernel {
                 oX = sX + rnX * (R)0.01f; oY = sY + rnY * (R)0.01f; oZ = sZ + rnZ * (R)0.01f;
                 dX = qX * ql; dY = qY * ql; dZ = qZ * ql;
                 mR *= aR; mG *= aG; mB *= aB;
+                if (tv) tv->albedo_mult = true;
             } else if (material == DFPT_MATERIAL_GLASS) {
                 const R a = (R)1.5f - (R)1, b = (R)1.5f + (R)1, c = (R)1 / (R)1.5f, dd = (R)1.5f / (R)1, e = (a * a) / (b * b);
                 const bool in = nX * wX + nY * wY + nZ * wZ > (R)0;
@@ -878,12 +953,18 @@ template <typename R> struct Kernel {
                 oX = sX + nX * (R)0.000001f; oY = sY + nY * (R)0.000001f; oZ = sZ + nZ * (R)0.000001f;
                 dX = rX; dY = rY; dZ = rZ;
                 mR *= aR; mG *= aG; mB *= aB;
+                if (tv) tv->albedo_mult = true;
             }
         } while (depth < depthMax);
         const bool hit = intersect(oX, oY, oZ, dX, dY, dZ, true) < K<R>::INF();
         if (!hit) {
             sky_color(dX, dY, dZ);
             pR += mR * color[0] * K<R>::INV_PI(); pG += mG * color[1] * K<R>::INV_PI(); pB += mB * color[2] * K<R>::INV_PI();
+            if (tape) {
+                tape->esc.push_back({depth, {(double)mR, (double)mG, (double)mB}, {(double)dX, (double)dY, (double)dZ}});
+                tape->contrib.push_back({depth, {(double)(mR * color[0] * K<R>::INV_PI()), (double)(mG * color[1] * K<R>::INV_PI()),
+                                                 (double)(mB * color[2] * K<R>::INV_PI())}});
+            }
         }
         out[0] = pR; out[1] = pG; out[2] = pB;
     }
@@ -1210,6 +1291,206 @@ int render(const Scene& S, int pass_begin, int passes, int threads, int row_begi
     return 0;
 }
 
+// ---- FP64 host adjoint -------------------------------------------------------------------------
+// Dual numbers over (turbidity, sun x, sun y, sun z) carry the sky and sun terms' derivatives
+// straight from Sky.set's inputs (Sky.java:295-333) through the Perez model and the sun sample.
+
+struct Dual {
+    double v, d[4];
+};
+Dual dc(double v) { return Dual{v, {0, 0, 0, 0}}; }
+Dual operator+(Dual a, Dual b) { Dual r{a.v + b.v, {}}; for (int j = 0; j < 4; ++j) r.d[j] = a.d[j] + b.d[j]; return r; }
+Dual operator-(Dual a, Dual b) { Dual r{a.v - b.v, {}}; for (int j = 0; j < 4; ++j) r.d[j] = a.d[j] - b.d[j]; return r; }
+Dual operator-(Dual a) { Dual r{-a.v, {}}; for (int j = 0; j < 4; ++j) r.d[j] = -a.d[j]; return r; }
+Dual operator*(Dual a, Dual b) { Dual r{a.v * b.v, {}}; for (int j = 0; j < 4; ++j) r.d[j] = a.d[j] * b.v + a.v * b.d[j]; return r; }
+Dual operator/(Dual a, Dual b) { Dual r{a.v / b.v, {}}; for (int j = 0; j < 4; ++j) r.d[j] = (a.d[j] * b.v - a.v * b.d[j]) / (b.v * b.v); return r; }
+Dual operator+(Dual a, double b) { return a + dc(b); }
+Dual operator+(double a, Dual b) { return dc(a) + b; }
+Dual operator-(Dual a, double b) { return a - dc(b); }
+Dual operator-(double a, Dual b) { return dc(a) - b; }
+Dual operator*(Dual a, double b) { return a * dc(b); }
+Dual operator*(double a, Dual b) { return dc(a) * b; }
+Dual operator/(double a, Dual b) { return dc(a) / b; }
+Dual operator/(Dual a, double b) { return a / dc(b); }
+Dual fn(Dual a, double v, double slope) { Dual r{v, {}}; for (int j = 0; j < 4; ++j) r.d[j] = a.d[j] * slope; return r; }
+Dual dexp(Dual a) { const double e = std::exp(a.v); return fn(a, e, e); }
+Dual dsqrt(Dual a) { const double s = std::sqrt(std::max(a.v, 0.0)); return fn(a, s, s > 0 ? 0.5 / s : 0.0); }
+Dual dtan(Dual a) { const double t = std::tan(a.v); return fn(a, t, 1.0 + t * t); }
+Dual dacos(Dual a) {
+    const double c = std::max(-1.0, std::min(1.0, a.v));
+    const double s = std::sqrt(std::max(0.0, 1.0 - c * c));
+    return fn(a, std::acos(c), (a.v > -1.0 && a.v < 1.0 && s > 1e-12) ? -1.0 / s : 0.0);
+}
+Dual dclamp(Dual a, double lo, double hi) { return a.v < lo ? dc(lo) : a.v > hi ? dc(hi) : a; }
+
+struct SunDual {
+    Dual w[3];       // world sun direction (normalised)
+    Dual sky[3];     // sky-frame sun direction (u = X, v = Z, w = Y)
+    Dual theta, zl, zx, zy, L[5], X[5], Y[5];
+};
+
+SunDual sky_set_dual(double turbidity, const double* s) {
+    SunDual r;
+    Dual t{turbidity, {1, 0, 0, 0}};
+    Dual sx{s[0], {0, 1, 0, 0}}, sy{s[1], {0, 0, 1, 0}}, sz{s[2], {0, 0, 0, 1}};
+    const Dual len = dsqrt(sx * sx + sy * sy + sz * sz);
+    r.w[0] = sx / len; r.w[1] = sy / len; r.w[2] = sz / len;
+    const Dual a = r.w[0], b = r.w[2], c = r.w[1];
+    const Dual l2 = dsqrt(a * a + b * b + c * c);
+    r.sky[0] = a / l2; r.sky[1] = b / l2; r.sky[2] = c / l2;
+    r.theta = dacos(dclamp(r.sky[2], -1.0, 1.0));
+    const Dual th = r.theta, th2 = th * th, th3 = th2 * th, t2 = t * t;
+    const double pi_f = (double)3.14159274101257324219f;
+    const Dual chi = (4.0 / 9.0 - t * (1.0 / 120.0)) * (pi_f - 2.0 * th);
+    r.zl = ((4.0453 * t - 4.9710) * dtan(chi) - 0.2155 * t + 2.4192) * 1000.0;
+    r.zx = (0.00165 * th3 - 0.00374 * th2 + 0.00208 * th) * t2 + (-0.02902 * th3 + 0.06377 * th2 - 0.03202 * th + 0.00394) * t +
+           (0.11693 * th3 - 0.21196 * th2 + 0.06052 * th + 0.25885);
+    r.zy = (0.00275 * th3 - 0.00610 * th2 + 0.00316 * th) * t2 + (-0.04212 * th3 + 0.08970 * th2 - 0.04153 * th + 0.00515) * t +
+           (0.15346 * th3 - 0.26756 * th2 + 0.06669 * th + 0.26688);
+    const double Lc[5][2] = {{0.17872, -1.46303}, {-0.35540, 0.42749}, {-0.02266, 5.32505}, {0.12064, -2.57705}, {-0.06696, 0.37027}};
+    const double Xc[5][2] = {{-0.01925, -0.25922}, {-0.06651, 0.00081}, {-0.00041, 0.21247}, {-0.06409, -0.89887}, {-0.00325, 0.04517}};
+    const double Yc[5][2] = {{-0.01669, -0.26078}, {-0.09495, 0.00921}, {-0.00792, 0.21023}, {-0.04405, -1.65369}, {-0.01092, 0.05291}};
+    for (int i = 0; i < 5; ++i) {
+        r.L[i] = Lc[i][0] * t + Lc[i][1];
+        r.X[i] = Xc[i][0] * t + Xc[i][1];
+        r.Y[i] = Yc[i][0] * t + Yc[i][1];
+    }
+    return r;
+}
+
+// The FP64 sky color of a direction (the R = double sky_color above) as duals.
+void sky_color_dual(const SunDual& k, bool active, double dX, double dY, double dZ, Dual out[3]) {
+    double d0X = dX, d0Y = dZ, d0Z = dY;  // basis u = X, v = Z, w = Y
+    out[0] = out[1] = out[2] = dc((double)0.01f);
+    if (!(d0Z >= 0.0 && active)) return;
+    d0Z = std::max(d0Z, (double)0.001f);
+    const double lr = 1.0 / std::sqrt(d0X * d0X + d0Y * d0Y + d0Z * d0Z);
+    const double d1X = d0X * lr, d1Y = d0Y * lr, d1Z = d0Z * lr;
+    const Dual dp = d1X * k.sky[0] + d1Y * k.sky[1] + d1Z * k.sky[2];
+    const double theta1 = std::acos(std::max(std::min(d1Z, 1.0), -1.0));
+    const double cos1 = std::cos(theta1), cos1r = 1.0 / (cos1 + 0.01);
+    const Dual cos0 = fn(k.theta, std::cos(k.theta.v), -std::sin(k.theta.v));
+    const Dual gamma = dacos(dp);
+    const Dual cosg = dclamp(dp, -1.0, 1.0);
+    const Dual* L = k.L;
+    const Dual* X = k.X;
+    const Dual* Y = k.Y;
+    const Dual den_l = (1.0 + L[0] * dexp(L[1])) * (1.0 + L[2] * dexp(L[3] * k.theta) + L[4] * cos0 * cos0);
+    const Dual num_l = (1.0 + L[0] * dexp(L[1] * cos1r)) * (1.0 + L[2] * dexp(L[3] * gamma) + L[4] * cosg * cosg);
+    const Dual rel = k.zl * num_l / den_l * 1.0e-4;
+    const Dual den_x = (1.0 + X[0] * dexp(X[1])) * (1.0 + X[2] * dexp(X[3] * theta1) + X[4] * cos0 * cos0);
+    const Dual num_x = (1.0 + X[0] * dexp(X[1] * cos1r)) * (1.0 + X[2] * dexp(X[3] * gamma) + X[4] * cosg * cosg);
+    const Dual x = k.zx * num_x / den_x;
+    const Dual den_y = (1.0 + Y[0] * dexp(Y[1])) * (1.0 + Y[2] * dexp(Y[3] * theta1) + Y[4] * cos0 * cos0);
+    const Dual num_y = (1.0 + Y[0] * dexp(Y[1] * cos1r)) * (1.0 + Y[2] * dexp(Y[3] * gamma) + Y[4] * cosg * cosg);
+    const Dual y = k.zy * num_y / den_y;
+    const Dual c0 = 1.0 / ((double)0.0241f + (double)0.2562f * x - (double)0.7341f * y);
+    const Dual c1 = ((double)-1.3515f - (double)1.7703f * x + (double)5.9114f * y) * c0;
+    const Dual c2 = ((double)0.03f - (double)31.4424f * x + (double)30.0717f * y) * c0;
+    const Dual cX = (double)10246.121f + c1 * (double)187.75537f + c2 * (double)213.14803f;
+    const Dual cY = (double)10676.695f + c1 * (double)192.59653f + c2 * (double)76.29494f;
+    const Dual cZ = (double)12372.504f + c1 * (double)3482.8765f + c2 * (double)-235.71611f;
+    const Dual R = cX * rel / cY, G = rel, B = cZ * rel / cY;
+    out[0] = (double)3.2410042f * R + (double)-1.5373994f * G + (double)-0.49861607f * B;
+    out[1] = (double)-0.9692241f * R + (double)1.8759298f * G + (double)0.041554242f * B;
+    out[2] = (double)0.05563942f * R + (double)-0.20401107f * G + (double)1.0571486f * B;
+    const int m = out[0].v <= out[1].v && out[0].v <= out[2].v ? 0 : out[1].v <= out[2].v ? 1 : 2;
+    if (out[m].v < 0.0) {
+        const Dual w = out[m];
+        for (int c = 0; c < 3; ++c) out[c] = out[c] - w;
+    }
+}
+
+// The sun sample's cosine (GRK:2238-2347, same draws) as a dual.
+Dual sun_cos_dual(const SunDual& k, const double* p, const double* n, double u, double v) {
+    const Dual tX = k.w[0] * 10000.0 - p[0], tY = k.w[1] * 10000.0 - p[1], tZ = k.w[2] * 10000.0 - p[2];
+    const Dual tl2 = tX * tX + tY * tY + tZ * tZ;
+    const Dual sin2 = (500.0 * 500.0) / tl2;
+    const Dual cosMax = dsqrt(1.0 - sin2);
+    const Dual cosT = u * (cosMax - 1.0) + 1.0;
+    const Dual sinT = dsqrt(1.0 - cosT * cosT);
+    const double phi = (double)(3.14159274101257324219f * 2.0f) * v;
+    const Dual x = std::cos(phi) * sinT, y = std::sin(phi) * sinT, z = cosT;
+    const Dual& sWX = k.w[0];
+    const Dual& sWY = k.w[1];
+    const Dual& sWZ = k.w[2];
+    const double aX = std::fabs(sWX.v), aY = std::fabs(sWY.v), aZ = std::fabs(sWZ.v);
+    const bool xmin = aX < aY && aX < aZ, ylt = aY < aZ;
+    const Dual vX = xmin ? dc(0) : ylt ? sWZ : sWY;
+    const Dual vY = xmin ? sWZ : ylt ? dc(0) : -sWX;
+    const Dual vZ = xmin ? -sWY : ylt ? -sWX : dc(0);
+    const Dual vl = 1.0 / dsqrt(vX * vX + vY * vY + vZ * vZ);
+    const Dual vnX = vX * vl, vnY = vY * vl, vnZ = vZ * vl;
+    const Dual unX = vnY * sWZ - vnZ * sWY, unY = vnZ * sWX - vnX * sWZ, unZ = vnX * sWY - vnY * sWX;
+    const Dual rX = unX * x + vnX * y + sWX * z, rY = unY * x + vnY * y + sWY * z, rZ = unZ * x + vnZ * y + sWZ * z;
+    const Dual rl = 1.0 / dsqrt(rX * rX + rY * rY + rZ * rZ);
+    return (rX * n[0] + rY * n[1] + rZ * n[2]) * rl;
+}
+
+// Renders with the parameters in FP64 and computes d(sum w * image)/d(parameters) by recording
+// each path's vertices and sweeping them (explicit sums of the later contributions).
+void diff_rows(const Scene& S, const DiffIn& din, const SunDual& sd, int pass_begin, int passes, int row_begin, int row_end,
+               const double* dldi, double* image, std::vector<double>& grad) {
+    Kernel<double> k(S);
+    k.diff = &din;
+    Tape tape;
+    k.tape = &tape;
+    const dfpt_params* p = S.p;
+    const int np = (int)(S.d->primitives_count / 3);
+    const double inv_pi = (double)(1.0f / 3.14159274101257324219f);
+    const bool sky_on = S.sky->is_sky_active == 1;
+    for (int y = row_begin; y < row_end; ++y) {
+        for (int x = 0; x < S.width; ++x) {
+            const int gid = y * S.width + x;
+            double acc[3] = {0, 0, 0};
+            const double w[3] = {dldi[3 * gid] / passes, dldi[3 * gid + 1] / passes, dldi[3 * gid + 2] / passes};
+            for (int pass = pass_begin; pass < pass_begin + passes; ++pass) {
+                k.rng.kind = p->rng_kind;
+                k.rng.pixel = (uint32_t)gid;
+                k.rng.pass = (uint32_t)pass;
+                k.rng.seed_lo = (uint32_t)p->seed;
+                k.rng.seed_hi = (uint32_t)(p->seed >> 32);
+                k.rng.draws = 0;
+                k.rng.lcg = 0;
+                tape.clear();
+                double c[3] = {0, 0, 0};
+                if (!k.create_primary_ray(gid)) continue;
+                int first_hit = -1;
+                k.path_trace(c, 0, &first_hit);
+                for (int ch = 0; ch < 3; ++ch) acc[ch] += c[ch];
+                // Reverse sweep over the record.
+                for (size_t vi = 0; vi < tape.v.size(); ++vi) {
+                    const TapeVertex& v = tape.v[vi];
+                    double later[3] = {0, 0, 0};
+                    for (auto& ct : tape.contrib)
+                        if (ct.first > (int)vi)
+                            for (int ch = 0; ch < 3; ++ch) later[ch] += ct.second[ch];
+                    double* g = grad.data() + (size_t)v.prim * 7;
+                    for (int ch = 0; ch < 3; ++ch) g[3 + ch] += w[ch] * v.T[ch];
+                    if (v.sun_vis) {
+                        for (int ch = 0; ch < 3; ++ch) g[ch] += w[ch] * v.T[ch] * v.tex[ch] * v.sun_dot * inv_pi;
+                        const Dual cd = sun_cos_dual(sd, v.p, v.w, v.sun_u, v.sun_v);
+                        const double cw = (w[0] * v.T[0] * v.a0[0] + w[1] * v.T[1] * v.a0[1] + w[2] * v.T[2] * v.a0[2]) * inv_pi;
+                        for (int j = 0; j < 4; ++j) grad[(size_t)np * 7 + j] += cw * cd.d[j];
+                    }
+                    if (v.alive && v.albedo_mult)
+                        for (int ch = 0; ch < 3; ++ch)
+                            if (v.a0[ch] != 0.0) g[ch] += w[ch] * later[ch] * v.tex[ch] / v.a0[ch];
+                    if (v.alive && v.material == DFPT_MATERIAL_PHONG && v.phong_ct > 0.0)
+                        g[6] += (w[0] * later[0] + w[1] * later[1] + w[2] * later[2]) * (1.0 / (v.exponent + 1.0) + std::log(v.phong_ct));
+                }
+                for (const TapeEscape& e : tape.esc) {
+                    Dual sc[3];
+                    sky_color_dual(sd, sky_on, e.d[0], e.d[1], e.d[2], sc);
+                    for (int j = 0; j < 4; ++j)
+                        grad[(size_t)np * 7 + j] += (w[0] * e.T[0] * sc[0].d[j] + w[1] * e.T[1] * sc[1].d[j] + w[2] * e.T[2] * sc[2].d[j]) * inv_pi;
+                }
+            }
+            for (int ch = 0; ch < 3; ++ch) image[3 * gid + ch] = acc[ch] / passes;
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1312,6 +1593,43 @@ int oracle_tonemap(const dfpt_params* params, const double* rgb3, int precision,
     else {
         const float f[3] = {(float)rgb3[0], (float)rgb3[1], (float)rgb3[2]};
         resolve<float>(params, f, -1, bgra4);
+    }
+    return 0;
+}
+
+// FP64 host adjoint: renders `passes` passes from `pass_begin` with per-primitive parameters
+// (albedo multiplier 3, added emission 3, Phong exponent 1 per primitive) under the sky `sky`
+// (which must equal Sky.set(sun, turbidity)), writes the mean image, and
+// grad[P * 7 + 4] = d(sum dldi * image)/d(albedo 3, emission 3, exponent; per primitive) and
+// d/d(turbidity, sun x, y, z).
+int oracle_diff(const dfpt_scene_desc* scene, const dfpt_sky* sky, const dfpt_params* params, int width, int height, int pass_begin,
+                int passes, int threads, const double* albedo, const double* emission, const double* exponent, double turbidity,
+                const double* sun3, const double* dldi, double* image, double* grad) {
+    if (!scene || !sky || !params || !albedo || !emission || !exponent || !sun3 || !dldi || !image || !grad) return -1;
+    if (width <= 0 || height <= 0 || passes < 1 || params->rng_kind != DFPT_RNG_COUNTER) return -1;
+    Scene S{scene, sky, params, width, height};
+    const DiffIn din{albedo, emission, exponent};
+    const SunDual sd = sky_set_dual(turbidity, sun3);
+    const int np = (int)(scene->primitives_count / 3);
+    const size_t glen = (size_t)np * 7 + 4;
+    if (threads < 1) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::vector<std::vector<double>> g((size_t)threads, std::vector<double>(glen, 0.0));
+    std::atomic<int> next_row(0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        pool.emplace_back([&, t]() {
+            for (;;) {
+                const int y = next_row.fetch_add(1);
+                if (y >= height) break;
+                diff_rows(S, din, sd, pass_begin, passes, y, y + 1, dldi, image, g[t]);
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+    for (size_t i = 0; i < glen; ++i) {
+        double v = 0;
+        for (int t = 0; t < threads; ++t) v += g[t][i];
+        grad[i] = v;
     }
     return 0;
 }

@@ -41,6 +41,8 @@ def load():
         _lib.oracle_random.argtypes = [C.c_int, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int, vp]
         _lib.oracle_tonemap.argtypes = [vp, vp, C.c_int, vp]
         _lib.oracle_philox.argtypes = [vp, vp, vp]
+        _lib.oracle_diff.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, vp]
+        _lib.oracle_diff.restype = C.c_int
     return _lib
 
 
@@ -129,3 +131,29 @@ def philox(counter, key):
     out = np.zeros(4, np.uint32)
     load().oracle_philox(_p(c), _p(k), _p(out))
     return [int(x) for x in out]
+
+
+def diff(scene, sky, params, width, height, albedo, emission, exponent, turbidity, sun_direction, dldi, pass_begin=0,
+         passes=1, threads=0):
+    """FP64 host adjoint. `sky` must be Sky.set(sun_direction, turbidity). Returns (image (H, W, 3),
+    grads dict) with grads of sum(dldi * image) per primitive (albedo, emission, phong_exponent)
+    and for turbidity and the sun direction."""
+    lib = load()
+    n_prim = scene.primitives.size // 3
+    a = np.ascontiguousarray(np.asarray(albedo, np.float64).reshape(-1))
+    e = np.ascontiguousarray(np.asarray(emission, np.float64).reshape(-1))
+    x = np.ascontiguousarray(np.asarray(exponent, np.float64).reshape(-1))
+    s = np.ascontiguousarray(np.asarray(sun_direction, np.float64))
+    w = np.ascontiguousarray(np.asarray(dldi, np.float64).reshape(-1))
+    assert a.size == 3 * n_prim and e.size == 3 * n_prim and x.size == n_prim and w.size == 3 * width * height
+    img = np.zeros(3 * width * height, np.float64)
+    g = np.zeros(7 * n_prim + 4, np.float64)
+    desc = scene.desc()
+    rc = lib.oracle_diff(C.addressof(desc), C.addressof(sky.raw), C.addressof(params), width, height, pass_begin, passes, threads,
+                         _p(a), _p(e), _p(x), float(turbidity), _p(s), _p(w), _p(img), _p(g))
+    if rc != 0:
+        raise RuntimeError(f"oracle_diff failed: {rc}")
+    gp = g[:7 * n_prim].reshape(n_prim, 7)
+    return img.reshape(height, width, 3), {"albedo": gp[:, 0:3].copy(), "emission": gp[:, 3:6].copy(),
+                                           "phong_exponent": gp[:, 6].copy(), "turbidity": float(g[7 * n_prim]),
+                                           "sun_direction": g[7 * n_prim + 1:].copy()}
