@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-scenes leg")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the inverse-rendering leg")
+    ap.add_argument("--adjoint-iters", type=int, default=10)
     return ap.parse_args()
 
 
@@ -283,6 +285,105 @@ def batch_leg(args, stream, torch, barrier, dist, world):
     }
 
 
+def adjoint_leg(args, torch, barrier, dist, world):
+    """Inverse rendering at 512x512, 16 spp per iteration: 256 spheres on a plane under a Perez sky;
+    the target is rendered at the true albedos U(0.1, 0.9)^3 and turbidity 3, the optimisation
+    starts at albedo 0.5 and turbidity 2. One iteration = dfpt_diff_forward (16 spp, image to host)
+    + FP64 L2 loss + dfpt_diff_backward (replay, gradients to host) + a normalised gradient step;
+    timed on the host clock around the whole iteration. t_fwd is the forward alone."""
+    import numpy as np
+    from dfpt import synthetic
+    from dfpt.diff import DiffRenderer
+    from dfpt.kernel import RendererKernel
+    from dfpt.scene import SkyState
+
+    cs, params, (w, h), truth, start = synthetic.inverse_scene(seed=6, width=512, height=512, count=256)
+    k = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), params)
+    k.update(w, h)
+    d = DiffRenderer(k)
+    spp = 16
+    target = d.forward(truth["albedo"], None, truth["phong_exponent"], truth["turbidity"], truth["sun_direction"], 256).astype(np.float64)
+    albedo = start["albedo"].astype(np.float64).copy()
+    turb = float(start["turbidity"])
+    expo, sun = start["phong_exponent"], start["sun_direction"]
+
+    def step(update=True):
+        img = d.forward(albedo, None, expo, turb, sun, spp).astype(np.float64)
+        r = img - target
+        loss = float(np.sum(r * r))
+        g = d.backward((2.0 * r).astype(np.float32))
+        return loss, g
+
+    for _ in range(2):  # warm-up: graphs, buffers
+        step()
+    barrier()
+    fw = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        d.forward(albedo, None, expo, turb, sun, spp)
+        fw.append(time.perf_counter() - t0)
+    t_fwd = min(fw)
+    losses, iters = [], []
+    for _ in range(args.adjoint_iters):
+        t0 = time.perf_counter()
+        loss, g = step()
+        ga = g["albedo"]
+        albedo[1:] -= 0.05 * ga[1:] / (np.abs(ga[1:]).max() + 1e-30)
+        np.clip(albedo, 0.01, 1.0, out=albedo)
+        turb = float(np.clip(turb - 0.1 * np.sign(g["turbidity"]), 1.5, 8.0))
+        iters.append(time.perf_counter() - t0)
+        losses.append(loss)
+    barrier()
+    t_adj = float(np.median(iters))
+    # Finite-difference spot checks at the start point (same seed on both sides: fresh handles), on
+    # the loss linearised at the start image (weights 2 r0: the L2 gradient at r0, and a central
+    # difference without the loss's own second-order term). Once as configured (Russian roulette
+    # from depth 3: its albedo-dependent decisions make the common-random-number difference
+    # noisy) and once with roulette off (the estimator is smooth in albedo and turbidity).
+    a0 = start["albedo"].astype(np.float64)
+    t0_ = float(start["turbidity"])
+    hstep = 1e-3
+
+    def fd_check(prm):
+        kk = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), prm)
+        kk.update(w, h)
+        dd = DiffRenderer(kk)
+        img0 = dd.forward(a0, None, expo, t0_, sun, spp).astype(np.float64)
+        wgt = 2.0 * (img0 - target)
+        g0 = dd.backward(wgt.astype(np.float32))
+        kk.dispose()
+
+        def lin(al, tb):
+            k2 = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), prm)
+            k2.update(w, h)
+            img = DiffRenderer(k2).forward(al, None, expo, tb, sun, spp).astype(np.float64)
+            k2.dispose()
+            return float(np.sum(wgt * img))
+
+        out = {}
+        for prim, c in ((1, 0), (17, 1), (100, 2), (200, 0)):
+            ap_, am_ = a0.copy(), a0.copy()
+            ap_[prim, c] += hstep
+            am_[prim, c] -= hstep
+            out[f"albedo[{prim},{c}]"] = {"adjoint": float(g0["albedo"][prim, c]), "fd": (lin(ap_, t0_) - lin(am_, t0_)) / (2 * hstep)}
+        out["turbidity"] = {"adjoint": float(g0["turbidity"]), "fd": (lin(a0, t0_ + hstep) - lin(a0, t0_ - hstep)) / (2 * hstep)}
+        for v in out.values():
+            v["rel_err"] = abs(v["adjoint"] - v["fd"]) / max(abs(v["fd"]), 1e-30)
+        return out
+
+    fd = fd_check(params)
+    fd_no_rr = fd_check(dict(params, pt_ray_depth_russian_roulette=params["pt_ray_depth_maximum"] + 1))
+    k.dispose()
+    return {
+        "metric": "adjoint iters/s", "value": world / t_adj, "unit": "iters/s", "t_adj_s": t_adj, "t_fwd_s": t_fwd,
+        "t_adj_over_t_fwd": t_adj / t_fwd, "spp_per_iter": spp, "resolution": [w, h], "primitives": int(cs.primitives.size // 3),
+        "loss_first": losses[0], "loss_last": losses[-1], "iters": len(losses),
+        "fd_check": fd, "fd_check_no_russian_roulette": fd_no_rr, "fd_step": hstep,
+        "workload": "inverse_scene seed 6: 256 spheres (every 4th Phong) on a plane, Perez sky; albedo U(0.1,0.9)^3, T 3 -> start 0.5, T 2",
+        "timing": "host clock around forward + FP64 loss + backward + update (C-ABI, host buffers)",
+    }
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -411,6 +512,9 @@ def main():
     batched = None
     if not args.no_batch:
         batched = batch_leg(args, stream, torch, barrier, dist, world)
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_leg(args, torch, barrier, dist, world)
 
     if rank != 0:
         if dist is not None:
@@ -467,6 +571,8 @@ def main():
         line["cpu_baseline"] = {k2: cpu[k2] for k2 in ("value", "unit", "cores", "kind", "sample")}
     if batched:
         line["batched"] = batched
+    if adjoint:
+        line["adjoint"] = adjoint
     line["rays_per_s"] = (cnt[0] + cnt[1]) * world / (total_s / args.steps)
     print(json.dumps(line), flush=True)
     k.dispose()
