@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the inverse-rendering leg")
     ap.add_argument("--adjoint-iters", type=int, default=10)
+    ap.add_argument("--trace-config", type=int, default=-1, help="fixed traversal configuration (skips the autotuner)")
     return ap.parse_args()
 
 
@@ -426,7 +427,11 @@ def main():
     k.synchronize()
     from dfpt.autotune import tune_trace
 
-    tuning = tune_trace(k, passes=3, warmup=1)
+    if args.trace_config >= 0:
+        k.set_tuning("trace_config", args.trace_config)
+        tuning = {"best": args.trace_config, "ms_per_pass": {}}
+    else:
+        tuning = tune_trace(k, passes=3, warmup=1)
     k.execute(args.warmup)
     k.synchronize()
 
