@@ -301,6 +301,9 @@ def adjoint_leg(args, torch, barrier, dist, world):
     cs, params, (w, h), truth, start = synthetic.inverse_scene(seed=6, width=512, height=512, count=256)
     k = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), params)
     k.update(w, h)
+    from dfpt.autotune import tune_trace
+
+    tuning = tune_trace(k, passes=4, warmup=1)
     d = DiffRenderer(k)
     spp = 16
     target = d.forward(truth["albedo"], None, truth["phong_exponent"], truth["turbidity"], truth["sun_direction"], 256).astype(np.float64)
@@ -380,6 +383,8 @@ def adjoint_leg(args, torch, barrier, dist, world):
         "t_adj_over_t_fwd": t_adj / t_fwd, "spp_per_iter": spp, "resolution": [w, h], "primitives": int(cs.primitives.size // 3),
         "loss_first": losses[0], "loss_last": losses[-1], "iters": len(losses),
         "fd_check": fd, "fd_check_no_russian_roulette": fd_no_rr, "fd_step": hstep,
+        "trace_config": tuning["best"], "primitive_culling": tuning.get("primitive_culling", 0),
+        "culling_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("culling_ms_per_pass", {}).items()},
         "workload": "inverse_scene seed 6: 256 spheres (every 4th Phong) on a plane, Perez sky; albedo U(0.1,0.9)^3, T 3 -> start 0.5, T 2",
         "timing": "host clock around forward + FP64 loss + backward + update (C-ABI, host buffers)",
     }
@@ -560,6 +565,8 @@ def main():
                    "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": 1,
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "scene_build_s": round(t_build, 1), "trace_config": tuning["best"],
+                   "primitive_culling": tuning.get("primitive_culling", 0),
+                   "culling_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("culling_ms_per_pass", {}).items()},
                    "trace_config_ms": {str(kk): round(v, 3) for kk, v in tuning["ms_per_pass"].items()}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4},
         "gpu_launches": int(launches),

@@ -233,6 +233,156 @@ int build_derived(const HostScene& s, Derived& d) {
     return DFPT_OK;
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// Primitive culling structure. World bounds of each bounded primitive: its object-space bound
+// (mesh: the BVH root box; sphere: center +- radius; triangle: its three vertices) mapped by the
+// inverse of its world-to-object matrix (the matrix the kernel transforms rays with), in double,
+// padded by 1e-4 of the box's extent and magnitude plus 1e-4 and rounded outward to float. Planes,
+// terrains, primitives with singular or non-finite matrices go to the unbounded list.
+
+bool invert_affine(const float* m, double* inv) {
+    // m: row-major 4x4 with rows 0-2 the affine map [A | t]; inv = [A^-1 | -A^-1 t].
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+    const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+    if (!(std::fabs(det) > 1e-300) || !std::isfinite(det)) return false;
+    const double r = 1.0 / det;
+    double A[9] = {(e * i - f * h) * r, (c * h - b * i) * r, (b * f - c * e) * r,
+                   (f * g - d * i) * r, (a * i - c * g) * r, (c * d - a * f) * r,
+                   (d * h - e * g) * r, (b * g - a * h) * r, (a * e - b * d) * r};
+    const double tx = m[3], ty = m[7], tz = m[11];
+    for (int k = 0; k < 3; ++k) {
+        inv[4 * k + 0] = A[3 * k]; inv[4 * k + 1] = A[3 * k + 1]; inv[4 * k + 2] = A[3 * k + 2];
+        inv[4 * k + 3] = -(A[3 * k] * tx + A[3 * k + 1] * ty + A[3 * k + 2] * tz);
+    }
+    for (int k = 0; k < 12; ++k)
+        if (!std::isfinite(inv[k])) return false;
+    return true;
+}
+
+struct CullItem { float lo[3], hi[3]; int prim; };
+
+int build_cull_node(std::vector<CullItem>& items, int begin, int end, Derived& d) {
+    const int node = (int)d.cull_nodes.size() / 2;
+    d.cull_nodes.push_back(make_float4(0, 0, 0, 0));
+    d.cull_nodes.push_back(make_float4(0, 0, 0, 0));
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = begin; k < end; ++k)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], items[k].lo[a]);
+            hi[a] = std::max(hi[a], items[k].hi[a]);
+            const float c = 0.5f * (items[k].lo[a] + items[k].hi[a]);
+            clo[a] = std::min(clo[a], c);
+            chi[a] = std::max(chi[a], c);
+        }
+    int l, r;
+    if (end - begin <= 4) {
+        std::vector<int> ps;
+        for (int k = begin; k < end; ++k) ps.push_back(items[k].prim);
+        std::sort(ps.begin(), ps.end());
+        l = -((int)d.cull_prims.size() + 1);
+        r = end - begin;
+        d.cull_prims.insert(d.cull_prims.end(), ps.begin(), ps.end());
+    } else {
+        int axis = 0;
+        for (int a = 1; a < 3; ++a)
+            if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+        const int mid = (begin + end) / 2;
+        std::nth_element(items.begin() + begin, items.begin() + mid, items.begin() + end, [axis](const CullItem& x, const CullItem& y) {
+            return x.lo[axis] + x.hi[axis] < y.lo[axis] + y.hi[axis];
+        });
+        l = build_cull_node(items, begin, mid, d);
+        r = build_cull_node(items, mid, end, d);
+    }
+    float la, ra;
+    std::memcpy(&la, &l, 4);
+    std::memcpy(&ra, &r, 4);
+    d.cull_nodes[2 * node] = make_float4(lo[0], lo[1], lo[2], la);
+    d.cull_nodes[2 * node + 1] = make_float4(hi[0], hi[1], hi[2], ra);
+    return node;
+}
+
+// Object-space bound per primitive (6 floats: lo, hi; NaN lo.x for unbounded shapes).
+void cull_object_bounds(const Derived& d, int np, std::vector<float>& obj) {
+    obj.assign((size_t)6 * np, 0.0f);
+    for (int i = 0; i < np; ++i) {
+        const int4 info = d.prim_info[i];
+        float* o = obj.data() + 6 * (size_t)i;
+        if (info.x == DFPT_SHAPE_TRIANGLE_MESH) {
+            const float4 a = d.nodes[2 * (size_t)info.w], b = d.nodes[2 * (size_t)info.w + 1];
+            o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = b.x; o[4] = b.y; o[5] = b.z;
+        } else if (info.x == DFPT_SHAPE_SPHERE) {
+            const float4 sp = d.sphere4[info.w];
+            const float r = std::fabs(sp.w);
+            o[0] = sp.x - r; o[1] = sp.y - r; o[2] = sp.z - r; o[3] = sp.x + r; o[4] = sp.y + r; o[5] = sp.z + r;
+        } else if (info.x == DFPT_SHAPE_TRIANGLE) {
+            const float4 a = d.tris[3 * (size_t)info.w], e0 = d.tris[3 * (size_t)info.w + 1], e1 = d.tris[3 * (size_t)info.w + 2];
+            const float v[3][3] = {{a.x, a.y, a.z}, {a.x + e0.x, a.y + e0.y, a.z + e0.z}, {a.x + e1.x, a.y + e1.y, a.z + e1.z}};
+            for (int c = 0; c < 3; ++c) {
+                o[c] = std::min(v[0][c], std::min(v[1][c], v[2][c]));
+                o[3 + c] = std::max(v[0][c], std::max(v[1][c], v[2][c]));
+            }
+            // The triangle's vertices a + e are rounded sums: widen by their rounding.
+            for (int c = 0; c < 3; ++c) {
+                const float m = std::max(std::fabs(o[c]), std::fabs(o[3 + c]));
+                o[c] -= m * 1e-6f;
+                o[3 + c] += m * 1e-6f;
+            }
+        } else {
+            o[0] = NAN;
+        }
+    }
+}
+
+// The culling BVH from object bounds and the world-to-object matrices.
+void build_culling(const std::vector<float>& obj, const std::vector<float>& w2o, int np, Derived& d) {
+    d.cull_nodes.clear();
+    d.cull_prims.clear();
+    d.always.clear();
+    std::vector<CullItem> items;
+    d.prim_box.assign((size_t)2 * std::max(np, 1), make_float4(-INFINITY, -INFINITY, -INFINITY, 0));
+    for (int i = 0; i < np; ++i) d.prim_box[2 * i + 1] = make_float4(INFINITY, INFINITY, INFINITY, 0);
+    for (int i = 0; i < np; ++i) {
+        const float* o = obj.data() + 6 * (size_t)i;
+        double inv[12];
+        bool ok = !std::isnan(o[0]) && invert_affine(w2o.data() + 16 * (size_t)i, inv);
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int k = 0; ok && k < 8; ++k) {
+            const double p[3] = {(k & 1) ? o[3] : o[0], (k & 2) ? o[4] : o[1], (k & 4) ? o[5] : o[2]};
+            for (int a = 0; a < 3; ++a) {
+                const double w = inv[4 * a] * p[0] + inv[4 * a + 1] * p[1] + inv[4 * a + 2] * p[2] + inv[4 * a + 3];
+                if (!std::isfinite(w)) ok = false;
+                lo[a] = std::min(lo[a], w);
+                hi[a] = std::max(hi[a], w);
+            }
+        }
+        if (!ok) {
+            d.always.push_back(i);
+            continue;
+        }
+        CullItem it;
+        it.prim = i;
+        double ext = 0, mag = 0;
+        for (int a = 0; a < 3; ++a) {
+            ext = std::max(ext, hi[a] - lo[a]);
+            mag = std::max(mag, std::max(std::fabs(lo[a]), std::fabs(hi[a])));
+        }
+        const double pad = 1e-4 * (ext + mag) + 1e-4;
+        for (int a = 0; a < 3; ++a) {
+            it.lo[a] = std::nextafter((float)(lo[a] - pad), -INFINITY);
+            it.hi[a] = std::nextafter((float)(hi[a] + pad), INFINITY);
+        }
+        d.prim_box[2 * i] = make_float4(it.lo[0], it.lo[1], it.lo[2], 0);
+        d.prim_box[2 * i + 1] = make_float4(it.hi[0], it.hi[1], it.hi[2], 0);
+        items.push_back(it);
+    }
+    d.bounded = (int)items.size();
+    if (!items.empty()) build_cull_node(items, 0, (int)items.size(), d);
+    if (d.cull_nodes.empty()) { d.cull_nodes.push_back(make_float4(0, 0, 0, 0)); d.cull_nodes.push_back(make_float4(0, 0, 0, 0)); }
+    if (d.cull_prims.empty()) d.cull_prims.push_back(0);
+}
+
 template <typename T>
 void copy_array(std::vector<T>& dst, const T* src, int64_t n) {
     dst.assign(src, src + n);
@@ -601,9 +751,11 @@ void SceneStore::release() {
     for (auto* b : fb) b->release();
     DevBuf<int>* ib[] = {&planes, &triangles, &primitives};
     for (auto* b : ib) b->release();
-    DevBuf<float4>* f4[] = {&nodes, &tris, &sphere4, &plane_a, &plane_n};
+    DevBuf<float4>* f4[] = {&nodes, &tris, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
     for (auto* b : f4) b->release();
     prim_info.release();
+    cull_prims.release();
+    always.release();
 }
 
 int scene_load(const dfpt_scene_desc* sd, SceneStore& st) {
@@ -632,6 +784,8 @@ int scene_load(const dfpt_scene_desc* sd, SceneStore& st) {
     Derived& d = st.derived;
     int r = build_derived(s, d);
     if (r) return r;
+    cull_object_bounds(d, (int)np, st.obj_box);
+    build_culling(st.obj_box, s.w2o, (int)np, d);
     if (d.nodes.size() / 2 > (size_t)INT32_MAX / 4 || d.tris.size() / 3 > (size_t)INT32_MAX / 4) return dfpt_fail(DFPT_ERR_NOT_SUPPORTED, "scene too large");
     st.scene.primitive_count = (int)np;
     st.scene.textures_count = (int)s.textures.size();
@@ -660,6 +814,8 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     CUDA_TRY(upload(st.sphere4, d.sphere4, s));
     CUDA_TRY(upload(st.plane_a, d.plane_a, s));
     CUDA_TRY(upload(st.plane_n, d.plane_n, s));
+    int rc = culling_upload(st, d, s);
+    if (rc) return rc;
     CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors below are freed
     DevScene& S = st.scene;
     S.point2fs = st.point2fs.p; S.point3fs = st.point3fs.p; S.vector3fs = st.vector3fs.p;
@@ -670,6 +826,36 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     S.plane_a = st.plane_a.p; S.plane_n = st.plane_n.p;
     st.derived = Derived();
     return DFPT_OK;
+}
+
+int culling_upload(SceneStore& st, const Derived& d, cudaStream_t s) {
+    CUDA_TRY(upload(st.cull_nodes, d.cull_nodes, s));
+    CUDA_TRY(upload(st.prim_box, d.prim_box, s));
+    CUDA_TRY(upload(st.cull_prims, d.cull_prims, s));
+    std::vector<int> always = d.always;
+    if (always.empty()) always.push_back(0);
+    CUDA_TRY(upload(st.always, always, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    DevScene& S = st.scene;
+    S.cull_nodes = st.cull_nodes.p; S.prim_box = st.prim_box.p; S.cull_prims = st.cull_prims.p;
+    S.always = st.always.p;
+    S.always_count = (int)d.always.size();
+    // Culling is offered for scenes with 8 or more bounded primitives; the default mode is the
+    // per-primitive box test, the autotuner may pick the BVH candidates or none.
+    st.culling_available = d.bounded >= 8;
+    S.use_culling = st.culling_available ? st.culling_wanted : 0;
+    return DFPT_OK;
+}
+
+int scene_rebuild_culling(SceneStore& st, cudaStream_t s) {
+    Derived d;
+    build_culling(st.obj_box, st.host.w2o, st.scene.primitive_count, d);
+    return culling_upload(st, d, s);
+}
+
+void scene_set_culling(SceneStore& st, int mode) {
+    st.culling_wanted = mode;
+    st.scene.use_culling = st.culling_available ? mode : 0;
 }
 
 int noise_tables_init(const KernelSet& ks, cudaStream_t st) {
@@ -812,6 +998,10 @@ int dfpt_set_transforms(dfpt_handle* h, const float* o2w, const float* w2o, int3
     CUDA_TRY(cudaMemcpyAsync(h->sc.o2w.p, h->sc.host.o2w.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaMemcpyAsync(h->sc.w2o.p, h->sc.host.w2o.data(), (size_t)count * 64, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    // World bounds follow the new transforms (the culling arrays may be reallocated).
+    int r = scene_rebuild_culling(h->sc, h->stream);
+    if (r) return r;
+    h->graph_valid = false;
     return DFPT_OK;
 }
 
@@ -872,6 +1062,12 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "primitive_culling") == 0) {
+        if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
+        scene_set_culling(h->sc, value);
+        h->graph_valid = false;
+        return DFPT_OK;
+    }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 
@@ -879,6 +1075,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (!h || !key || !value) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (std::strcmp(key, "trace_config") == 0) { *value = h->ctx.trace_config; return DFPT_OK; }
     if (std::strcmp(key, "trace_configs") == 0) { *value = h->fast.trace_configs; return DFPT_OK; }
+    if (std::strcmp(key, "primitive_culling") == 0) { *value = h->sc.scene.use_culling; return DFPT_OK; }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 

@@ -464,9 +464,75 @@ __device__ Hit trace_warp(const DevScene& S, bool valid, float ox, float oy, flo
     return h;
 }
 
+// One primitive of doIntersectPrimitives (GRK:1048-1256): the ray in object space, then the
+// shape's test against the closest distance so far. Returns true when an any-hit query is done.
+template <bool ANY, int V>
+__device__ __forceinline__ bool prim_test(const DevScene& S, int i, float ox, float oy, float oz, float dx, float dy, float dz, Hit& h,
+                                          TraceStats& st) {
+    const int4 info = __ldg(S.prim_info + i);
+    const float4* W = reinterpret_cast<const float4*>(S.w2o) + i * 4;
+    const float4 r0 = __ldg(W), r1 = __ldg(W + 1), r2 = __ldg(W + 2);
+    const float oxo = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
+    const float oyo = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
+    const float ozo = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
+    const float dxo = r0.x * dx + r0.y * dy + r0.z * dz;
+    const float dyo = r1.x * dx + r1.y * dy + r1.z * dz;
+    const float dzo = r2.x * dx + r2.y * dy + r2.z * dz;
+    float t = INF;
+    const int type = info.x;
+    if (type == DFPT_SHAPE_TRIANGLE_MESH) {
+        // The mesh updates the closest hit in place; t stays INF for the check below.
+        if (mesh_walk<ANY, V>(S, info.w, i, oxo, oyo, ozo, dxo, dyo, dzo, h, st)) return true;
+    } else if (type == DFPT_SHAPE_PLANE) {
+        t = isect_plane(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.plane_a + info.w), __ldg(S.plane_n + info.w), h.t);
+    } else if (type == DFPT_SHAPE_SPHERE) {
+        t = isect_sphere(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.sphere4 + info.w), h.t);
+    } else if (type == DFPT_SHAPE_TERRAIN) {
+        t = isect_terrain(oxo, oyo, ozo, dxo, dyo, dzo);
+    } else if (type == DFPT_SHAPE_TRIANGLE) {
+        st.tris++;
+        t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.tris + 3 * info.w), __ldg(S.tris + 3 * info.w + 1),
+                           __ldg(S.tris + 3 * info.w + 2), h.t);
+    }
+    if (t < h.t) {
+        h.t = t;
+        h.prim = i;
+        h.shape_type = type;
+        h.shape_offset = info.y;
+    }
+    return ANY && h.prim != -1;
+}
+
+// Slab test of a padded world box against the ray's half line t >= 0: the entry distance, or
+// +inf when the line misses. An axis whose direction component is (nearly) zero is a slab the
+// ray stays in or out of for every t, tested on the origin directly (no 0 * inf).
+__device__ __forceinline__ void cull_slab(float lo, float hi, float o, float d, float inv, float& tmin, float& tmax) {
+    if (fabsf(d) < 1.0e-20f) {
+        if (!(o >= lo && o <= hi)) {
+            tmin = INFINITY;
+            tmax = -INFINITY;
+        }
+        return;
+    }
+    const float t0 = (lo - o) * inv, t1 = (hi - o) * inv;
+    tmin = fmaxf(tmin, fminf(t0, t1));
+    tmax = fminf(tmax, fmaxf(t0, t1));
+}
+__device__ __forceinline__ float box_entry(float4 lo, float4 hi, float ox, float oy, float oz, float dx, float dy, float dz, float ix,
+                                           float iy, float iz) {
+    float tmin = 0.0f, tmax = INFINITY;
+    cull_slab(lo.x, hi.x, ox, dx, ix, tmin, tmax);
+    cull_slab(lo.y, hi.y, oy, dy, iy, tmin, tmax);
+    cull_slab(lo.z, hi.z, oz, dz, iz, tmin, tmax);
+    return tmin <= tmax ? tmin : INFINITY;
+}
+
 // doIntersectPrimitives (GRK:1048-1256): a linear loop over primitives, each ray transformed
 // to object space; meshes walk the threaded (preorder, skip-pointer) BVH exactly as flattened.
-// ANY = isTesting: return at the first primitive with a hit.
+// ANY = isTesting: return at the first primitive with a hit. With culling mode 1 each primitive's
+// padded world box is tested first and the primitive skipped when the ray's half line misses it
+// or enters it beyond the closest distance found so far (see trace_culled for why that leaves
+// the result unchanged); the loop order is the reference's.
 template <bool ANY, int V = 0>
 __device__ Hit trace(const DevScene& S, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
     Hit h;
@@ -475,41 +541,94 @@ __device__ Hit trace(const DevScene& S, float ox, float oy, float oz, float dx, 
     h.shape_type = -1;
     h.shape_offset = -1;
     const int np = S.primitive_count;
-    for (int i = 0; i < np; ++i) {
-        const int4 info = __ldg(S.prim_info + i);
-        const float4* W = reinterpret_cast<const float4*>(S.w2o) + i * 4;
-        const float4 r0 = __ldg(W), r1 = __ldg(W + 1), r2 = __ldg(W + 2);
-        const float oxo = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
-        const float oyo = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
-        const float ozo = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
-        const float dxo = r0.x * dx + r0.y * dy + r0.z * dz;
-        const float dyo = r1.x * dx + r1.y * dy + r1.z * dz;
-        const float dzo = r2.x * dx + r2.y * dy + r2.z * dz;
-        float t = INF;
-        const int type = info.x;
-        if (type == DFPT_SHAPE_TRIANGLE_MESH) {
-            // The mesh updates the closest hit in place; t stays INF for the check below.
-            if (mesh_walk<ANY, V>(S, info.w, i, oxo, oyo, ozo, dxo, dyo, dzo, h, st)) return h;
-        } else if (type == DFPT_SHAPE_PLANE) {
-            t = isect_plane(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.plane_a + info.w), __ldg(S.plane_n + info.w), h.t);
-        } else if (type == DFPT_SHAPE_SPHERE) {
-            t = isect_sphere(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.sphere4 + info.w), h.t);
-        } else if (type == DFPT_SHAPE_TERRAIN) {
-            t = isect_terrain(oxo, oyo, ozo, dxo, dyo, dzo);
-        } else if (type == DFPT_SHAPE_TRIANGLE) {
-            st.tris++;
-            t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, __ldg(S.tris + 3 * info.w), __ldg(S.tris + 3 * info.w + 1),
-                               __ldg(S.tris + 3 * info.w + 2), h.t);
+    if (S.use_culling == 1) {
+        const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+        for (int i = 0; i < np; ++i) {
+            const float4 lo = __ldg(S.prim_box + 2 * i), hi = __ldg(S.prim_box + 2 * i + 1);
+            if (box_entry(lo, hi, ox, oy, oz, dx, dy, dz, ix, iy, iz) > h.t) continue;
+            if (prim_test<ANY, V>(S, i, ox, oy, oz, dx, dy, dz, h, st)) return h;
         }
-        if (t < h.t) {
-            h.t = t;
-            h.prim = i;
-            h.shape_type = type;
-            h.shape_offset = info.y;
+        return h;
+    }
+    for (int i = 0; i < np; ++i)
+        if (prim_test<ANY, V>(S, i, ox, oy, oz, dx, dy, dz, h, st)) return h;
+    return h;
+}
+
+// The same loop over only the primitives the ray can reach, still in primitive order. A
+// primitive whose padded world box the ray's half line misses, or enters beyond the closest
+// distance found so far, cannot change the closest hit - its object-space root box or shape
+// test would reject it (the world box holds the primitive's geometry under the inverse of its
+// world-to-object matrix, padded for rounding) - so skipping it leaves every later test with
+// the closest distance the full loop would have. The reachable primitives are collected from
+// the culling BVH, sorted, merged with the unbounded ones, and tested with prim_test. More than
+// DFPT_CULL_CANDIDATES of them (or a deeper tree than the stack) falls back to the full loop.
+template <bool ANY, int V>
+__device__ Hit trace_culled(const DevScene& S, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
+    const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+    int cand[DFPT_CULL_CANDIDATES];
+    int nc = 0;
+    bool overflow = false;
+    int stack[DFPT_CULL_STACK];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        const float4 a = __ldg(S.cull_nodes + 2 * node), b = __ldg(S.cull_nodes + 2 * node + 1);
+        if (box_entry(a, b, ox, oy, oz, dx, dy, dz, ix, iy, iz) < INFINITY) {
+            const int l = __float_as_int(a.w), r = __float_as_int(b.w);
+            if (l < 0) {
+                for (int k = -l - 1, e = -l - 1 + r; k < e; ++k) {
+                    if (nc == DFPT_CULL_CANDIDATES) { overflow = true; break; }
+                    const int p = __ldg(S.cull_prims + k);
+                    int j = nc++;
+                    while (j > 0 && cand[j - 1] > p) { cand[j] = cand[j - 1]; --j; }
+                    cand[j] = p;
+                }
+                if (overflow) break;
+            } else {
+                if (sp == DFPT_CULL_STACK) { overflow = true; break; }
+                stack[sp++] = r;
+                node = l;
+                continue;
+            }
         }
-        if (ANY && h.prim != -1) return h;
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    if (overflow) {
+        // The full loop, with the per-primitive box test (mode 1).
+        DevScene flat = S;
+        flat.use_culling = 1;
+        return trace<ANY, V>(flat, ox, oy, oz, dx, dy, dz, st);
+    }
+    Hit h;
+    h.t = INF;
+    h.prim = -1;
+    h.shape_type = -1;
+    h.shape_offset = -1;
+    int ia = 0, ic = 0;
+    const int na = S.always_count;
+    while (ia < na || ic < nc) {
+        const int pa = ia < na ? __ldg(S.always + ia) : 0x7FFFFFFF;
+        const int pc = ic < nc ? cand[ic] : 0x7FFFFFFF;
+        int i;
+        if (pa < pc) {
+            i = pa;
+            ++ia;
+        } else {
+            i = pc;
+            ++ic;
+            const float4 lo = __ldg(S.prim_box + 2 * i), hi = __ldg(S.prim_box + 2 * i + 1);
+            if (box_entry(lo, hi, ox, oy, oz, dx, dy, dz, ix, iy, iz) > h.t) continue;
+        }
+        if (prim_test<ANY, V>(S, i, ox, oy, oz, dx, dy, dz, h, st)) return h;
     }
     return h;
+}
+
+// Closest hit of one ray with the per-lane walk, through the culling structure when the scene has one.
+__device__ __forceinline__ Hit trace_s(const DevScene& S, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
+    return S.use_culling == 2 ? trace_culled<false, 0>(S, ox, oy, oz, dx, dy, dz, st) : trace<false, 0>(S, ox, oy, oz, dx, dy, dz, st);
 }
 
 // Selects the walk: V 0/1 per-lane (every lane may call it alone), V 2 warp-synchronous (all 32
@@ -519,7 +638,7 @@ __device__ __forceinline__ Hit trace_v(const DevScene& S, bool valid, float ox, 
     if constexpr (V == 2) {
         return trace_warp<ANY>(S, valid, ox, oy, oz, dx, dy, dz, st);
     } else {
-        if (valid) return trace<ANY, V>(S, ox, oy, oz, dx, dy, dz, st);
+        if (valid) return S.use_culling == 2 ? trace_culled<ANY, V>(S, ox, oy, oz, dx, dy, dz, st) : trace<ANY, V>(S, ox, oy, oz, dx, dy, dz, st);
     }
     Hit h;
     h.t = INF;

@@ -31,7 +31,18 @@ struct DevScene {
     const float4* sphere4;  // {position.xyz, radius} per sphere record
     const float4* plane_a;  // point A per plane record
     const float4* plane_n;  // surface normal per plane record
+    // Primitive culling (scenes with many primitives): a BVH over padded world-space bounds of
+    // the bounded primitives, and the unbounded ones (planes, terrains) that every ray tests.
+    int use_culling;          // 0: the full primitive loop; 1: the loop with a world-box test per
+                              // primitive; 2: the candidates collected from the culling BVH
+    const float4* cull_nodes; // 2 per node: {lo.xyz, left child or -(first + 1) for a leaf}, {hi.xyz, right child or count}
+    const int* cull_prims;    // leaf primitive lists, ascending within a leaf
+    const int* always;        // unbounded primitives, ascending
+    int always_count;
+    const float4* prim_box;   // 2 per primitive: padded world bounds lo, hi (unbounded: -/+inf)
 };
+#define DFPT_CULL_CANDIDATES 16  // candidates a ray collects before falling back to the full loop
+#define DFPT_CULL_STACK 32
 
 // Renderer parameters and derived per-scene constants, in device memory (read through __ldg) so
 // captured CUDA graphs stay valid when they change.

@@ -903,7 +903,7 @@ __device__ int phong0(const DevScene& S, const DevParams& P, bool test, float px
     const float lr = 1.0f / ll;
     const float lnx = lx * lr, lny = ly * lr, lnz = lz * lr;
     float t = INF;
-    if (test) t = trace<false>(S, px, py, pz, lnx, lny, lnz, st).t;
+    if (test) t = trace_s(S, px, py, pz, lnx, lny, lnz, st).t;
     if (t >= INF || t > l2) {
         const float ldn = lnx * nx + lny * ny + lnz * nz;
         r += ar * 0.5f * jmax(ldn, 0.0f) * 1.0f;
@@ -979,7 +979,7 @@ __global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __r
                 } else {
                     const int depth_max = mode == DFPT_RENDERER_RAY_TRACER ? 5 : 1;
                     for (int depth = 0; depth < depth_max; ++depth) {
-                        const Hit h = trace<false>(S, ox, oy, oz, dx, dy, dz, st);
+                        const Hit h = trace_s(S, ox, oy, oz, dx, dy, dz, st);
                         segs++;
                         if (depth == 0) B.primitive_offsets[i] = h.prim >= 0 ? h.prim * 3 : -1;
                         if (h.t == INF || h.prim == -1) {
@@ -1018,7 +1018,7 @@ __global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __r
                             const float e1z = e0x * u2z + e0y * v0z + e0z * w1z;
                             const float er = rsqrt_j(e1x * e1x + e1y * e1y + e1z * e1z);
                             const float aox = s.px + w1x * 0.01f, aoy = s.py + w1y * 0.01f, aoz = s.pz + w1z * 0.01f;
-                            const float t = trace<false>(S, aox, aoy, aoz, e1x * er, e1y * er, e1z * er, st).t;
+                            const float t = trace_s(S, aox, aoy, aoz, e1x * er, e1y * er, e1z * er, st).t;
                             segs++;
                             const bool hit = t < P.ao_max_distance;
                             const float v = hit ? 1.0f : 0.0f;  // bright 1, dark 0
@@ -1066,7 +1066,7 @@ __global__ void __launch_bounds__(128) k_wireframe(DevScene S, const DevParams* 
         if (i < n && B.pixel_flags[i] == 0) {
             TraceStats st{0, 0};
             const float4 o = B.primary_o[i], d = B.primary_d[i];
-            const Hit h = trace<false>(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            const Hit h = trace_s(S, o.x, o.y, o.z, d.x, d.y, d.z, st);
             const float line_cos = P.wire_cos;
             if (h.t != INF && h.prim != -1 && h.shape_type == DFPT_SHAPE_TRIANGLE) {
                 const Surf s = surface(S, P, o.x, o.y, o.z, d.x, d.y, d.z, h);

@@ -57,6 +57,10 @@ struct HostScene {
 struct Derived {
     std::vector<int4> prim_info;
     std::vector<float4> nodes, tris, sphere4, plane_a, plane_n;
+    // Primitive culling (see build_culling): BVH nodes, leaf lists, unbounded primitives, boxes.
+    std::vector<float4> cull_nodes, prim_box;
+    std::vector<int> cull_prims, always;
+    int bounded = 0;  // primitives with a world box
 };
 
 // One validated compiled scene: the host copy, its device arrays and the kernel-side view.
@@ -67,6 +71,11 @@ struct SceneStore {
     DevBuf<int> planes, triangles, primitives;
     DevBuf<int4> prim_info;
     DevBuf<float4> nodes, tris, sphere4, plane_a, plane_n;
+    DevBuf<float4> cull_nodes, prim_box;
+    DevBuf<int> cull_prims, always;
+    std::vector<float> obj_box;      // object-space bound per primitive (culling rebuilds)
+    bool culling_available = false;  // enough bounded primitives for culling to pay
+    int culling_wanted = 1;          // 0 none, 1 box test per primitive, 2 BVH candidates
     DevScene scene{};
     void release();
 };
@@ -75,6 +84,12 @@ struct SceneStore {
 int scene_load(const dfpt_scene_desc* sd, SceneStore& st);
 // Uploads a loaded scene to the device on `s` and fills `st.scene`.
 int scene_upload(SceneStore& st, cudaStream_t s);
+// Selects the primitive culling mode in st.scene (0 none, 1 box test, 2 BVH candidates; 0 when
+// the scene has too few bounded primitives).
+void scene_set_culling(SceneStore& st, int mode);
+// Rebuilds the culling structure after the world-to-object matrices changed.
+int scene_rebuild_culling(SceneStore& st, cudaStream_t s);
+int culling_upload(SceneStore& st, const Derived& d, cudaStream_t s);
 // Packs parameters, sky and camera into the device record (host-computed tangents and constants).
 void dev_params_fill(DevParams& d, const dfpt_params& p, const dfpt_sky& k, const float* camera19, int width, int height);
 // Loads the simplex noise tables into the kernel set's device copies.

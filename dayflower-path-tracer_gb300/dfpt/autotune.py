@@ -11,7 +11,24 @@ import time
 
 
 def tune_trace(kernel, passes: int = 4, warmup: int = 1, verbose: bool = False) -> dict:
-    """Times each configuration on `kernel` (a RendererKernel after update()); sets the best one."""
+    """Times each configuration on `kernel` (a RendererKernel after update()); sets the best one.
+    Scenes with enough bounded primitives first get their primitive-culling mode picked (0 the
+    reference's full loop, 1 a world-box test per primitive, 2 candidates from a BVH over the
+    boxes; all three give the same hits)."""
+    culling = {}
+    kernel.set_tuning("primitive_culling", 1)
+    if kernel.get_tuning("primitive_culling") == 1:
+        for mode in (0, 1, 2):
+            kernel.set_tuning("primitive_culling", mode)
+            kernel.execute(warmup)
+            kernel.synchronize()
+            t0 = time.perf_counter()
+            kernel.execute(passes)
+            kernel.synchronize()
+            culling[mode] = (time.perf_counter() - t0) / passes * 1e3
+            if verbose:
+                print(f"primitive_culling {mode}: {culling[mode]:.3f} ms/pass", flush=True)
+        kernel.set_tuning("primitive_culling", min(culling, key=culling.get))
     n = kernel.get_tuning("trace_configs")
     results = {}
     for cfg in range(n):
@@ -26,7 +43,11 @@ def tune_trace(kernel, passes: int = 4, warmup: int = 1, verbose: bool = False) 
             print(f"trace_config {cfg}: {results[cfg]:.3f} ms/pass", flush=True)
     best = min(results, key=results.get)
     kernel.set_tuning("trace_config", best)
-    return {"best": best, "ms_per_pass": results}
+    out = {"best": best, "ms_per_pass": results}
+    if culling:
+        out["primitive_culling"] = kernel.get_tuning("primitive_culling")
+        out["culling_ms_per_pass"] = culling
+    return out
 
 
 def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=None, window: int | None = None,
