@@ -1,8 +1,11 @@
 """Benchmark: M path samples/s of the GB300 renderer core on the 1080p triangle-mesh workload.
 
-One step = one pass of the path tracer over the whole 1920x1080 image (one sample per pixel), the
-unit of the reference's Kernel.execute (DayflowerApplication.java:853). The workload is
-mesh_scene: an fBm-displaced geodesic icosphere (200,000 triangles, 4 Lambertian/Phong regions)
+One step = one dfpt_render call of --spp-per-step passes (default 16) over the whole 1920x1080
+image; a pass is one sample per pixel, the unit of the reference's Kernel.execute
+(DayflowerApplication.java:853), so the default 16 timed steps render the 256 spp of the
+triangle-mesh configuration. Inside a call, all passes but the last run `wide_samples` at a time
+through the wave kernels (same samples, same film as pass-by-pass rendering, tested). The workload
+is mesh_scene: an fBm-displaced geodesic icosphere (200,000 triangles, 4 Lambertian/Phong regions)
 over a 512x512 fBm heightfield (522,242 triangles), BVHs built by the restated reference builder,
 depth 8, ACES; seeded synthetic data (the reference publishes no scenes).
 
@@ -34,14 +37,15 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "dayflower-path-tracer_gb300"))
 sys.path.insert(0, str(ROOT))
 
-METRIC = "M path samples/s @1080p (1 spp passes)"
+METRIC = "M path samples/s @1080p"
 UNIT = "M samples/s"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=32)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--spp-per-step", type=int, default=16, help="passes (1 spp each) per step: one dfpt_render call")
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="dfpt", choices=["dfpt", "reference"])
     ap.add_argument("--workload", default="mesh_scene", choices=["mesh_scene", "sphere_scene", "instances_scene"])
@@ -414,6 +418,11 @@ def main():
         torch.cuda.synchronize()
 
     from dfpt.kernel import RendererKernel
+    from dfpt import _lib as dlib
+
+    def l2_reset():
+        # Persisting L2 lines survive a plain flush: return them to normal too.
+        dlib.check(dlib.load().dfpt_l2_reset())
 
     t_build = time.perf_counter()
     scene, sky, params, (w, h) = build_workload(args.workload, args.width, args.height)
@@ -426,22 +435,25 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     n_pix = w * h
 
-    # Warm-up (graphs built here), then the traversal launch configuration is autotuned on this
-    # scene (outside the timed region).
-    k.execute(args.warmup)
+    # Warm-up (graphs built here), then the launch configuration is autotuned on this scene
+    # (outside the timed region): passes per wave, primitive culling, L2 residency, traversal kernel.
+    S = args.spp_per_step
+    k.execute(S)
     k.synchronize()
-    from dfpt.autotune import tune_trace
+    from dfpt.autotune import tune_trace, tune_wide
 
+    wide = tune_wide(k, passes=S)
     if args.trace_config >= 0:
         k.set_tuning("trace_config", args.trace_config)
         tuning = {"best": args.trace_config, "ms_per_pass": {}}
     else:
-        tuning = tune_trace(k, passes=3, warmup=1)
-    k.execute(args.warmup)
+        tuning = tune_trace(k, passes=S, warmup=1)
+    for _ in range(args.warmup):
+        k.execute(S)
     k.synchronize()
 
-    # Timed region: the pass graph replayed once per step, per-step events on the handle's stream,
-    # L2 flushed between steps.
+    # Timed region: one dfpt_render call of S passes per step (waves of wide passes + the last
+    # pass, replayed graphs), per-step events on the handle's stream, L2 flushed between steps.
     sampler = ClockSampler(local)
     launches0 = k.launch_count()
     barrier()
@@ -450,10 +462,11 @@ def main():
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
+            l2_reset()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-        k.execute(1)
+        k.execute(S)
         with torch.cuda.stream(stream):
             e1.record(stream)
         e1.synchronize()
@@ -466,19 +479,20 @@ def main():
         t = torch.tensor([total_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_s = float(t.item())
-    value = world * n_pix * args.steps / total_s / 1e6
+    value = world * n_pix * S * args.steps / total_s / 1e6
 
     # The same steps with an event between kernels (direct launches): per-kernel times, and the
-    # average duration of the closest-hit traversal launch for the roofline.
+    # closest-hit traversal time for the roofline.
     k.set_profiling(True)
     trace_ms, trace_n, kind_ms, prof_ms = 0.0, 0, {}, []
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
+            l2_reset()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-        k.execute(1)
+        k.execute(S)
         with torch.cuda.stream(stream):
             e1.record(stream)
         e1.synchronize()
@@ -492,9 +506,9 @@ def main():
             a[1] += n
     k.set_profiling(False)
 
-    # Traversal counters over one extra pass (not timed): segments per pass.
+    # Traversal counters over one extra step (not timed): segments per step.
     k.set_counting(True)
-    k.execute(1)
+    k.execute(S)
     k.synchronize()
     cnt = k.counters().astype(float)
     k.set_counting(False)
@@ -509,7 +523,7 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         k.update_camera(cam)
-        k.execute(1)
+        k.execute(S)
         k.get(host_img)
     barrier()
     e2e_s = time.perf_counter() - t0
@@ -517,7 +531,7 @@ def main():
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e_value = world * n_pix * args.steps / e2e_s / 1e6
+    e2e_value = world * n_pix * S * args.steps / e2e_s / 1e6
 
     batched = None
     if not args.no_batch:
@@ -546,10 +560,13 @@ def main():
     nodes_per_seg = cpu["nodes_per_segment"] if cpu else (cnt[2] / max(cnt[0] + cnt[1], 1))
     tris_per_seg = cpu["tris_per_segment"] if cpu else (cnt[3] / max(cnt[0] + cnt[1], 1))
     bytes_per_seg = nodes_per_seg * 32 + tris_per_seg * 48 + 64
+    # Closest-hit segments of one step (counters over a step) x algorithmic bytes per segment,
+    # over the closest-hit traversal time of a step (events inside the profiled loop).
     avg_trace_ms = trace_ms / max(trace_n, 1)
-    launches_per_pass = max(trace_n / args.steps, 1)
-    bytes_per_launch = closest_segments / launches_per_pass * bytes_per_seg
-    achieved = bytes_per_launch / (avg_trace_ms / 1e3) / 1e9
+    trace_ms_per_step = trace_ms / args.steps
+    launches_per_step = max(trace_n / args.steps, 1)
+    bytes_per_launch = closest_segments / launches_per_step * bytes_per_seg
+    achieved = closest_segments * bytes_per_seg / (trace_ms_per_step / 1e3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "trace_traffic.json"
     if tf.exists():
@@ -562,21 +579,26 @@ def main():
         "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": f"{args.workload} {w}x{h}", "triangles": int(len(scene.triangles) // 12),
-                   "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": 1,
+                   "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": S, "spp_total": S * args.steps,
+                   "wide_samples": wide["best"], "wide_ms_per_step": wide["ms_per_step"],
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "scene_build_s": round(t_build, 1), "trace_config": tuning["best"],
                    "primitive_culling": tuning.get("primitive_culling", 0),
+                   "l2_persist": tuning.get("l2_persist", 0),
+                   "l2_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("l2_ms_per_pass", {}).items()},
                    "culling_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("culling_ms_per_pass", {}).items()},
                    "trace_config_ms": {str(kk): round(v, 3) for kk, v in tuning["ms_per_pass"].items()}},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4,
+                "loop": "dfpt_set_camera(host) + dfpt_render(S passes) + dfpt_read_bgra8(host) per step"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": peak_note,
                      "kernel": "k_trace<closest>", "avg_launch_ms": avg_trace_ms,
-                     "bytes_per_segment": bytes_per_seg, "segments_per_launch": closest_segments / launches_per_pass},
+                     "bytes_per_segment": bytes_per_seg, "segments_per_launch": closest_segments / launches_per_step,
+                     "segments_per_step": closest_segments},
         "kernels_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in kind_ms.items() if v[1]},
         "ms_per_step_profiled": sum(prof_ms) / len(prof_ms),
-        "rays_per_s": (cnt[0] + cnt[1]) / (total_s / args.steps) / 1e9 * 1e3,
+
         "clocks": clocks,
     }
     if cpu:
@@ -585,7 +607,7 @@ def main():
         line["batched"] = batched
     if adjoint:
         line["adjoint"] = adjoint
-    line["rays_per_s"] = (cnt[0] + cnt[1]) * world / (total_s / args.steps)
+    line["rays_per_s"] = (cnt[0] + cnt[1]) * world / (total_s / args.steps)  # segments of one step / step time
     print(json.dumps(line), flush=True)
     k.dispose()
     if dist is not None:

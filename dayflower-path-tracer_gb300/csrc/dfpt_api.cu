@@ -444,7 +444,29 @@ struct dfpt_handle {
     bool graph_valid = false;
     int graph_kernels = 0;
     bool use_graph = true;
+    // Wide passes: dfpt_render's passes but the last run `wide_samples` at a time through the
+    // batch stages (one scene), so each launch carries k samples per pixel (see render_wide).
+    int wide_samples = 8;
+    int wide_capacity = 0;
+    size_t wide_shadow = 0;
+    DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput, w_radiance;
+    DevBuf<int4> w_q_hit, w_slot_key;
+    DevBuf<uint64_t> w_rng;
+    DevBuf<int> w_pixel_flags, w_counts, w_wave_entries;
+    DevBuf<DevScene> w_scene;
+    DevBuf<long long> w_sample_begin, w_film_begin, w_wave_base, w_wave_tab;
+    DevPass wpass{};
+    DevBatch wq{};
+    LaunchCtx wctx{};
+    cudaGraphExec_t wide_graph = nullptr;
+    bool wide_graph_valid = false;
+    int wide_graph_kernels = 0;
+    long long wide_range[4] = {0, 0, 0, -1};  // wave base, range end, pass of sample 0, clear sample
+    int pass_index_host = 0;  // source of pass-index copies (pageable: consumed on return)
     uint64_t launches = 0;
+    // L2 residency of the traversal records (see apply_l2_policy).
+    bool l2_persist = true;
+    cudaAccessPolicyWindow l2_window{};
     // Per-kernel timing (direct launches with an event between kernels).
     bool profiling = false;
     std::vector<cudaEvent_t> events;
@@ -459,6 +481,15 @@ void release(dfpt_handle* h) {
     h->events.clear();
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     h->graph_exec = nullptr;
+    if (h->wide_graph) cudaGraphExecDestroy(h->wide_graph);
+    h->wide_graph = nullptr;
+    {
+        DevBuf<float4>* w4[] = {&h->w_q_o0, &h->w_q_o1, &h->w_q_d0, &h->w_q_d1, &h->w_s_o, &h->w_s_d, &h->w_s_c, &h->w_throughput, &h->w_radiance};
+        for (auto* b : w4) b->release();
+        h->w_q_hit.release(); h->w_slot_key.release(); h->w_rng.release(); h->w_pixel_flags.release(); h->w_counts.release();
+        h->w_wave_entries.release(); h->w_scene.release(); h->w_sample_begin.release(); h->w_film_begin.release();
+        h->w_wave_base.release(); h->w_wave_tab.release();
+    }
     h->sc.release();
     h->diff_albedo.release(); h->diff_emission.release(); h->diff_L.release(); h->diff_dldi.release();
     h->diff_exponent.release(); h->diff_sky_tan.release(); h->vis.release(); h->diff_vis.release();
@@ -658,7 +689,6 @@ int issue_pass(dfpt_handle* h) {
     const KernelSet& K = kset(h);
     const LaunchCtx& c = h->ctx;
     int k = 0;
-    h->events_used = 0;
     cudaMemsetAsync(h->counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), h->stream);
     if (is_simple_mode(h->params.renderer_type)) {
         mark(h, KIND_SIMPLE); K.simple(c); ++k;
@@ -698,6 +728,147 @@ int issue_replay_pass(dfpt_handle* h) {
     return k;
 }
 
+int bounces_of(const dfpt_handle* h);
+
+// ---- Wide passes -------------------------------------------------------------------------------
+// dfpt_render(h, n) renders passes p .. p+n-1. With the path tracer, the counter-based RNG and no
+// per-pass outputs in use (wireframes, hit records, differentiable mode, strict kernels), passes
+// p .. p+n-2 run through the batch stages as one scene whose samples are (pass, pixel): a wave holds
+// `wide_samples` passes of every pixel, so every launch - late bounces included - carries k times
+// the rays of a pass. The RNG is keyed by (pixel, pass index) exactly as in a pass, and the film
+// takes each pixel's samples in pass order (k_bfilm), so the film equals pass-by-pass rendering.
+// The last pass runs as a normal pass: it writes the selection buffer and tone maps the image.
+
+bool wide_eligible(const dfpt_handle* h) {
+    return h->wide_samples > 1 && !is_simple_mode(h->params.renderer_type) && h->params.rng_kind == DFPT_RNG_COUNTER &&
+           h->params.wireframes != 1 && !h->record_hits && !h->diff_on && !h->use_strict && h->fast.b_camera != nullptr;
+}
+
+int wide_prepare(dfpt_handle* h) {
+    const size_t n = (size_t)h->n_pixels;
+    const int cap = (int)std::min<size_t>((size_t)h->wide_samples * n, (size_t)1 << 27);
+    const size_t shadow = (size_t)cap * (size_t)bounces_of(h);
+    if (cap != h->wide_capacity || shadow != h->wide_shadow) {
+        DevBuf<float4>* w4[] = {&h->w_q_o0, &h->w_q_o1, &h->w_q_d0, &h->w_q_d1, &h->w_s_o, &h->w_s_d, &h->w_s_c, &h->w_throughput, &h->w_radiance};
+        for (auto* b : w4) b->release();
+        h->w_q_hit.release(); h->w_slot_key.release(); h->w_rng.release(); h->w_pixel_flags.release();
+        const size_t c = (size_t)cap;
+        CUDA_TRY(h->w_q_o0.alloc(c)); CUDA_TRY(h->w_q_o1.alloc(c)); CUDA_TRY(h->w_q_d0.alloc(c)); CUDA_TRY(h->w_q_d1.alloc(c));
+        CUDA_TRY(h->w_q_hit.alloc(c)); CUDA_TRY(h->w_slot_key.alloc(c));
+        CUDA_TRY(h->w_throughput.alloc(c)); CUDA_TRY(h->w_radiance.alloc(c)); CUDA_TRY(h->w_rng.alloc(c)); CUDA_TRY(h->w_pixel_flags.alloc(c));
+        CUDA_TRY(h->w_s_o.alloc(shadow)); CUDA_TRY(h->w_s_d.alloc(shadow)); CUDA_TRY(h->w_s_c.alloc(shadow));
+        h->wide_capacity = cap;
+        h->wide_shadow = shadow;
+        h->wide_graph_valid = false;
+    }
+    if (!h->w_counts.p) {
+        CUDA_TRY(h->w_counts.alloc(DFPT_COUNTS_SIZE));
+        CUDA_TRY(h->w_wave_entries.alloc(1));
+        CUDA_TRY(h->w_scene.alloc(1));
+        CUDA_TRY(h->w_wave_base.alloc(4));
+        CUDA_TRY(h->w_wave_tab.alloc(8));
+        const std::vector<long long> sb = {0, 1ll << 62}, fb = {0, (long long)n};
+        CUDA_TRY(upload(h->w_sample_begin, sb, h->stream));
+        CUDA_TRY(upload(h->w_film_begin, fb, h->stream));
+    }
+    // The scene record (culling mode and pointers may change between calls).
+    std::vector<DevScene> one(1, h->sc.scene);
+    CUDA_TRY(upload(h->w_scene, one, h->stream));
+    DevPass& B = h->wpass;
+    B = DevPass{};
+    B.n_pixels = h->wide_capacity;
+    B.q_o[0] = h->w_q_o0.p; B.q_o[1] = h->w_q_o1.p; B.q_d[0] = h->w_q_d0.p; B.q_d[1] = h->w_q_d1.p;
+    B.q_hit = h->w_q_hit.p; B.s_o = h->w_s_o.p; B.s_d = h->w_s_d.p; B.s_c = h->w_s_c.p;
+    B.throughput = h->w_throughput.p; B.radiance = h->w_radiance.p; B.rng = h->w_rng.p; B.pixel_flags = h->w_pixel_flags.p;
+    B.counts = h->w_counts.p; B.stats = h->stats.p; B.pass_index = h->pass_index.p;
+    B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
+    DevBatch& Q = h->wq;
+    Q.scenes = h->w_scene.p;
+    Q.params = h->dev_params.p;
+    Q.sample_begin = h->w_sample_begin.p;
+    Q.film_begin = h->w_film_begin.p;
+    Q.n_scenes = 1;
+    Q.capacity = h->wide_capacity;
+    Q.total = 1ll << 62;
+    Q.wave_base = h->w_wave_base.p;
+    Q.slot_key = h->w_slot_key.p;
+    Q.wave_tab = h->w_wave_tab.p;
+    Q.wave_entries = h->w_wave_entries.p;
+    LaunchCtx& c = h->wctx;
+    c = h->ctx;
+    c.scene = nullptr;
+    c.pass = &h->wpass;
+    c.batch = &h->wq;
+    return DFPT_OK;
+}
+
+// One wave; returns the number of kernels launched.
+int issue_wide_wave(dfpt_handle* h) {
+    const KernelSet& K = h->fast;
+    const LaunchCtx& c = h->wctx;
+    int k = 0;
+    cudaMemsetAsync(h->w_counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), h->stream);
+    K.b_wave(c, 0); ++k;
+    mark(h, KIND_CAMERA); K.b_camera(c, 0); ++k;
+    const int nb = bounces_of(h);
+    for (int b = 0; b < nb; ++b) {
+        mark(h, KIND_TRACE); K.b_trace_closest(c, b); ++k;
+        mark(h, KIND_SHADE); K.b_shade(c, b); ++k;
+    }
+    mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
+    if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.b_shadow(c, 0); ++k; }
+    mark(h, KIND_FILM); K.b_film(c, 0); ++k;
+    mark(h, KIND_END); K.b_end(c, 0); ++k;
+    mark(h, KIND_COUNT);
+    return k;
+}
+
+// Passes host_pass .. host_pass + passes - 1 as waves of wide_samples passes.
+int render_wide(dfpt_handle* h, int passes) {
+    int r = wide_prepare(h);
+    if (r) return r;
+    const long long n = h->n_pixels;
+    // The RNG pass of sample j is host_pass + j; the film restarts at the clear pass if it is here.
+    const long long cs = (long long)h->clear_pass - h->host_pass;
+    h->wide_range[0] = 0;
+    h->wide_range[1] = (long long)passes * n;
+    h->wide_range[2] = h->host_pass;
+    h->wide_range[3] = (cs >= 0 && cs < passes) ? cs : -1;
+    CUDA_TRY(cudaMemcpyAsync(h->w_wave_base.p, h->wide_range, 4 * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+    const long long waves = (h->wide_range[1] + h->wide_capacity - 1) / h->wide_capacity;
+    if (h->use_graph && !h->profiling) {
+        if (!h->wide_graph_valid) {
+            if (h->wide_graph) cudaGraphExecDestroy(h->wide_graph);
+            h->wide_graph = nullptr;
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            const int k = issue_wide_wave(h);
+            cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&h->wide_graph, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                h->wide_graph = nullptr;
+                return dfpt_fail(DFPT_ERR_CUDA, "wide-pass graph: %s", cudaGetErrorString(e));
+            }
+            h->wide_graph_kernels = k;
+            h->wide_graph_valid = true;
+        }
+        for (long long w = 0; w < waves; ++w) {
+            CUDA_TRY(cudaGraphLaunch(h->wide_graph, h->stream));
+            h->launches += (uint64_t)h->wide_graph_kernels;
+        }
+    } else {
+        for (long long w = 0; w < waves; ++w) h->launches += (uint64_t)issue_wide_wave(h);
+        CUDA_TRY(cudaGetLastError());
+    }
+    // The device pass counter follows (the next normal pass reads it).
+    h->host_pass += passes;
+    h->pass_index_host = h->host_pass;
+    CUDA_TRY(cudaMemcpyAsync(h->pass_index.p, &h->pass_index_host, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    return DFPT_OK;
+}
+
 int bounces_of(const dfpt_handle* h) {
     const int d = h->params.pt_ray_depth_maximum;
     return d < 1 ? 1 : (d > DFPT_MAX_DEPTH ? DFPT_MAX_DEPTH : d);
@@ -714,6 +885,38 @@ int ensure_shadow_capacity(dfpt_handle* h) {
     h->shadow_capacity = need;
     h->pass.s_o = h->s_o.p; h->pass.s_d = h->s_d.p; h->pass.s_c = h->s_c.p;
     h->graph_valid = false;
+    h->wide_graph_valid = false;
+    return DFPT_OK;
+}
+
+// L2 residency: the traversal records (BVH nodes + triangles, one allocation) get an access-policy
+// window - hits persisting, misses streaming - on the handle's stream and on every kernel node of
+// the pass graph, so the ray queues and path state streaming through L2 each bounce do not evict
+// the scene. The persisting carve-out is a limit of this process's CUDA context (it ends with it).
+int apply_l2_policy(dfpt_handle* h) {
+    cudaAccessPolicyWindow w{};
+    if (h->l2_persist && h->sc.trav.p) {
+        int dev = 0, max_window = 0, max_persist = 0;
+        CUDA_TRY(cudaGetDevice(&dev));
+        CUDA_TRY(cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev));
+        CUDA_TRY(cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev));
+        const size_t bytes = std::min(h->sc.trav.n * sizeof(float4), (size_t)std::max(max_window, 0));
+        if (bytes > 0 && max_persist > 0) {
+            size_t current = 0;
+            CUDA_TRY(cudaDeviceGetLimit(&current, cudaLimitPersistingL2CacheSize));
+            const size_t want = std::min(bytes, (size_t)max_persist);
+            if (current < want) CUDA_TRY(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want));
+            w.base_ptr = h->sc.trav.p;
+            w.num_bytes = bytes;
+            w.hitRatio = (float)std::min(1.0, (double)want / (double)bytes);
+            w.hitProp = cudaAccessPropertyPersisting;
+            w.missProp = cudaAccessPropertyStreaming;
+        }
+    }
+    h->l2_window = w;
+    cudaStreamAttrValue v{};
+    v.accessPolicyWindow = w;
+    CUDA_TRY(cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &v));
     return DFPT_OK;
 }
 
@@ -721,6 +924,7 @@ int build_graph(dfpt_handle* h) {
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     h->graph_exec = nullptr;
     h->graph_valid = false;
+    h->wide_graph_valid = false;
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     const int k = issue_pass(h);
@@ -728,6 +932,26 @@ int build_graph(dfpt_handle* h) {
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
         return dfpt_fail(DFPT_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    }
+    if (h->l2_window.num_bytes > 0) {
+        // The window on every kernel node (capture does not have to carry stream attributes).
+        size_t count = 0;
+        e = cudaGraphGetNodes(g, nullptr, &count);
+        std::vector<cudaGraphNode_t> nodes(count);
+        if (e == cudaSuccess && count) e = cudaGraphGetNodes(g, nodes.data(), &count);
+        cudaKernelNodeAttrValue kv{};
+        kv.accessPolicyWindow = h->l2_window;
+        for (size_t i = 0; e == cudaSuccess && i < count; ++i) {
+            cudaGraphNodeType type;
+            e = cudaGraphNodeGetType(nodes[i], &type);
+            if (e == cudaSuccess && type == cudaGraphNodeTypeKernel)
+                e = cudaGraphKernelNodeSetAttribute(nodes[i], cudaKernelNodeAttributeAccessPolicyWindow, &kv);
+        }
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            cudaGraphDestroy(g);
+            return dfpt_fail(DFPT_ERR_CUDA, "graph L2 window: %s", cudaGetErrorString(e));
+        }
     }
     e = cudaGraphInstantiate(&h->graph_exec, g, 0);
     cudaGraphDestroy(g);
@@ -751,7 +975,7 @@ void SceneStore::release() {
     for (auto* b : fb) b->release();
     DevBuf<int>* ib[] = {&planes, &triangles, &primitives};
     for (auto* b : ib) b->release();
-    DevBuf<float4>* f4[] = {&nodes, &tris, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
+    DevBuf<float4>* f4[] = {&trav, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
     for (auto* b : f4) b->release();
     prim_info.release();
     cull_prims.release();
@@ -809,8 +1033,13 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     CUDA_TRY(upload(st.w2o, h.w2o, s));
     CUDA_TRY(upload(st.camera, h.camera, s));
     CUDA_TRY(upload(st.prim_info, d.prim_info, s));
-    CUDA_TRY(upload(st.nodes, d.nodes, s));
-    CUDA_TRY(upload(st.tris, d.tris, s));
+    {
+        std::vector<float4> trav(d.nodes);
+        trav.insert(trav.end(), d.tris.begin(), d.tris.end());
+        st.trav_nodes = d.nodes.size();
+        CUDA_TRY(upload(st.trav, trav, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+    }
     CUDA_TRY(upload(st.sphere4, d.sphere4, s));
     CUDA_TRY(upload(st.plane_a, d.plane_a, s));
     CUDA_TRY(upload(st.plane_n, d.plane_n, s));
@@ -822,7 +1051,7 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     S.planes = st.planes.p; S.spheres = st.spheres.p; S.terrains = st.terrains.p; S.triangles = st.triangles.p;
     S.textures = st.textures.p; S.surfaces = st.surfaces.p; S.primitives = st.primitives.p;
     S.o2w = st.o2w.p; S.w2o = st.w2o.p; S.camera = st.camera.p;
-    S.prim_info = st.prim_info.p; S.nodes = st.nodes.p; S.tris = st.tris.p; S.sphere4 = st.sphere4.p;
+    S.prim_info = st.prim_info.p; S.nodes = st.trav.p; S.tris = st.trav.p + st.trav_nodes; S.sphere4 = st.sphere4.p;
     S.plane_a = st.plane_a.p; S.plane_n = st.plane_n.p;
     st.derived = Derived();
     return DFPT_OK;
@@ -954,6 +1183,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     h->fast.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
     r = push_params(h);
     if (!r) r = reset_rng(h);
+    if (!r) r = apply_l2_policy(h);
     if (r) { release(h); delete h; return r; }
     *out = h;
     return DFPT_OK;
@@ -979,7 +1209,8 @@ int dfpt_set_stream(dfpt_handle* h, void* stream) {
     }
     h->ctx.stream = h->stream;
     h->graph_valid = false;
-    return DFPT_OK;
+    h->wide_graph_valid = false;
+    return apply_l2_policy(h);
 }
 
 int dfpt_set_camera(dfpt_handle* h, const float* camera19) {
@@ -1002,6 +1233,7 @@ int dfpt_set_transforms(dfpt_handle* h, const float* o2w, const float* w2o, int3
     int r = scene_rebuild_culling(h->sc, h->stream);
     if (r) return r;
     h->graph_valid = false;
+    h->wide_graph_valid = false;
     return DFPT_OK;
 }
 
@@ -1024,6 +1256,7 @@ int dfpt_set_sky(dfpt_handle* h, const dfpt_sky* sky) {
     const bool sun_changed = (h->sky.is_sun_active == 1) != (sky->is_sun_active == 1);
     h->sky = *sky;
     if (sun_changed) h->graph_valid = false;
+    h->wide_graph_valid = false;
     return push_params(h);
 }
 
@@ -1034,6 +1267,7 @@ int dfpt_set_params(dfpt_handle* h, const dfpt_params* p) {
     if (p->renderer_type != h->params.renderer_type || p->pt_ray_depth_maximum != h->params.pt_ray_depth_maximum ||
         p->wireframes != h->params.wireframes)
         h->graph_valid = false;
+    h->wide_graph_valid = false;
     h->params = *p;
     int r = push_params(h);
     if (r) return r;
@@ -1050,6 +1284,7 @@ int dfpt_set_strict(dfpt_handle* h, int32_t strict) {
     else h->fast.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
     h->ctx.grid_trace = kset(h).trace_grid(h->ctx.trace_config, h->sms);
     h->graph_valid = false;
+    h->wide_graph_valid = false;
     return DFPT_OK;
 }
 
@@ -1060,12 +1295,25 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->ctx.trace_config = value;
         h->ctx.grid_trace = kset(h).trace_grid(value, h->sms);
         h->graph_valid = false;
+    h->wide_graph_valid = false;
         return DFPT_OK;
+    }
+    if (std::strcmp(key, "wide_samples") == 0) {
+        if (value < 1 || value > 64) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "wide_samples %d outside [1, 64]", value);
+        h->wide_samples = value;
+        return DFPT_OK;
+    }
+    if (std::strcmp(key, "l2_persist") == 0) {
+        h->l2_persist = value != 0;
+        h->graph_valid = false;
+    h->wide_graph_valid = false;
+        return apply_l2_policy(h);
     }
     if (std::strcmp(key, "primitive_culling") == 0) {
         if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
         scene_set_culling(h->sc, value);
         h->graph_valid = false;
+    h->wide_graph_valid = false;
         return DFPT_OK;
     }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
@@ -1076,6 +1324,8 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "trace_config") == 0) { *value = h->ctx.trace_config; return DFPT_OK; }
     if (std::strcmp(key, "trace_configs") == 0) { *value = h->fast.trace_configs; return DFPT_OK; }
     if (std::strcmp(key, "primitive_culling") == 0) { *value = h->sc.scene.use_culling; return DFPT_OK; }
+    if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }
+    if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 
@@ -1108,9 +1358,15 @@ int dfpt_render(dfpt_handle* h, int32_t passes) {
     if (passes < 0) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "passes < 0");
     if (h->counting) CUDA_TRY(cudaMemsetAsync(h->stats.p, 0, 4 * sizeof(unsigned long long), h->stream));
     if (passes == 0) return DFPT_OK;
+    h->events_used = 0;
     {
         int r = ensure_shadow_capacity(h);
         if (r) return r;
+    }
+    if (passes >= 2 && wide_eligible(h)) {
+        int r = render_wide(h, passes - 1);
+        if (r) return r;
+        passes = 1;
     }
     if (h->use_graph && !h->profiling) {
         if (!h->graph_valid) {
@@ -1222,6 +1478,7 @@ int dfpt_diff_forward(dfpt_handle* h, const dfpt_diff_params* dp, int32_t spp, f
     sky.is_sky_active = sky_on;
     sky.is_sun_active = sun_on;
     if ((h->sky.is_sun_active == 1) != (sky.is_sun_active == 1)) h->graph_valid = false;
+    h->wide_graph_valid = false;
     h->sky = sky;
     std::vector<float> tan(4 * DFPT_SKY_FIELDS);
     const double dir[3] = {dp->sun_direction[0], dp->sun_direction[1], dp->sun_direction[2]};
@@ -1250,7 +1507,8 @@ int dfpt_diff_forward(dfpt_handle* h, const dfpt_diff_params* dp, int32_t spp, f
     DevPass& B = h->pass;
     B.vis = h->vis.p; B.diff_L = h->diff_L.p; B.diff_vis = h->diff_vis.p; B.diff_dldi = h->diff_dldi.p;
     B.diff_rows = h->diff_rows.p; B.diff_row_len = row_len;
-    h->graph_valid = false;  // the pass record changed
+    h->graph_valid = false;
+    h->wide_graph_valid = false;  // the pass record changed
     h->diff_on = true;
     h->diff_pass0 = h->host_pass;
     h->diff_spp = spp;
@@ -1305,7 +1563,13 @@ int dfpt_diff_end(dfpt_handle* h) {
     DevPass& B = h->pass;
     B.diff_L = nullptr; B.diff_vis = nullptr; B.diff_rows = nullptr;
     h->graph_valid = false;
+    h->wide_graph_valid = false;
     return push_params(h);
+}
+
+int dfpt_l2_reset(void) {
+    CUDA_TRY(cudaCtxResetPersistingL2Cache());
+    return DFPT_OK;
 }
 
 int dfpt_read_counters(dfpt_handle* h, uint64_t* c4) {

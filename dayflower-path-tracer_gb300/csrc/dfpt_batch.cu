@@ -61,7 +61,7 @@ struct dfpt_batch {
     bool graph_valid = false;
     int graph_kernels = 0;
     uint64_t launches = 0;
-    long long range_host[2] = {0, 0};  // source of the last range copy (pageable: consumed on return)
+    long long range_host[4] = {0, 0, 0, -1};  // wave base, range end, pass of sample 0, clear sample
 };
 
 namespace {
@@ -111,7 +111,7 @@ int batch_prepare(dfpt_batch* b) {
         CUDA_TRY(upload(b->d_run, run, st));
         b->d_wave_tab.release();
         CUDA_TRY(b->d_wave_tab.alloc(4 * ((size_t)n + 1)));
-        if (!b->d_wave_base.p) CUDA_TRY(b->d_wave_base.alloc(2));
+        if (!b->d_wave_base.p) CUDA_TRY(b->d_wave_base.alloc(4));
         if (!b->d_wave_entries.p) CUDA_TRY(b->d_wave_entries.alloc(1));
         if (!b->counts.p) CUDA_TRY(b->counts.alloc(DFPT_COUNTS_SIZE));
         if (!b->pass_index.p) CUDA_TRY(b->pass_index.alloc(1));
@@ -361,7 +361,7 @@ int dfpt_batch_render_range(dfpt_batch* b, int64_t first_sample, int64_t count) 
     if (count == 0) return DFPT_OK;
     b->range_host[0] = first_sample;
     b->range_host[1] = first_sample + count;
-    CUDA_TRY(cudaMemcpyAsync(b->d_wave_base.p, b->range_host, 2 * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+    CUDA_TRY(cudaMemcpyAsync(b->d_wave_base.p, b->range_host, 4 * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
     const long long waves = (count + b->capacity - 1) / b->capacity;
     if (b->use_graph) {
         if (!b->graph_valid) {

@@ -626,6 +626,133 @@ __device__ Hit trace_culled(const DevScene& S, float ox, float oy, float oz, flo
     return h;
 }
 
+// Lane-refill traversal: every lane of a warp carries its own ray through a small state machine
+// (the primitive loop of trace() and the threaded walk of mesh_walk, one node visit per step) and
+// a lane whose ray is finished takes the next ray of the queue while the others go on, so the
+// warp's lanes stay busy until the queue is empty instead of waiting for the slowest of 32 rays.
+// Each ray goes through exactly the operations of trace<ANY, 0> (with the per-primitive box test
+// when the scene selects culling), in the same order, so the results are the same. All 32 lanes call it
+// together. `load(i, o, d)` reads queue entry i, `finish(i, o, d, hit)` consumes its result; the
+// scene comes from `scene(i)` (the kernel's own, or the entry's scene in a batch).
+template <bool ANY, class SceneOf, class Load, class Finish>
+__device__ __forceinline__ void trace_refill(int n, int* fetch, SceneOf scene, Load load, Finish finish, TraceStats& st) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    int idx = -1, prim = 0, node = -1;
+    float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+    float oxo = 0, oyo = 0, ozo = 0, dxo = 0, dyo = 0, dzo = 1, ix = 0, iy = 0, iz = 1;
+    float4 n0 = make_float4(0, 0, 0, 0), n1 = make_float4(0, 0, 0, 0);
+    Hit h;
+    h.t = INF; h.prim = -1; h.shape_type = -1; h.shape_offset = -1;
+    bool exhausted = false;
+    for (;;) {
+        // Refill when at least half the lanes are idle (or all of them).
+        const unsigned idle = __ballot_sync(FULL, idx < 0);
+        if (!exhausted && __popc(idle) >= 16) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(fetch, __popc(idle));
+            base = __shfl_sync(FULL, base, 0);
+            if (base + __popc(idle) >= n) exhausted = true;
+            if (idx < 0) {
+                const int j = base + __popc(idle & ((1u << lane) - 1u));
+                if (j < n) {
+                    idx = j;
+                    load(j, o, d);
+                    prim = 0;
+                    node = -1;
+                    h.t = INF; h.prim = -1; h.shape_type = -1; h.shape_offset = -1;
+                }
+            }
+        }
+        const unsigned busy = __ballot_sync(FULL, idx >= 0);
+        if (busy == 0) {
+            if (exhausted) break;
+            continue;
+        }
+        if (idx < 0) continue;
+        const DevScene& S = scene(idx, d);
+        if (node < 0) {
+            // Between primitives: finish the ray or set up the next primitive.
+            if (prim >= S.primitive_count) {
+                finish(idx, o, d, h);
+                idx = -1;
+                continue;
+            }
+            const int i = prim;
+            if (S.use_culling != 0) {
+                // Box test per primitive (the BVH-candidate mode gives the same hits this way).
+                const float4 lo = __ldg(S.prim_box + 2 * i), hi = __ldg(S.prim_box + 2 * i + 1);
+                if (box_entry(lo, hi, o.x, o.y, o.z, d.x, d.y, d.z, 1.0f / d.x, 1.0f / d.y, 1.0f / d.z) > h.t) {
+                    ++prim;
+                    continue;
+                }
+            }
+            const int4 info = __ldg(S.prim_info + i);
+            if (info.x != DFPT_SHAPE_TRIANGLE_MESH) {
+                if (prim_test<ANY, 0>(S, i, o.x, o.y, o.z, d.x, d.y, d.z, h, st)) {
+                    finish(idx, o, d, h);
+                    idx = -1;
+                    continue;
+                }
+                ++prim;
+                continue;
+            }
+            const float4* W = reinterpret_cast<const float4*>(S.w2o) + i * 4;
+            const float4 r0 = __ldg(W), r1 = __ldg(W + 1), r2 = __ldg(W + 2);
+            oxo = r0.x * o.x + r0.y * o.y + r0.z * o.z + r0.w;
+            oyo = r1.x * o.x + r1.y * o.y + r1.z * o.z + r1.w;
+            ozo = r2.x * o.x + r2.y * o.y + r2.z * o.z + r2.w;
+            dxo = r0.x * d.x + r0.y * d.y + r0.z * d.z;
+            dyo = r1.x * d.x + r1.y * d.y + r1.z * d.z;
+            dzo = r2.x * d.x + r2.y * d.y + r2.z * d.z;
+            ix = 1.0f / dxo; iy = 1.0f / dyo; iz = 1.0f / dzo;
+            node = info.w;
+            n0 = __ldg(S.nodes + 2 * node);
+            n1 = __ldg(S.nodes + 2 * node + 1);
+            continue;
+        }
+        // One node of mesh_walk.
+        st.nodes++;
+        const int next = __float_as_int(n0.w);
+        const int leaf = __float_as_int(n1.w);
+        const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
+        const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
+        const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
+        const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+        const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
+        bool stop = false;
+        if (tb >= 0.0f && leaf != -1) {
+            for (int k = leaf; k >= 0;) {
+                const float4 a = __ldg(S.tris + 3 * k);
+                const float4 e0 = __ldg(S.tris + 3 * k + 1);
+                const float4 e1 = __ldg(S.tris + 3 * k + 2);
+                st.tris++;
+                const float t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, a, e0, e1, h.t);
+                if (t < h.t) {
+                    h.t = t;
+                    h.prim = prim;
+                    h.shape_type = DFPT_SHAPE_TRIANGLE;
+                    h.shape_offset = __float_as_int(a.w);
+                }
+                if (ANY && h.prim != -1) { stop = true; break; }
+                k = __float_as_int(e0.w) != 0 ? -1 : k + 1;
+            }
+        }
+        if (stop) {
+            finish(idx, o, d, h);
+            idx = -1;
+            continue;
+        }
+        node = (tb >= 0.0f && leaf == -1) ? node + 1 : next;
+        if (node < 0) {
+            ++prim;
+        } else {
+            n0 = __ldg(S.nodes + 2 * node);
+            n1 = __ldg(S.nodes + 2 * node + 1);
+        }
+    }
+}
+
 // Closest hit of one ray with the per-lane walk, through the culling structure when the scene has one.
 __device__ __forceinline__ Hit trace_s(const DevScene& S, float ox, float oy, float oz, float dx, float dy, float dz, TraceStats& st) {
     return S.use_culling == 2 ? trace_culled<false, 0>(S, ox, oy, oz, dx, dy, dz, st) : trace<false, 0>(S, ox, oy, oz, dx, dy, dz, st);

@@ -151,8 +151,10 @@ struct DevBatch {
     int capacity;                     // path slots per wave
     long long total;                  // samples of all scenes
     long long* wave_base;             // device: [0] global sample of slot 0 of the current wave,
-                                      //         [1] end of the sample range being rendered
-    int4* slot_key;                   // per slot {scene, pixel, sample, 0}
+                                      // [1] end of the sample range being rendered, [2] RNG pass
+                                      // index of sample 0, [3] sample whose film update replaces
+                                      // the pixel (-1: none)
+    int4* slot_key;                   // per slot {scene, pixel, RNG pass index, 0}
     long long* wave_tab;              // per scene in the wave {scene, local begin, local end, film-task prefix}
     int* wave_entries;                // entries in wave_tab
 };

@@ -505,10 +505,11 @@ template <bool BATCH>
 __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q) {
     const int n = BATCH ? Q.capacity : B.n_pixels;
     const uint32_t pass = BATCH ? 0u : (uint32_t)*B.pass_index;
-    long long base = 0, end = 0;
+    long long base = 0, end = 0, pass0 = 0;
     if constexpr (BATCH) {
         base = Q.wave_base[0];
         end = Q.wave_base[1];
+        pass0 = Q.wave_base[2];
     }
     GRID_STRIDE_UNIFORM(i, n) {
         bool valid = i < n;
@@ -523,8 +524,9 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
                     sid = batch_scene_of(Q, g);
                     const long long local = g - Q.sample_begin[sid];
                     const long long np = (long long)Q.params[sid].width * Q.params[sid].height;
-                    sample = (uint32_t)(local / np);
-                    pixel = (int)(local - (long long)sample * np);
+                    const long long j = local / np;
+                    pixel = (int)(local - j * np);
+                    sample = (uint32_t)(j + pass0);
                     Q.slot_key[i] = make_int4(sid, pixel, (int)sample, 0);
                 }
             }
@@ -566,18 +568,33 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S0, const DevPar
     const int n = B.counts[bounce];
     const float4* __restrict__ qo = B.q_o[which_queue];
     const float4* __restrict__ qd = B.q_d[which_queue];
-    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + bounce) {
+    if constexpr (V == 3) {
         TraceStats st{0, 0};
-        const bool valid = i < n;
-        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
-        if (valid) {
-            o = qo[i];
-            d = qd[i];
+        uint32_t segs = 0;
+        trace_refill<ANY>(
+            n, B.counts + DFPT_COUNTS_FETCH + bounce,
+            [&](int, const float4& d) -> const DevScene& { return scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0); },
+            [&](int i, float4& o, float4& d) { o = qo[i]; d = qd[i]; },
+            [&](int i, const float4&, const float4&, const Hit& h) {
+                B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
+                ++segs;
+            },
+            st);
+        warp_add_stats(P, B.stats, ANY ? 1 : 0, segs, st.nodes, st.tris);
+    } else {
+        WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + bounce) {
+            TraceStats st{0, 0};
+            const bool valid = i < n;
+            float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+            if (valid) {
+                o = qo[i];
+                d = qd[i];
+            }
+            const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
+            const Hit h = trace_v<ANY, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            if (valid) B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
+            warp_add_stats(P, B.stats, ANY ? 1 : 0, valid ? 1u : 0u, st.nodes, st.tris);
         }
-        const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
-        const Hit h = trace_v<ANY, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
-        if (valid) B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
-        warp_add_stats(P, B.stats, ANY ? 1 : 0, valid ? 1u : 0u, st.nodes, st.tris);
     }
 }
 
@@ -830,28 +847,44 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevPa
     const DevParams& P = *Pp;
     const int n = B.counts[DFPT_COUNTS_SHADOW];
     (void)bounce;
-    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1) {
+    // Unoccluded: the pending contribution joins the path radiance. A path has up to one shadow
+    // ray per bounce in this queue, so several threads may add to the same path: atomics (the
+    // sum's order, and so its last bit, may vary).
+    auto unoccluded = [&](int i, const float4& o, const float4& c) {
+        const int path = __float_as_int(o.w);
+        float* L = reinterpret_cast<float*>(B.radiance + path);
+        atomicAdd(L, c.x);
+        atomicAdd(L + 1, c.y);
+        atomicAdd(L + 2, c.z);
+        if (!BATCH && P.diff) atomicOr(B.vis + path, 1 << __float_as_int(c.w));
+    };
+    if constexpr (V == 3) {
         TraceStats st{0, 0};
-        const bool valid = i < n;
-        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
-        if (valid) {
-            o = B.s_o[i];
-            d = B.s_d[i];
+        uint32_t segs = 0;
+        trace_refill<true>(
+            n, B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1,
+            [&](int, const float4& d) -> const DevScene& { return scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0); },
+            [&](int i, float4& o, float4& d) { o = B.s_o[i]; d = B.s_d[i]; },
+            [&](int i, const float4& o, const float4&, const Hit& h) {
+                ++segs;
+                if (h.t >= INF - 0.0001f) unoccluded(i, o, B.s_c[i]);
+            },
+            st);
+        warp_add_stats(P, B.stats, 1, segs, st.nodes, st.tris);
+    } else {
+        WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1) {
+            TraceStats st{0, 0};
+            const bool valid = i < n;
+            float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+            if (valid) {
+                o = B.s_o[i];
+                d = B.s_d[i];
+            }
+            const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
+            const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            if (valid && h.t >= INF - 0.0001f) unoccluded(i, o, B.s_c[i]);
+            warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
         }
-        const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
-        const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
-        if (valid && h.t >= INF - 0.0001f) {
-            // A path has up to one shadow ray per bounce in this queue, so several threads may add
-            // to the same path: atomics (the sum's order, and so its last bit, may vary).
-            const int path = __float_as_int(o.w);
-            const float4 c = B.s_c[i];
-            float* L = reinterpret_cast<float*>(B.radiance + path);
-            atomicAdd(L, c.x);
-            atomicAdd(L + 1, c.y);
-            atomicAdd(L + 2, c.z);
-            if (!BATCH && P.diff) atomicOr(B.vis + path, 1 << __float_as_int(c.w));
-        }
-        warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
     }
 }
 
@@ -861,31 +894,46 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S0, const DevPar
     const DevParams& P0 = *Pp;  // run-wide flags (statistics counting)
     const int n = B.counts[bounce];
     const int qi = bounce & 1;
-    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + bounce) {
-        TraceStats st{0, 0};
-        const bool valid = i < n;
-        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
-        if (valid) {
-            o = B.q_o[qi][i];
-            d = B.q_d[qi][i];
-        }
+    // The continuation escaped: sky, as at a miss.
+    auto escaped = [&](const float4& o, const float4& d) {
         const int sid = BATCH ? __float_as_int(d.w) : 0;
-        const DevScene& S = scene_of<BATCH>(S0, Q, sid);
-        const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
-        if (valid) {
-            const DevParams& P = params_of<BATCH>(Pp, Q, sid);
-            if (!(h.t < INF)) {
-                const int path = __float_as_int(o.w);
-                const float4 T = B.throughput[path];
-                const float3 sky = sky_color(P, d.x, d.y, d.z);
-                float4 L = B.radiance[path];
-                L.x += T.x * sky.x * INV_PI;
-                L.y += T.y * sky.y * INV_PI;
-                L.z += T.z * sky.z * INV_PI;
-                B.radiance[path] = L;
+        const DevParams& P = params_of<BATCH>(Pp, Q, sid);
+        const int path = __float_as_int(o.w);
+        const float4 T = B.throughput[path];
+        const float3 sky = sky_color(P, d.x, d.y, d.z);
+        float4 L = B.radiance[path];
+        L.x += T.x * sky.x * INV_PI;
+        L.y += T.y * sky.y * INV_PI;
+        L.z += T.z * sky.z * INV_PI;
+        B.radiance[path] = L;
+    };
+    if constexpr (V == 3) {
+        TraceStats st{0, 0};
+        uint32_t segs = 0;
+        trace_refill<true>(
+            n, B.counts + DFPT_COUNTS_FETCH + bounce,
+            [&](int, const float4& d) -> const DevScene& { return scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0); },
+            [&](int i, float4& o, float4& d) { o = B.q_o[qi][i]; d = B.q_d[qi][i]; },
+            [&](int, const float4& o, const float4& d, const Hit& h) {
+                ++segs;
+                if (!(h.t < INF)) escaped(o, d);
+            },
+            st);
+        warp_add_stats(P0, B.stats, 1, segs, st.nodes, st.tris);
+    } else {
+        WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + bounce) {
+            TraceStats st{0, 0};
+            const bool valid = i < n;
+            float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+            if (valid) {
+                o = B.q_o[qi][i];
+                d = B.q_d[qi][i];
             }
+            const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
+            const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            if (valid && !(h.t < INF)) escaped(o, d);
+            warp_add_stats(P0, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
         }
-        warp_add_stats(P0, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
     }
 }
 
@@ -1231,6 +1279,7 @@ __global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
     const int E = *Q.wave_entries;
     const long long tasks = Q.wave_tab[4 * E + 3];
     const long long base = Q.wave_base[0];
+    const long long clear_sample = Q.wave_base[3];
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tasks; t += (long long)gridDim.x * blockDim.x) {
         int e = 0;
         while (e + 1 < E && Q.wave_tab[4 * (e + 1) + 3] <= t) ++e;
@@ -1245,7 +1294,7 @@ __global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
         int cnt = B.film_n[f];
         for (long long loc = first; loc < b; loc += np) {
             const int slot = (int)(slot0 + loc);
-            film_add(B.radiance[slot], B.pixel_flags[slot], false, sum, comp, cnt);
+            film_add(B.radiance[slot], B.pixel_flags[slot], loc / np == clear_sample, sum, comp, cnt);
         }
         B.film_sum[f] = sum; B.film_comp[f] = comp; B.film_n[f] = cnt;
     }
@@ -1317,7 +1366,10 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
 // Host-side launchers (the kernel set of this translation unit).
 
 // Tuning configurations of the traversal kernels: {walk variant, block size, resident blocks}.
-#define TRACE_CONFIGS(X) X(0, 0, 256, 4) X(1, 1, 256, 4) X(2, 1, 256, 3) X(3, 0, 128, 8) X(4, 2, 256, 4) X(5, 2, 128, 8) X(6, 2, 256, 3)
+#define TRACE_CONFIGS(X) \
+    X(0, 0, 256, 4) X(1, 1, 256, 4) X(2, 1, 256, 3) X(3, 0, 128, 8) X(4, 2, 256, 4) X(5, 2, 128, 8) X(6, 2, 256, 3) \
+    X(7, 3, 256, 4) X(8, 3, 128, 8) X(9, 3, 256, 3) X(10, 3, 256, 2) \
+    X(11, 0, 256, 6) X(12, 1, 256, 6) X(13, 0, 256, 8) X(14, 1, 256, 8)
 
 template <int V, int BLOCK, int MINB>
 struct TraceCfg {
@@ -1460,7 +1512,7 @@ KernelSet kernel_set() {
     k.init_tables = launch_init_tables;
     k.occupancy = occupancy;
     k.trace_grid = trace_grid;
-    k.trace_configs = 7;
+    k.trace_configs = 15;
 #ifdef DFPT_EXTENDED_KERNELS
     k.b_camera = launch_b_camera;
     k.b_trace_closest = launch_b_closest;

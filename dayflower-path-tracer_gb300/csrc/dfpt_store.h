@@ -70,7 +70,9 @@ struct SceneStore {
     DevBuf<float> point2fs, point3fs, vector3fs, spheres, terrains, textures, surfaces, o2w, w2o, camera;
     DevBuf<int> planes, triangles, primitives;
     DevBuf<int4> prim_info;
-    DevBuf<float4> nodes, tris, sphere4, plane_a, plane_n;
+    DevBuf<float4> trav;  // BVH nodes then triangles, one allocation (one L2 persistence window)
+    size_t trav_nodes = 0;  // float4 records of nodes at the start of trav
+    DevBuf<float4> sphere4, plane_a, plane_n;
     DevBuf<float4> cull_nodes, prim_box;
     DevBuf<int> cull_prims, always;
     std::vector<float> obj_box;      // object-space bound per primitive (culling rebuilds)

@@ -29,6 +29,19 @@ def tune_trace(kernel, passes: int = 4, warmup: int = 1, verbose: bool = False) 
             if verbose:
                 print(f"primitive_culling {mode}: {culling[mode]:.3f} ms/pass", flush=True)
         kernel.set_tuning("primitive_culling", min(culling, key=culling.get))
+    # L2 residency of the traversal records on or off.
+    l2 = {}
+    for mode in (1, 0):
+        kernel.set_tuning("l2_persist", mode)
+        kernel.execute(warmup)
+        kernel.synchronize()
+        t0 = time.perf_counter()
+        kernel.execute(passes)
+        kernel.synchronize()
+        l2[mode] = (time.perf_counter() - t0) / passes * 1e3
+        if verbose:
+            print(f"l2_persist {mode}: {l2[mode]:.3f} ms/pass", flush=True)
+    kernel.set_tuning("l2_persist", min(l2, key=l2.get))
     n = kernel.get_tuning("trace_configs")
     results = {}
     for cfg in range(n):
@@ -43,7 +56,7 @@ def tune_trace(kernel, passes: int = 4, warmup: int = 1, verbose: bool = False) 
             print(f"trace_config {cfg}: {results[cfg]:.3f} ms/pass", flush=True)
     best = min(results, key=results.get)
     kernel.set_tuning("trace_config", best)
-    out = {"best": best, "ms_per_pass": results}
+    out = {"best": best, "ms_per_pass": results, "l2_persist": kernel.get_tuning("l2_persist"), "l2_ms_per_pass": l2}
     if culling:
         out["primitive_culling"] = kernel.get_tuning("primitive_culling")
         out["culling_ms_per_pass"] = culling
@@ -87,3 +100,22 @@ def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=N
     batch.clear()
     return {"best": {"wave_capacity": best[0], "trace_config": best[1]},
             "m_samples_per_s": {f"{k[0]}/{k[1]}": round(v, 2) for k, v in results.items()}}
+
+
+def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16), verbose: bool = False) -> dict:
+    """Picks how many passes run per wave in dfpt_render (1 = one pass at a time) by timing
+    `passes` passes per candidate on the handle's own scene; every choice gives the same film."""
+    results = {}
+    for k in candidates:
+        kernel.set_tuning("wide_samples", k)
+        kernel.execute(passes)
+        kernel.synchronize()
+        t0 = time.perf_counter()
+        kernel.execute(passes)
+        kernel.synchronize()
+        results[k] = (time.perf_counter() - t0) * 1e3
+        if verbose:
+            print(f"wide_samples {k}: {results[k]:.3f} ms / {passes} passes", flush=True)
+    best = min(results, key=results.get)
+    kernel.set_tuning("wide_samples", best)
+    return {"best": best, "ms_per_step": {str(k): round(v, 3) for k, v in results.items()}}

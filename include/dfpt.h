@@ -205,11 +205,20 @@ int dfpt_set_counting(dfpt_handle* handle, int32_t enabled);
 int dfpt_set_profiling(dfpt_handle* handle, int32_t enabled);
 int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind9, int32_t* launches_by_kind9);
 
-/* Launch tuning. Key "trace_config" picks the configuration of the traversal kernels (walk
- * variant x block size x resident blocks per SM, 0..N-1, N readable as "trace_configs"); every
- * configuration visits the same nodes in the same order, so results do not depend on it. */
+/* Launch tuning (no reference counterpart; results never depend on it). Keys:
+ *   "trace_config"      traversal kernel configuration (walk variant x block size x resident
+ *                       blocks per SM, 0..N-1, N readable as "trace_configs"); every configuration
+ *                       visits the same nodes in the same order;
+ *   "primitive_culling" 0 the reference's full primitive loop, 1 a padded world-box test per
+ *                       primitive, 2 candidates from a BVH over those boxes, tested in primitive
+ *                       order (scenes with fewer than 8 bounded primitives always use 0);
+ *   "l2_persist"        1 (default) keeps the BVH nodes and triangles L2-persistent through an
+ *                       access-policy window on the handle's stream; 0 turns it off. */
 int dfpt_set_tuning(dfpt_handle* handle, const char* key, int32_t value);
 int dfpt_get_tuning(dfpt_handle* handle, const char* key, int32_t* value);
+/* Measurement hook (no reference counterpart): returns every persisting L2 line of this process
+ * to normal, as a benchmark's L2 flush between timed steps must. */
+int dfpt_l2_reset(void);
 
 /* Number of kernels the handle launched since it was created (for launch accounting). */
 int dfpt_launch_count(dfpt_handle* handle, uint64_t* launches);

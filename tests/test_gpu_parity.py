@@ -208,3 +208,28 @@ def test_trace_configs_agree(scenes):
             # Shadow contributions of one path are added with float atomics in any order: a few ulps.
             assert np.allclose(got[1], ref[1], rtol=1e-5, atol=1e-6), (cfg, np.abs(got[1] - ref[1]).max())
         cfg += 1
+
+
+@pytest.mark.parametrize("name", ["spheres", "meshes"])
+def test_wide_passes_equal_pass_by_pass(scenes, name):
+    """dfpt_render(h, n) with wide passes (k passes per wave through the batch stages) gives the
+    film of n single passes: same samples per pixel, same Kahan order; float atomics of the sun
+    contributions leave a few ulps (rtol 1e-5). A clear between calls restarts both the same way;
+    the selection buffer and the image come from the last (normal) pass in both."""
+    scene, sky, params, (w, h) = scenes[name]
+    out = []
+    for wide in (1, 8):
+        k = _kernel(scene, sky, dict(params, renderer_type=2), w, h)
+        k.set_tuning("wide_samples", wide)
+        k.execute(13)
+        k.clear()
+        k.execute(11)
+        film, n = k.film()
+        out.append((film.copy(), n.copy(), k.primitive_offsets().copy(), k.get().copy()))
+        k.dispose()
+    (fa, na, pa, ba), (fb, nb, pb, bb) = out
+    assert np.array_equal(na, nb)
+    assert (na == 11).sum() > 0.9 * na.size
+    np.testing.assert_allclose(fa, fb, rtol=1e-5, atol=1e-6)
+    assert np.array_equal(pa, pb)
+    assert np.abs(ba.astype(int) - bb.astype(int)).max() <= 1
