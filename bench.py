@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the inverse-rendering leg")
     ap.add_argument("--adjoint-iters", type=int, default=10)
     ap.add_argument("--trace-config", type=int, default=-1, help="fixed traversal configuration (skips the autotuner)")
+    ap.add_argument("--wide", type=int, default=0, help="fixed passes per wave (skips that tuner)")
     return ap.parse_args()
 
 
@@ -442,7 +443,11 @@ def main():
     k.synchronize()
     from dfpt.autotune import tune_trace, tune_wide
 
-    wide = tune_wide(k, passes=S)
+    if args.wide > 0:
+        k.set_tuning("wide_samples", args.wide)
+        wide = {"best": args.wide, "ms_per_step": {}}
+    else:
+        wide = tune_wide(k, passes=S)
     if args.trace_config >= 0:
         k.set_tuning("trace_config", args.trace_config)
         tuning = {"best": args.trace_config, "ms_per_pass": {}}
@@ -581,6 +586,7 @@ def main():
         "config": {"workload": f"{args.workload} {w}x{h}", "triangles": int(len(scene.triangles) // 12),
                    "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": S, "spp_total": S * args.steps,
                    "wide_samples": wide["best"], "wide_ms_per_step": wide["ms_per_step"],
+                   "ray_sort": wide.get("ray_sort"), "sort_ms_per_step": wide.get("sort_ms_per_step"),
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "scene_build_s": round(t_build, 1), "trace_config": tuning["best"],
                    "primitive_culling": tuning.get("primitive_culling", 0),

@@ -378,7 +378,14 @@ void build_culling(const std::vector<float>& obj, const std::vector<float>& w2o,
         items.push_back(it);
     }
     d.bounded = (int)items.size();
-    if (!items.empty()) build_cull_node(items, 0, (int)items.size(), d);
+    if (!items.empty()) {
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (const CullItem& it : items)
+            for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], it.lo[a]); hi[a] = std::max(hi[a], it.hi[a]); }
+        d.bounds_lo = make_float4(lo[0], lo[1], lo[2], 0);
+        d.bounds_hi = make_float4(hi[0], hi[1], hi[2], 0);
+        build_cull_node(items, 0, (int)items.size(), d);
+    }
     if (d.cull_nodes.empty()) { d.cull_nodes.push_back(make_float4(0, 0, 0, 0)); d.cull_nodes.push_back(make_float4(0, 0, 0, 0)); }
     if (d.cull_prims.empty()) d.cull_prims.push_back(0);
 }
@@ -463,6 +470,8 @@ struct dfpt_handle {
     int wide_graph_kernels = 0;
     long long wide_range[4] = {0, 0, 0, -1};  // wave base, range end, pass of sample 0, clear sample
     int pass_index_host = 0;  // source of pass-index copies (pageable: consumed on return)
+    bool ray_sort = true;     // bin rays between bounces in wide passes
+    DevBuf<int> w_sort_bins;
     uint64_t launches = 0;
     // L2 residency of the traversal records (see apply_l2_policy).
     bool l2_persist = true;
@@ -488,7 +497,7 @@ void release(dfpt_handle* h) {
         for (auto* b : w4) b->release();
         h->w_q_hit.release(); h->w_slot_key.release(); h->w_rng.release(); h->w_pixel_flags.release(); h->w_counts.release();
         h->w_wave_entries.release(); h->w_scene.release(); h->w_sample_begin.release(); h->w_film_begin.release();
-        h->w_wave_base.release(); h->w_wave_tab.release();
+        h->w_wave_base.release(); h->w_wave_tab.release(); h->w_sort_bins.release();
     }
     h->sc.release();
     h->diff_albedo.release(); h->diff_emission.release(); h->diff_L.release(); h->diff_dldi.release();
@@ -669,7 +678,7 @@ bool is_simple_mode(int rt) {
 }
 
 // Kernel kinds reported by dfpt_read_profile.
-enum { KIND_CAMERA, KIND_TRACE, KIND_SHADE, KIND_SHADOW, KIND_FINAL, KIND_SIMPLE, KIND_WIREFRAME, KIND_FILM, KIND_END, KIND_COUNT };
+enum { KIND_CAMERA, KIND_TRACE, KIND_SHADE, KIND_SHADOW, KIND_FINAL, KIND_SIMPLE, KIND_WIREFRAME, KIND_FILM, KIND_END, KIND_SORT, KIND_COUNT };
 
 void mark(dfpt_handle* h, int kind) {
     if (!h->profiling) return;
@@ -767,6 +776,7 @@ int wide_prepare(dfpt_handle* h) {
         CUDA_TRY(h->w_scene.alloc(1));
         CUDA_TRY(h->w_wave_base.alloc(4));
         CUDA_TRY(h->w_wave_tab.alloc(8));
+        CUDA_TRY(h->w_sort_bins.alloc(DFPT_SORT_BINS));
         const std::vector<long long> sb = {0, 1ll << 62}, fb = {0, (long long)n};
         CUDA_TRY(upload(h->w_sample_begin, sb, h->stream));
         CUDA_TRY(upload(h->w_film_begin, fb, h->stream));
@@ -782,6 +792,8 @@ int wide_prepare(dfpt_handle* h) {
     B.throughput = h->w_throughput.p; B.radiance = h->w_radiance.p; B.rng = h->w_rng.p; B.pixel_flags = h->w_pixel_flags.p;
     B.counts = h->w_counts.p; B.stats = h->stats.p; B.pass_index = h->pass_index.p;
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
+    B.sorted_queues = (h->ray_sort && h->fast.b_sort) ? 1 : 0;
+    B.sort_bins = h->w_sort_bins.p;
     DevBatch& Q = h->wq;
     Q.scenes = h->w_scene.p;
     Q.params = h->dev_params.p;
@@ -814,6 +826,7 @@ int issue_wide_wave(dfpt_handle* h) {
     for (int b = 0; b < nb; ++b) {
         mark(h, KIND_TRACE); K.b_trace_closest(c, b); ++k;
         mark(h, KIND_SHADE); K.b_shade(c, b); ++k;
+        if (h->wpass.sorted_queues) { mark(h, KIND_SORT); K.b_sort(c, b); k += 3; }
     }
     mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
     if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.b_shadow(c, 0); ++k; }
@@ -1069,6 +1082,8 @@ int culling_upload(SceneStore& st, const Derived& d, cudaStream_t s) {
     S.cull_nodes = st.cull_nodes.p; S.prim_box = st.prim_box.p; S.cull_prims = st.cull_prims.p;
     S.always = st.always.p;
     S.always_count = (int)d.always.size();
+    S.bounds_lo = d.bounds_lo;
+    S.bounds_hi = d.bounds_hi;
     // Culling is offered for scenes with 8 or more bounded primitives; the default mode is the
     // per-primitive box test, the autotuner may pick the BVH candidates or none.
     st.culling_available = d.bounded >= 8;
@@ -1298,6 +1313,11 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
     h->wide_graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "ray_sort") == 0) {
+        h->ray_sort = value != 0;
+        h->wide_graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "wide_samples") == 0) {
         if (value < 1 || value > 64) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "wide_samples %d outside [1, 64]", value);
         h->wide_samples = value;
@@ -1326,6 +1346,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "primitive_culling") == 0) { *value = h->sc.scene.use_culling; return DFPT_OK; }
     if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
+    if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 

@@ -40,6 +40,7 @@ struct DevScene {
     const int* always;        // unbounded primitives, ascending
     int always_count;
     const float4* prim_box;   // 2 per primitive: padded world bounds lo, hi (unbounded: -/+inf)
+    float4 bounds_lo, bounds_hi;  // union of the bounded primitives' world boxes (ray binning grid)
 };
 #define DFPT_CULL_CANDIDATES 16  // candidates a ray collects before falling back to the full loop
 #define DFPT_CULL_STACK 32
@@ -137,7 +138,12 @@ struct DevPass {
     const float4* diff_dldi;   // per pixel dLoss/dImage (rgb)
     double* diff_rows;         // per block of the adjoint kernels: gradient partials
     int diff_row_len;          // primitives x 7 + 4
+    // Ray binning between bounces (wide passes): with sorted_queues set, shading writes queue 1,
+    // the binning pass moves it to queue 0 in bin order, and every bounce reads queue 0.
+    int sorted_queues;
+    int* sort_bins;            // DFPT_SORT_BINS counters, then exclusive offsets
 };
+#define DFPT_SORT_BINS 4096
 
 // Many scenes rendered by one set of launches. Every scene's samples form one global sequence
 // (scene-major, then sample, then pixel); a wave takes `capacity` consecutive samples of it, one

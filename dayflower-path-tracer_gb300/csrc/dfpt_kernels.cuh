@@ -727,7 +727,7 @@ __device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     const int n = B.counts[bounce];
-    const int qi = bounce & 1;
+    const int qi = B.sorted_queues ? 0 : (bounce & 1);
     const uint32_t pass = BATCH ? 0u : (uint32_t)*B.pass_index;
     GRID_STRIDE_UNIFORM(i, n) {
         bool emit_next = false, emit_shadow = false;
@@ -893,7 +893,7 @@ template <bool BATCH, int V, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     const DevParams& P0 = *Pp;  // run-wide flags (statistics counting)
     const int n = B.counts[bounce];
-    const int qi = bounce & 1;
+    const int qi = B.sorted_queues ? 0 : (bounce & 1);
     // The continuation escaped: sky, as at a miss.
     auto escaped = [&](const float4& o, const float4& d) {
         const int sid = BATCH ? __float_as_int(d.w) : 0;
@@ -1319,6 +1319,81 @@ __global__ void k_bend_wave(DevBatch Q) {
     if (threadIdx.x == 0 && blockIdx.x == 0) Q.wave_base[0] += Q.capacity;
 }
 
+// Ray binning between bounces (one scene): the bin of a ray is its direction octant (3 bits) and
+// its origin's cell in an 8 x 8 x 8 grid over the scene bounds, in Morton order (9 bits). Rays of
+// a bin start near each other and head the same way, so a warp of them walks much the same nodes.
+// Only the processing order changes: every ray keeps its path id and its own result.
+__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d) {
+    int cell = 0;
+    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
+    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
+    const float p[3] = {o.x, o.y, o.z};
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 8.0f;
+        c[a] = u >= 0.0f ? (u < 7.0f ? (int)u : 7) : 0;  // NaN and below: 0
+    }
+    for (int b = 0; b < 3; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
+    const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
+    return (oct << 9) | cell;
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(DevBatch Q, DevPass B, int bounce) {
+    __shared__ int h[DFPT_SORT_BINS];
+    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    const int n = B.counts[bounce + 1];
+    const DevScene& S = Q.scenes[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(h + ray_bin(S, B.q_o[1][i], B.q_d[1][i]), 1);
+    __syncthreads();
+    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x)
+        if (h[k]) atomicAdd(B.sort_bins + k, h[k]);
+}
+
+// Exclusive scan of the bin counts (one block of 1024 threads, 4 bins each).
+__global__ void __launch_bounds__(1024) k_sort_scan(DevPass B) {
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    int v[4], sum = 0;
+    for (int j = 0; j < 4; ++j) { v[j] = B.sort_bins[4 * t + j]; sum += v[j]; }
+    part[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int x = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    int run = part[t] - sum;
+    for (int j = 0; j < 4; ++j) { B.sort_bins[4 * t + j] = run; run += v[j]; }
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(DevBatch Q, DevPass B, int bounce) {
+    const int n = B.counts[bounce + 1];
+    const DevScene& S = Q.scenes[0];
+    GRID_STRIDE_UNIFORM(i, n) {
+        int key = -1;
+        float4 o, d;
+        if (i < n) {
+            o = B.q_o[1][i];
+            d = B.q_d[1][i];
+            key = ray_bin(S, o, d);
+        }
+        // Lanes with the same bin take consecutive places with one atomic.
+        const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
+        const int leader = __ffs(same) - 1;
+        int base = 0;
+        if (key >= 0 && (int)(threadIdx.x & 31) == leader) base = atomicAdd(B.sort_bins + key, __popc(same));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (key >= 0) {
+            const int pos = base + __popc(same & ((1u << (threadIdx.x & 31)) - 1u));
+            B.q_o[0][pos] = o;
+            B.q_d[0][pos] = d;
+        }
+    }
+}
+
 // FP64 mean of the film average (AIK film semantics: sum / samples per pixel).
 __global__ void __launch_bounds__(256) k_film_mean(DevPass B, double* out3) {
     double r = 0.0, g = 0.0, b = 0.0;
@@ -1374,7 +1449,7 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
 template <int V, int BLOCK, int MINB>
 struct TraceCfg {
     static void closest(const LaunchCtx& c, int bounce) {
-        k_trace<false, false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce, bounce & 1);
+        k_trace<false, false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce, c.pass->sorted_queues ? 0 : (bounce & 1));
     }
     static void shadow(const LaunchCtx& c, int bounce) {
         k_shadow<false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce);
@@ -1391,7 +1466,7 @@ struct TraceCfg {
     // Batch traversal: per-lane walks only (a warp may hold rays of several scenes).
     static constexpr int BV = V == 2 ? 1 : V;
     static void b_closest(const LaunchCtx& c, int bounce) {
-        k_trace<true, false, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce, bounce & 1);
+        k_trace<true, false, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce, c.pass->sorted_queues ? 0 : (bounce & 1));
     }
     static void b_shadow(const LaunchCtx& c, int bounce) {
         k_shadow<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce);
@@ -1462,6 +1537,13 @@ static void launch_b_wave(const LaunchCtx& c, int) { k_bwave<<<1, 32, 0, c.strea
 static void launch_b_film(const LaunchCtx& c, int) { k_bfilm<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_resolve(const LaunchCtx& c, int) { k_bresolve<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_end(const LaunchCtx& c, int) { k_bend_wave<<<1, 32, 0, c.stream>>>(*c.batch); }
+// Bins the rays shading queued for bounce + 1 (queue 1 -> queue 0); one scene.
+static void launch_b_sort(const LaunchCtx& c, int bounce) {
+    cudaMemsetAsync(c.pass->sort_bins, 0, DFPT_SORT_BINS * sizeof(int), c.stream);
+    k_sort_hist<<<(c.grid + 3) / 4, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
+    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass);
+    k_sort_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
+}
 
 // Path-replay adjoint. Per-primitive partials live in shared memory when they fit in 44 KB.
 static void launch_shade_adj(const LaunchCtx& c, int bounce) {
@@ -1523,6 +1605,7 @@ KernelSet kernel_set() {
     k.b_film = launch_b_film;
     k.b_resolve = launch_b_resolve;
     k.b_end = launch_b_end;
+    k.b_sort = launch_b_sort;
     k.shade_adj = launch_shade_adj;
     k.final_adj = launch_final_adj;
     k.diff_reduce = launch_diff_reduce;

@@ -41,6 +41,7 @@ struct KernelSet {
     void (*b_film)(const LaunchCtx&, int) = nullptr;
     void (*b_resolve)(const LaunchCtx&, int) = nullptr;
     void (*b_end)(const LaunchCtx&, int) = nullptr;
+    void (*b_sort)(const LaunchCtx&, int bounce) = nullptr;  // ray binning (one scene, sorted queues)
     // Path-replay adjoint (the fast kernel set only).
     void (*shade_adj)(const LaunchCtx&, int bounce) = nullptr;
     void (*final_adj)(const LaunchCtx&, int bounce) = nullptr;

@@ -61,6 +61,7 @@ struct Derived {
     std::vector<float4> cull_nodes, prim_box;
     std::vector<int> cull_prims, always;
     int bounded = 0;  // primitives with a world box
+    float4 bounds_lo = make_float4(-1.0e4f, -1.0e4f, -1.0e4f, 0), bounds_hi = make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0);
 };
 
 // One validated compiled scene: the host copy, its device arrays and the kernel-side view.

@@ -118,4 +118,16 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16), verbose: bool 
             print(f"wide_samples {k}: {results[k]:.3f} ms / {passes} passes", flush=True)
     best = min(results, key=results.get)
     kernel.set_tuning("wide_samples", best)
-    return {"best": best, "ms_per_step": {str(k): round(v, 3) for k, v in results.items()}}
+    sort = {}
+    if best > 1:
+        for mode in (1, 0):
+            kernel.set_tuning("ray_sort", mode)
+            kernel.execute(passes)
+            kernel.synchronize()
+            t0 = time.perf_counter()
+            kernel.execute(passes)
+            kernel.synchronize()
+            sort[mode] = (time.perf_counter() - t0) * 1e3
+        kernel.set_tuning("ray_sort", min(sort, key=sort.get))
+    return {"best": best, "ms_per_step": {str(k): round(v, 3) for k, v in results.items()},
+            "ray_sort": kernel.get_tuning("ray_sort"), "sort_ms_per_step": {str(k): round(v, 3) for k, v in sort.items()}}

@@ -156,14 +156,14 @@ class RendererKernel:
         check(self._lib.dfpt_read_counters(self._need(), ptr(c, C.c_uint64)))
         return c
 
-    PROFILE_KINDS = ("camera", "trace", "shade", "shadow", "final", "simple", "wireframe", "film", "end")
+    PROFILE_KINDS = ("camera", "trace", "shade", "shadow", "final", "simple", "wireframe", "film", "end", "sort")
 
     def set_profiling(self, enabled: bool) -> None:
         check(self._lib.dfpt_set_profiling(self._need(), 1 if enabled else 0))
 
     def read_profile(self) -> dict:
-        ms = np.zeros(9, np.float64)
-        n = np.zeros(9, np.int32)
+        ms = np.zeros(len(self.PROFILE_KINDS), np.float64)
+        n = np.zeros(len(self.PROFILE_KINDS), np.int32)
         check(self._lib.dfpt_read_profile(self._need(), ptr(ms, C.c_double), ptr(n, C.c_int32)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PROFILE_KINDS)}
 

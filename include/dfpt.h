@@ -198,12 +198,12 @@ int dfpt_read_counters(dfpt_handle* handle, uint64_t* counters4);
 /* Enables (1) or disables (0, the default) the traversal counters; counting costs atomics. */
 int dfpt_set_counting(dfpt_handle* handle, int32_t enabled);
 
-/* Per-kernel timing of the last pass: when enabled, passes are issued as direct launches with a
- * CUDA event between kernels (no graph), and dfpt_read_profile returns, per kernel kind
- * (0 camera, 1 trace closest, 2 shade, 3 shadow, 4 final any-hit, 5 per-pixel modes,
- * 6 wireframe, 7 film, 8 end of pass), the milliseconds and the launch count of the last pass. */
+/* Per-kernel timing of the last dfpt_render call: when enabled, passes are issued as direct
+ * launches with a CUDA event between kernels (no graph), and dfpt_read_profile returns, per kernel
+ * kind (0 camera, 1 trace closest, 2 shade, 3 shadow, 4 final any-hit, 5 per-pixel modes,
+ * 6 wireframe, 7 film, 8 end of pass, 9 ray binning), the milliseconds and the launch count. */
 int dfpt_set_profiling(dfpt_handle* handle, int32_t enabled);
-int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind9, int32_t* launches_by_kind9);
+int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launches_by_kind10);
 
 /* Launch tuning (no reference counterpart; results never depend on it). Keys:
  *   "trace_config"      traversal kernel configuration (walk variant x block size x resident
@@ -213,7 +213,11 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind9, int32_t* launche
  *                       primitive, 2 candidates from a BVH over those boxes, tested in primitive
  *                       order (scenes with fewer than 8 bounded primitives always use 0);
  *   "l2_persist"        1 (default) keeps the BVH nodes and triangles L2-persistent through an
- *                       access-policy window on the handle's stream; 0 turns it off. */
+ *                       access-policy window on the handle's stream; 0 turns it off;
+ *   "wide_samples"      passes per wave when dfpt_render renders several passes (1..64, default
+ *                       8; 1 renders pass by pass); the film is the same either way;
+ *   "ray_sort"          1 (default) bins rays by origin cell and direction octant between the
+ *                       bounces of wide passes (processing order only). */
 int dfpt_set_tuning(dfpt_handle* handle, const char* key, int32_t value);
 int dfpt_get_tuning(dfpt_handle* handle, const char* key, int32_t* value);
 /* Measurement hook (no reference counterpart): returns every persisting L2 line of this process
