@@ -472,6 +472,9 @@ struct dfpt_handle {
     int pass_index_host = 0;  // source of pass-index copies (pageable: consumed on return)
     bool ray_sort = true;     // bin rays between bounces in wide passes
     DevBuf<int> w_sort_bins;
+    DevBuf<float4> w_s2_o, w_s2_d, w_s2_c;  // the binned copy of the shadow queue
+    DevPass wpass_shadow{};                  // wpass with the shadow queue pointing at the copy
+    LaunchCtx wctx_shadow{};
     uint64_t launches = 0;
     // L2 residency of the traversal records (see apply_l2_policy).
     bool l2_persist = true;
@@ -498,6 +501,7 @@ void release(dfpt_handle* h) {
         h->w_q_hit.release(); h->w_slot_key.release(); h->w_rng.release(); h->w_pixel_flags.release(); h->w_counts.release();
         h->w_wave_entries.release(); h->w_scene.release(); h->w_sample_begin.release(); h->w_film_begin.release();
         h->w_wave_base.release(); h->w_wave_tab.release(); h->w_sort_bins.release();
+        h->w_s2_o.release(); h->w_s2_d.release(); h->w_s2_c.release();
     }
     h->sc.release();
     h->diff_albedo.release(); h->diff_emission.release(); h->diff_L.release(); h->diff_dldi.release();
@@ -766,6 +770,7 @@ int wide_prepare(dfpt_handle* h) {
         CUDA_TRY(h->w_q_hit.alloc(c)); CUDA_TRY(h->w_slot_key.alloc(c));
         CUDA_TRY(h->w_throughput.alloc(c)); CUDA_TRY(h->w_radiance.alloc(c)); CUDA_TRY(h->w_rng.alloc(c)); CUDA_TRY(h->w_pixel_flags.alloc(c));
         CUDA_TRY(h->w_s_o.alloc(shadow)); CUDA_TRY(h->w_s_d.alloc(shadow)); CUDA_TRY(h->w_s_c.alloc(shadow));
+        h->w_s2_o.release(); h->w_s2_d.release(); h->w_s2_c.release();
         h->wide_capacity = cap;
         h->wide_shadow = shadow;
         h->wide_graph_valid = false;
@@ -794,6 +799,17 @@ int wide_prepare(dfpt_handle* h) {
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
     B.sorted_queues = (h->ray_sort && h->fast.b_sort) ? 1 : 0;
     B.sort_bins = h->w_sort_bins.p;
+    if (B.sorted_queues && !h->w_s2_o.p) {
+        CUDA_TRY(h->w_s2_o.alloc(h->wide_shadow));
+        CUDA_TRY(h->w_s2_d.alloc(h->wide_shadow));
+        CUDA_TRY(h->w_s2_c.alloc(h->wide_shadow));
+    }
+    h->wpass_shadow = B;
+    if (B.sorted_queues) {
+        h->wpass_shadow.s_o = h->w_s2_o.p;
+        h->wpass_shadow.s_d = h->w_s2_d.p;
+        h->wpass_shadow.s_c = h->w_s2_c.p;
+    }
     DevBatch& Q = h->wq;
     Q.scenes = h->w_scene.p;
     Q.params = h->dev_params.p;
@@ -811,6 +827,8 @@ int wide_prepare(dfpt_handle* h) {
     c.scene = nullptr;
     c.pass = &h->wpass;
     c.batch = &h->wq;
+    h->wctx_shadow = c;
+    h->wctx_shadow.pass = &h->wpass_shadow;
     return DFPT_OK;
 }
 
@@ -829,7 +847,14 @@ int issue_wide_wave(dfpt_handle* h) {
         if (h->wpass.sorted_queues) { mark(h, KIND_SORT); K.b_sort(c, b); k += 3; }
     }
     mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
-    if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.b_shadow(c, 0); ++k; }
+    if (h->sky.is_sun_active == 1) {
+        if (h->wpass.sorted_queues && K.b_sort_shadow) {
+            mark(h, KIND_SORT); K.b_sort_shadow(c, h->wpass_shadow); k += 3;
+            mark(h, KIND_SHADOW); K.b_shadow(h->wctx_shadow, 0); ++k;
+        } else {
+            mark(h, KIND_SHADOW); K.b_shadow(c, 0); ++k;
+        }
+    }
     mark(h, KIND_FILM); K.b_film(c, 0); ++k;
     mark(h, KIND_END); K.b_end(c, 0); ++k;
     mark(h, KIND_COUNT);

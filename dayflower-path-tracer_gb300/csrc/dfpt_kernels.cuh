@@ -1351,6 +1351,61 @@ __global__ void __launch_bounds__(256) k_sort_hist(DevBatch Q, DevPass B, int bo
         if (h[k]) atomicAdd(B.sort_bins + k, h[k]);
 }
 
+// Shadow rays all head for the sun: their bin is the origin's cell in a 16 x 16 x 16 grid over the
+// scene bounds (Morton order, 12 bits).
+__device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
+    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
+    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
+    const float p[3] = {o.x, o.y, o.z};
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 16.0f;
+        c[a] = u >= 0.0f ? (u < 15.0f ? (int)u : 15) : 0;
+    }
+    int cell = 0;
+    for (int b = 0; b < 4; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
+    return cell;
+}
+
+__global__ void __launch_bounds__(256) k_sort_shadow_hist(DevBatch Q, DevPass B) {
+    __shared__ int h[DFPT_SORT_BINS];
+    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    const int n = B.counts[DFPT_COUNTS_SHADOW];
+    const DevScene& S = Q.scenes[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(h + shadow_bin(S, B.s_o[i]), 1);
+    __syncthreads();
+    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x)
+        if (h[k]) atomicAdd(B.sort_bins + k, h[k]);
+}
+
+// Moves the shadow queue (B.s_*) into the second set (out) in bin order.
+__global__ void __launch_bounds__(256) k_sort_shadow_scatter(DevBatch Q, DevPass B, float4* out_o, float4* out_d, float4* out_c) {
+    const int n = B.counts[DFPT_COUNTS_SHADOW];
+    const DevScene& S = Q.scenes[0];
+    GRID_STRIDE_UNIFORM(i, n) {
+        int key = -1;
+        float4 o, d, c;
+        if (i < n) {
+            o = B.s_o[i];
+            d = B.s_d[i];
+            c = B.s_c[i];
+            key = shadow_bin(S, o);
+        }
+        const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
+        const int leader = __ffs(same) - 1;
+        int base = 0;
+        if (key >= 0 && (int)(threadIdx.x & 31) == leader) base = atomicAdd(B.sort_bins + key, __popc(same));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (key >= 0) {
+            const int pos = base + __popc(same & ((1u << (threadIdx.x & 31)) - 1u));
+            out_o[pos] = o;
+            out_d[pos] = d;
+            out_c[pos] = c;
+        }
+    }
+}
+
 // Exclusive scan of the bin counts (one block of 1024 threads, 4 bins each).
 __global__ void __launch_bounds__(1024) k_sort_scan(DevPass B) {
     __shared__ int part[1024];
@@ -1544,6 +1599,13 @@ static void launch_b_sort(const LaunchCtx& c, int bounce) {
     k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass);
     k_sort_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
 }
+// Bins the deferred shadow queue into `to` (a pass record whose s_* point at the second set).
+static void launch_b_sort_shadow(const LaunchCtx& c, const DevPass& to) {
+    cudaMemsetAsync(c.pass->sort_bins, 0, DFPT_SORT_BINS * sizeof(int), c.stream);
+    k_sort_shadow_hist<<<(c.grid + 3) / 4, 256, 0, c.stream>>>(*c.batch, *c.pass);
+    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass);
+    k_sort_shadow_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, to.s_o, to.s_d, to.s_c);
+}
 
 // Path-replay adjoint. Per-primitive partials live in shared memory when they fit in 44 KB.
 static void launch_shade_adj(const LaunchCtx& c, int bounce) {
@@ -1606,6 +1668,7 @@ KernelSet kernel_set() {
     k.b_resolve = launch_b_resolve;
     k.b_end = launch_b_end;
     k.b_sort = launch_b_sort;
+    k.b_sort_shadow = launch_b_sort_shadow;
     k.shade_adj = launch_shade_adj;
     k.final_adj = launch_final_adj;
     k.diff_reduce = launch_diff_reduce;
