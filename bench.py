@@ -239,13 +239,16 @@ def batch_leg(args, stream, torch, barrier, dist, world):
     barrier()
     batch_launches = b.launch_count() - launches0
 
+    # Sequential single-scene renders, (a) pass by pass (the plain kernel: one launch sequence per
+    # pass) and (b) with the handle's wide passes (8 passes per wave).
     handles = []
     for x in work:
         k = RendererKernel(x["scene"], x["sky"], x["params"])
         k.update(x["width"], x["height"])
         k.set_stream(stream.cuda_stream)
         k.set_tuning("trace_config", tuning["best"]["trace_config"])
-        k.execute(1)  # builds the pass graph
+        k.set_tuning("wide_samples", 1)
+        k.execute(2)  # builds the pass graph
         handles.append(k)
     torch.cuda.synchronize()
 
@@ -256,6 +259,13 @@ def batch_leg(args, stream, torch, barrier, dist, world):
 
     barrier()
     seq_s = timed(sequential)
+    barrier()
+    for k in handles:
+        k.set_tuning("wide_samples", 8)
+        k.execute(9)  # builds the wave graph
+    torch.cuda.synchronize()
+    barrier()
+    seq_wide_s = timed(sequential)
     barrier()
     for k in handles:
         k.dispose()
@@ -276,13 +286,16 @@ def batch_leg(args, stream, torch, barrier, dist, world):
         worst = max(worst, float(np.max(np.abs(fb - fs) / (np.abs(fs) + 1e-3))))
     b.dispose()
     if dist is not None:
-        t = torch.tensor([batch_s, seq_s], device="cuda")
+        t = torch.tensor([batch_s, seq_s, seq_wide_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        batch_s, seq_s = (float(v) for v in t.tolist())
+        batch_s, seq_s, seq_wide_s = (float(v) for v in t.tolist())
     n = len(work)
     return {
         "metric": "scenes/s", "value": world * n / batch_s, "sequential_value": world * n / seq_s,
         "speedup_vs_sequential": seq_s / batch_s, "samples": samples,
+        "sequential_wide_value": world * n / seq_wide_s, "speedup_vs_sequential_wide": seq_wide_s / batch_s,
+        "sequential": "64 RendererKernel handles on one stream, clear + dfpt_render(spp) each: pass by pass "
+                      "(wide_samples 1, the plain kernel) and with 8-pass waves (sequential_wide_*)",
         "m_samples_per_s": world * samples / batch_s / 1e6, "sequential_m_samples_per_s": world * samples / seq_s / 1e6,
         "batch_s": batch_s, "sequential_s": seq_s, "gpu_launches": int(batch_launches),
         "triangles_total": sum(x["triangles"] for x in work), "scenes": n, "scene_build_s": round(build_s, 1),
@@ -587,6 +600,7 @@ def main():
                    "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": S, "spp_total": S * args.steps,
                    "wide_samples": wide["best"], "wide_ms_per_step": wide["ms_per_step"],
                    "ray_sort": wide.get("ray_sort"), "sort_ms_per_step": wide.get("sort_ms_per_step"),
+                   "shadow_defer": wide.get("shadow_defer"), "defer_ms_per_step": wide.get("defer_ms_per_step"),
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "scene_build_s": round(t_build, 1), "trace_config": tuning["best"],
                    "primitive_culling": tuning.get("primitive_culling", 0),

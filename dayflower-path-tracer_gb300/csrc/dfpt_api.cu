@@ -471,6 +471,7 @@ struct dfpt_handle {
     long long wide_range[4] = {0, 0, 0, -1};  // wave base, range end, pass of sample 0, clear sample
     int pass_index_host = 0;  // source of pass-index copies (pageable: consumed on return)
     bool ray_sort = true;     // bin rays between bounces in wide passes
+    bool shadow_defer = false;  // wide passes: one shadow launch per wave (queue of slots x depth)
     DevBuf<int> w_sort_bins;
     DevBuf<float4> w_s2_o, w_s2_d, w_s2_c;  // the binned copy of the shadow queue
     DevPass wpass_shadow{};                  // wpass with the shadow queue pointing at the copy
@@ -760,7 +761,8 @@ bool wide_eligible(const dfpt_handle* h) {
 int wide_prepare(dfpt_handle* h) {
     const size_t n = (size_t)h->n_pixels;
     const int cap = (int)std::min<size_t>((size_t)h->wide_samples * n, (size_t)1 << 27);
-    const size_t shadow = (size_t)cap * (size_t)bounces_of(h);
+    // One bounce of shadow rays (traced before the next bounce), or every bounce's when deferred.
+    const size_t shadow = (size_t)cap * (size_t)(h->shadow_defer ? bounces_of(h) : 1);
     if (cap != h->wide_capacity || shadow != h->wide_shadow) {
         DevBuf<float4>* w4[] = {&h->w_q_o0, &h->w_q_o1, &h->w_q_d0, &h->w_q_d1, &h->w_s_o, &h->w_s_d, &h->w_s_c, &h->w_throughput, &h->w_radiance};
         for (auto* b : w4) b->release();
@@ -841,20 +843,26 @@ int issue_wide_wave(dfpt_handle* h) {
     K.b_wave(c, 0); ++k;
     mark(h, KIND_CAMERA); K.b_camera(c, 0); ++k;
     const int nb = bounces_of(h);
-    for (int b = 0; b < nb; ++b) {
-        mark(h, KIND_TRACE); K.b_trace_closest(c, b); ++k;
-        mark(h, KIND_SHADE); K.b_shade(c, b); ++k;
-        if (h->wpass.sorted_queues) { mark(h, KIND_SORT); K.b_sort(c, b); k += 3; }
-    }
-    mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
-    if (h->sky.is_sun_active == 1) {
-        if (h->wpass.sorted_queues && K.b_sort_shadow) {
+    // Sun shadow rays: traced right after each bounce's shading (the queue holds one bounce), or,
+    // with shadow_defer, all bounces' at once after the last bounce (queue of slots x depth).
+    auto shadows = [&]() {
+        if (h->sky.is_sun_active != 1) return;
+        if (h->wpass.sorted_queues) {
             mark(h, KIND_SORT); K.b_sort_shadow(c, h->wpass_shadow); k += 3;
             mark(h, KIND_SHADOW); K.b_shadow(h->wctx_shadow, 0); ++k;
         } else {
             mark(h, KIND_SHADOW); K.b_shadow(c, 0); ++k;
         }
+        mark(h, KIND_END); K.b_shadow_reset(c, 0); ++k;
+    };
+    for (int b = 0; b < nb; ++b) {
+        mark(h, KIND_TRACE); K.b_trace_closest(c, b); ++k;
+        mark(h, KIND_SHADE); K.b_shade(c, b); ++k;
+        if (h->wpass.sorted_queues) { mark(h, KIND_SORT); K.b_sort(c, b); k += 3; }
+        if (!h->shadow_defer) shadows();
     }
+    mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
+    if (h->shadow_defer) shadows();
     mark(h, KIND_FILM); K.b_film(c, 0); ++k;
     mark(h, KIND_END); K.b_end(c, 0); ++k;
     mark(h, KIND_COUNT);
@@ -1343,6 +1351,11 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->wide_graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "shadow_defer") == 0) {
+        h->shadow_defer = value != 0;
+        h->wide_graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "wide_samples") == 0) {
         if (value < 1 || value > 64) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "wide_samples %d outside [1, 64]", value);
         h->wide_samples = value;
@@ -1372,6 +1385,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
+    if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 

@@ -5,7 +5,7 @@
 // All samples of all scenes form one global sequence (scene-major, then sample, then pixel). A wave
 // takes `wave_capacity` consecutive samples of it - one path slot each, whatever scenes they belong
 // to - and runs the path tracer's stages over them, one launch per stage:
-//   wave table -> camera -> [trace closest -> shade] x depth -> final any-hit -> sun shadow rays ->
+//   wave table -> camera -> [trace closest -> shade -> sun shadow rays] x depth -> final any-hit ->
 //   film -> advance
 // captured once as a CUDA graph and replayed per wave. A pixel's samples enter its film in sample
 // order, so each scene's film is the one a single-scene handle gives after `spp` passes with the
@@ -62,6 +62,12 @@ struct dfpt_batch {
     int graph_kernels = 0;
     uint64_t launches = 0;
     long long range_host[4] = {0, 0, 0, -1};  // wave base, range end, pass of sample 0, clear sample
+    // Ray binning between bounces and before the shadow launch (same scheme as wide passes).
+    bool ray_sort = true;
+    DevBuf<int> sort_bins;
+    DevBuf<float4> s2_o, s2_d, s2_c;
+    DevPass pass_shadow{};
+    LaunchCtx ctx_shadow{};
 };
 
 namespace {
@@ -73,6 +79,7 @@ void batch_release_buffers(dfpt_batch* b) {
     b->slot_key.release();
     b->rng.release();
     b->pixel_flags.release();
+    b->s2_o.release(); b->s2_d.release(); b->s2_c.release();
     b->capacity = 0;
     b->shadow_slots = 0;
 }
@@ -88,6 +95,7 @@ void batch_release(dfpt_batch* b) {
     b->d_scenes.release(); b->d_params.release(); b->d_run.release();
     b->d_sample_begin.release(); b->d_film_begin.release(); b->d_wave_base.release(); b->d_wave_tab.release();
     b->d_wave_entries.release();
+    b->sort_bins.release();
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     b->stream = nullptr;
 }
@@ -133,14 +141,14 @@ int batch_prepare(dfpt_batch* b) {
     }
     const long long want = std::min<long long>(b->capacity_request, total_samples(b));
     const int cap = (int)std::max<long long>(want, 1);
-    const size_t shadow = (size_t)cap * (size_t)b->depth;
+    const size_t shadow = (size_t)cap;  // one bounce of shadow rays (traced before the next bounce)
     if (cap != b->capacity || shadow != b->shadow_slots) {
         batch_release_buffers(b);
         const size_t c = (size_t)cap;
         CUDA_TRY(b->q_o0.alloc(c)); CUDA_TRY(b->q_o1.alloc(c)); CUDA_TRY(b->q_d0.alloc(c)); CUDA_TRY(b->q_d1.alloc(c));
         CUDA_TRY(b->q_hit.alloc(c)); CUDA_TRY(b->slot_key.alloc(c));
         CUDA_TRY(b->throughput.alloc(c)); CUDA_TRY(b->radiance.alloc(c)); CUDA_TRY(b->rng.alloc(c)); CUDA_TRY(b->pixel_flags.alloc(c));
-        // Each path leaves at most one sun shadow ray per bounce.
+        // Each path leaves at most one sun shadow ray per bounce; a bounce's are traced at once.
         CUDA_TRY(b->s_o.alloc(shadow)); CUDA_TRY(b->s_d.alloc(shadow)); CUDA_TRY(b->s_c.alloc(shadow));
         b->capacity = cap;
         b->shadow_slots = shadow;
@@ -154,6 +162,22 @@ int batch_prepare(dfpt_batch* b) {
     B.throughput = b->throughput.p; B.radiance = b->radiance.p; B.rng = b->rng.p; B.pixel_flags = b->pixel_flags.p;
     B.counts = b->counts.p; B.stats = b->stats.p; B.pass_index = b->pass_index.p;
     B.film_sum = b->film_sum.p; B.film_comp = b->film_comp.p; B.film_n = b->film_n.p; B.bgra = b->bgra.p;
+    B.sorted_queues = (b->ray_sort && b->ks.b_sort) ? 1 : 0;
+    if (B.sorted_queues) {
+        if (!b->sort_bins.p) CUDA_TRY(b->sort_bins.alloc(DFPT_SORT_BINS));
+        if (!b->s2_o.p) {
+            CUDA_TRY(b->s2_o.alloc(b->shadow_slots));
+            CUDA_TRY(b->s2_d.alloc(b->shadow_slots));
+            CUDA_TRY(b->s2_c.alloc(b->shadow_slots));
+        }
+    }
+    B.sort_bins = b->sort_bins.p;
+    b->pass_shadow = B;
+    if (B.sorted_queues) {
+        b->pass_shadow.s_o = b->s2_o.p;
+        b->pass_shadow.s_d = b->s2_d.p;
+        b->pass_shadow.s_c = b->s2_c.p;
+    }
     DevBatch& Q = b->Q;
     Q.scenes = b->d_scenes.p;
     Q.params = b->d_params.p;
@@ -175,6 +199,8 @@ int batch_prepare(dfpt_batch* b) {
     b->ks.occupancy(b->sms, c.grid, c.grid_trace, c.grid_simple);
     c.trace_config = b->trace_config;
     c.grid_trace = b->ks.trace_grid(b->trace_config, b->sms);
+    b->ctx_shadow = c;
+    b->ctx_shadow.pass = &b->pass_shadow;
     return DFPT_OK;
 }
 
@@ -189,9 +215,18 @@ int issue_wave(dfpt_batch* b) {
     for (int i = 0; i < b->depth; ++i) {
         K.b_trace_closest(c, i); ++k;
         K.b_shade(c, i); ++k;
+        if (b->pass.sorted_queues) { K.b_sort(c, i); k += 3; }
+        if (b->any_sun) {
+            if (b->pass.sorted_queues) {
+                K.b_sort_shadow(c, b->pass_shadow); k += 3;
+                K.b_shadow(b->ctx_shadow, 0); ++k;
+            } else {
+                K.b_shadow(c, 0); ++k;
+            }
+            K.b_shadow_reset(c, 0); ++k;
+        }
     }
     K.b_final(c, b->depth); ++k;
-    if (b->any_sun) { K.b_shadow(c, 0); ++k; }
     K.b_film(c, 0); ++k;
     K.b_end(c, 0); ++k;
     return k;
@@ -319,6 +354,8 @@ int dfpt_batch_set_tuning(dfpt_batch* b, const char* key, int64_t value) {
         b->trace_config = (int)value;
     } else if (k == "graphs") {
         b->use_graph = value != 0;
+    } else if (k == "ray_sort") {
+        b->ray_sort = value != 0;
     } else {
         return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
     }
@@ -333,6 +370,7 @@ int dfpt_batch_get_tuning(dfpt_batch* b, const char* key, int64_t* value) {
     else if (k == "trace_config") *value = b->trace_config;
     else if (k == "trace_configs") *value = b->ks.trace_configs;
     else if (k == "graphs") *value = b->use_graph ? 1 : 0;
+    else if (k == "ray_sort") *value = b->ray_sort ? 1 : 0;
     else if (k == "scenes") *value = (int64_t)b->stores.size();
     else if (k == "total_samples") *value = total_samples(b);
     else if (k == "depth") *value = b->depth;

@@ -143,7 +143,7 @@ struct DevPass {
     int sorted_queues;
     int* sort_bins;            // DFPT_SORT_BINS counters, then exclusive offsets
 };
-#define DFPT_SORT_BINS 4096
+#define DFPT_SORT_BINS 16384  // 2 bits of scene (within a wave) x 3 bits of octant x 9 bits of cell
 
 // Many scenes rendered by one set of launches. Every scene's samples form one global sequence
 // (scene-major, then sample, then pixel); a wave takes `capacity` consecutive samples of it, one

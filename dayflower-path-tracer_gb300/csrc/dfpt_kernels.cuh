@@ -1315,14 +1315,29 @@ __global__ void __launch_bounds__(256) k_bresolve(DevBatch Q, DevPass B) {
     }
 }
 
+// Empties the shadow queue after its launch (waves trace each bounce's shadow rays at once).
+__global__ void k_shadow_reset(DevPass B) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        B.counts[DFPT_COUNTS_SHADOW] = 0;
+        B.counts[DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1] = 0;
+    }
+}
+
 __global__ void k_bend_wave(DevBatch Q) {
     if (threadIdx.x == 0 && blockIdx.x == 0) Q.wave_base[0] += Q.capacity;
 }
 
-// Ray binning between bounces (one scene): the bin of a ray is its direction octant (3 bits) and
-// its origin's cell in an 8 x 8 x 8 grid over the scene bounds, in Morton order (9 bits). Rays of
-// a bin start near each other and head the same way, so a warp of them walks much the same nodes.
-// Only the processing order changes: every ray keeps its path id and its own result.
+// Ray binning between bounces: the bin of a ray is its direction octant (3 bits) and its origin's
+// cell in an 8 x 8 x 8 grid over its scene's bounds, in Morton order (9 bits), under 2 bits of its
+// scene's place in the wave (a wave holds consecutive scenes). Rays of a bin start near each other
+// and head the same way, so a warp of them walks much the same nodes. Only the processing order
+// changes: every ray keeps its path id and its own result.
+__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d);
+__device__ __forceinline__ int wave_first_scene(const DevBatch& Q) { return (int)Q.wave_tab[0]; }
+__device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
+    const int sid = __float_as_int(d.w);
+    return (((sid - first) & 3) << 12) | ray_bin(Q.scenes[sid], o, d);
+}
 __device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d) {
     int cell = 0;
     const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
@@ -1338,17 +1353,16 @@ __device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d) {
     return (oct << 9) | cell;
 }
 
+// Bin counts with one atomic per distinct bin of a warp.
+__device__ __forceinline__ void bin_count(int* bins, int key) {
+    const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
+    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(bins + key, __popc(same));
+}
+
 __global__ void __launch_bounds__(256) k_sort_hist(DevBatch Q, DevPass B, int bounce) {
-    __shared__ int h[DFPT_SORT_BINS];
-    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x) h[k] = 0;
-    __syncthreads();
     const int n = B.counts[bounce + 1];
-    const DevScene& S = Q.scenes[0];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        atomicAdd(h + ray_bin(S, B.q_o[1][i], B.q_d[1][i]), 1);
-    __syncthreads();
-    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x)
-        if (h[k]) atomicAdd(B.sort_bins + k, h[k]);
+    const int first = wave_first_scene(Q);
+    GRID_STRIDE_UNIFORM(i, n) bin_count(B.sort_bins, i < n ? ray_bin_in_wave(Q, first, B.q_o[1][i], B.q_d[1][i]) : -1);
 }
 
 // Shadow rays all head for the sun: their bin is the origin's cell in a 16 x 16 x 16 grid over the
@@ -1367,22 +1381,21 @@ __device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
     return cell;
 }
 
+__device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
+    const int sid = __float_as_int(d.w);
+    return (((sid - first) & 3) << 12) | shadow_bin(Q.scenes[sid], o);
+}
+
 __global__ void __launch_bounds__(256) k_sort_shadow_hist(DevBatch Q, DevPass B) {
-    __shared__ int h[DFPT_SORT_BINS];
-    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x) h[k] = 0;
-    __syncthreads();
     const int n = B.counts[DFPT_COUNTS_SHADOW];
-    const DevScene& S = Q.scenes[0];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(h + shadow_bin(S, B.s_o[i]), 1);
-    __syncthreads();
-    for (int k = threadIdx.x; k < DFPT_SORT_BINS; k += blockDim.x)
-        if (h[k]) atomicAdd(B.sort_bins + k, h[k]);
+    const int first = wave_first_scene(Q);
+    GRID_STRIDE_UNIFORM(i, n) bin_count(B.sort_bins, i < n ? shadow_bin_in_wave(Q, first, B.s_o[i], B.s_d[i]) : -1);
 }
 
 // Moves the shadow queue (B.s_*) into the second set (out) in bin order.
 __global__ void __launch_bounds__(256) k_sort_shadow_scatter(DevBatch Q, DevPass B, float4* out_o, float4* out_d, float4* out_c) {
     const int n = B.counts[DFPT_COUNTS_SHADOW];
-    const DevScene& S = Q.scenes[0];
+    const int first = wave_first_scene(Q);
     GRID_STRIDE_UNIFORM(i, n) {
         int key = -1;
         float4 o, d, c;
@@ -1390,7 +1403,7 @@ __global__ void __launch_bounds__(256) k_sort_shadow_scatter(DevBatch Q, DevPass
             o = B.s_o[i];
             d = B.s_d[i];
             c = B.s_c[i];
-            key = shadow_bin(S, o);
+            key = shadow_bin_in_wave(Q, first, o, d);
         }
         const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
         const int leader = __ffs(same) - 1;
@@ -1406,12 +1419,13 @@ __global__ void __launch_bounds__(256) k_sort_shadow_scatter(DevBatch Q, DevPass
     }
 }
 
-// Exclusive scan of the bin counts (one block of 1024 threads, 4 bins each).
+// Exclusive scan of the bin counts (one block of 1024 threads, DFPT_SORT_BINS / 1024 bins each).
 __global__ void __launch_bounds__(1024) k_sort_scan(DevPass B) {
+    constexpr int PER = DFPT_SORT_BINS / 1024;
     __shared__ int part[1024];
     const int t = threadIdx.x;
-    int v[4], sum = 0;
-    for (int j = 0; j < 4; ++j) { v[j] = B.sort_bins[4 * t + j]; sum += v[j]; }
+    int v[PER], sum = 0;
+    for (int j = 0; j < PER; ++j) { v[j] = B.sort_bins[PER * t + j]; sum += v[j]; }
     part[t] = sum;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {
@@ -1421,19 +1435,19 @@ __global__ void __launch_bounds__(1024) k_sort_scan(DevPass B) {
         __syncthreads();
     }
     int run = part[t] - sum;
-    for (int j = 0; j < 4; ++j) { B.sort_bins[4 * t + j] = run; run += v[j]; }
+    for (int j = 0; j < PER; ++j) { B.sort_bins[PER * t + j] = run; run += v[j]; }
 }
 
 __global__ void __launch_bounds__(256) k_sort_scatter(DevBatch Q, DevPass B, int bounce) {
     const int n = B.counts[bounce + 1];
-    const DevScene& S = Q.scenes[0];
+    const int first = wave_first_scene(Q);
     GRID_STRIDE_UNIFORM(i, n) {
         int key = -1;
         float4 o, d;
         if (i < n) {
             o = B.q_o[1][i];
             d = B.q_d[1][i];
-            key = ray_bin(S, o, d);
+            key = ray_bin_in_wave(Q, first, o, d);
         }
         // Lanes with the same bin take consecutive places with one atomic.
         const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
@@ -1592,17 +1606,18 @@ static void launch_b_wave(const LaunchCtx& c, int) { k_bwave<<<1, 32, 0, c.strea
 static void launch_b_film(const LaunchCtx& c, int) { k_bfilm<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_resolve(const LaunchCtx& c, int) { k_bresolve<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_end(const LaunchCtx& c, int) { k_bend_wave<<<1, 32, 0, c.stream>>>(*c.batch); }
-// Bins the rays shading queued for bounce + 1 (queue 1 -> queue 0); one scene.
+static void launch_b_shadow_reset(const LaunchCtx& c, int) { k_shadow_reset<<<1, 32, 0, c.stream>>>(*c.pass); }
+// Bins the rays shading queued for bounce + 1 (queue 1 -> queue 0).
 static void launch_b_sort(const LaunchCtx& c, int bounce) {
     cudaMemsetAsync(c.pass->sort_bins, 0, DFPT_SORT_BINS * sizeof(int), c.stream);
-    k_sort_hist<<<(c.grid + 3) / 4, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
+    k_sort_hist<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
     k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass);
     k_sort_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
 }
 // Bins the deferred shadow queue into `to` (a pass record whose s_* point at the second set).
 static void launch_b_sort_shadow(const LaunchCtx& c, const DevPass& to) {
     cudaMemsetAsync(c.pass->sort_bins, 0, DFPT_SORT_BINS * sizeof(int), c.stream);
-    k_sort_shadow_hist<<<(c.grid + 3) / 4, 256, 0, c.stream>>>(*c.batch, *c.pass);
+    k_sort_shadow_hist<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass);
     k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass);
     k_sort_shadow_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, to.s_o, to.s_d, to.s_c);
 }
@@ -1669,6 +1684,7 @@ KernelSet kernel_set() {
     k.b_end = launch_b_end;
     k.b_sort = launch_b_sort;
     k.b_sort_shadow = launch_b_sort_shadow;
+    k.b_shadow_reset = launch_b_shadow_reset;
     k.shade_adj = launch_shade_adj;
     k.final_adj = launch_final_adj;
     k.diff_reduce = launch_diff_reduce;

@@ -43,6 +43,7 @@ struct KernelSet {
     void (*b_end)(const LaunchCtx&, int) = nullptr;
     void (*b_sort)(const LaunchCtx&, int bounce) = nullptr;  // ray binning (one scene, sorted queues)
     void (*b_sort_shadow)(const LaunchCtx&, const DevPass& to) = nullptr;  // shadow-ray binning into to.s_*
+    void (*b_shadow_reset)(const LaunchCtx&, int) = nullptr;               // empties the shadow queue
     // Path-replay adjoint (the fast kernel set only).
     void (*shade_adj)(const LaunchCtx&, int bounce) = nullptr;
     void (*final_adj)(const LaunchCtx&, int bounce) = nullptr;

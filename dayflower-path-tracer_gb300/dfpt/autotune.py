@@ -97,9 +97,21 @@ def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=N
     best = max(results, key=results.get)
     batch.set_tuning("wave_capacity", max(best[0], 1024))
     batch.set_tuning("trace_config", best[1])
+    # Ray binning on or off at the best point (results[best] was measured with the default, on).
+    sort = {1: results[best]}
+    batch.set_tuning("ray_sort", 0)
     batch.clear()
-    return {"best": {"wave_capacity": best[0], "trace_config": best[1]},
-            "m_samples_per_s": {f"{k[0]}/{k[1]}": round(v, 2) for k, v in results.items()}}
+    batch.render_range(first, min(span, best[0]))
+    batch.synchronize()
+    t0 = time.perf_counter()
+    batch.render_range(first, span)
+    batch.synchronize()
+    sort[0] = span / (time.perf_counter() - t0) / 1e6
+    batch.set_tuning("ray_sort", max(sort, key=sort.get))
+    batch.clear()
+    return {"best": {"wave_capacity": best[0], "trace_config": best[1], "ray_sort": max(sort, key=sort.get)},
+            "m_samples_per_s": {f"{k[0]}/{k[1]}": round(v, 2) for k, v in results.items()},
+            "ray_sort_m_samples_per_s": {str(k): round(v, 2) for k, v in sort.items()}}
 
 
 def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16), verbose: bool = False) -> dict:
@@ -129,5 +141,21 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16), verbose: bool 
             kernel.synchronize()
             sort[mode] = (time.perf_counter() - t0) * 1e3
         kernel.set_tuning("ray_sort", min(sort, key=sort.get))
+    defer = {}
+    if best > 1:
+        # One shadow launch per wave needs a queue of depth x the slots: try it where memory allows.
+        for mode in (0, 1):
+            try:
+                kernel.set_tuning("shadow_defer", mode)
+                kernel.execute(passes)
+                kernel.synchronize()
+            except Exception:
+                continue
+            t0 = time.perf_counter()
+            kernel.execute(passes)
+            kernel.synchronize()
+            defer[mode] = (time.perf_counter() - t0) * 1e3
+        kernel.set_tuning("shadow_defer", min(defer, key=defer.get) if defer else 0)
     return {"best": best, "ms_per_step": {str(k): round(v, 3) for k, v in results.items()},
-            "ray_sort": kernel.get_tuning("ray_sort"), "sort_ms_per_step": {str(k): round(v, 3) for k, v in sort.items()}}
+            "ray_sort": kernel.get_tuning("ray_sort"), "sort_ms_per_step": {str(k): round(v, 3) for k, v in sort.items()},
+            "shadow_defer": kernel.get_tuning("shadow_defer"), "defer_ms_per_step": {str(k): round(v, 3) for k, v in defer.items()}}

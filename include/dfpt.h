@@ -217,7 +217,10 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *   "wide_samples"      passes per wave when dfpt_render renders several passes (1..64, default
  *                       8; 1 renders pass by pass); the film is the same either way;
  *   "ray_sort"          1 (default) bins rays by origin cell and direction octant between the
- *                       bounces of wide passes (processing order only). */
+ *                       bounces of wide passes (processing order only);
+ *   "shadow_defer"      0 (default) traces each bounce's sun shadow rays after its shading in wide
+ *                       passes; 1 traces all bounces' at once after the last (faster, but the
+ *                       shadow queue holds depth x as many rays). */
 int dfpt_set_tuning(dfpt_handle* handle, const char* key, int32_t value);
 int dfpt_get_tuning(dfpt_handle* handle, const char* key, int32_t* value);
 /* Measurement hook (no reference counterpart): returns every persisting L2 line of this process
