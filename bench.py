@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--adjoint-iters", type=int, default=10)
     ap.add_argument("--trace-config", type=int, default=-1, help="fixed traversal configuration (skips the autotuner)")
     ap.add_argument("--wide", type=int, default=0, help="fixed passes per wave (skips that tuner)")
+    ap.add_argument("--shadow-defer", type=int, default=-1, help="with --wide: 1 one shadow launch per wave, 0 per bounce")
     return ap.parse_args()
 
 
@@ -458,7 +459,9 @@ def main():
 
     if args.wide > 0:
         k.set_tuning("wide_samples", args.wide)
-        wide = {"best": args.wide, "ms_per_step": {}}
+        if args.shadow_defer >= 0:
+            k.set_tuning("shadow_defer", args.shadow_defer)
+        wide = {"best": args.wide, "ms_per_step": {}, "shadow_defer": k.get_tuning("shadow_defer")}
     else:
         wide = tune_wide(k, passes=S)
     if args.trace_config >= 0:
