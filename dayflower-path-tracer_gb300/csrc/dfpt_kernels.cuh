@@ -524,8 +524,15 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
                     sid = batch_scene_of(Q, g);
                     const long long local = g - Q.sample_begin[sid];
                     const long long np = (long long)Q.params[sid].width * Q.params[sid].height;
-                    const long long j = local / np;
-                    pixel = (int)(local - j * np);
+                    long long j;
+                    if (local < 0x7FFFFFFFll) {  // 32-bit division where it fits (np < 2^28)
+                        const unsigned q = (unsigned)local / (unsigned)np;
+                        j = q;
+                        pixel = (int)((unsigned)local - q * (unsigned)np);
+                    } else {
+                        j = local / np;
+                        pixel = (int)(local - j * np);
+                    }
                     sample = (uint32_t)(j + pass0);
                     Q.slot_key[i] = make_int4(sid, pixel, (int)sample, 0);
                 }
