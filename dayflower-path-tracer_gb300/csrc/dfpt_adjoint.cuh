@@ -223,16 +223,18 @@ __device__ __forceinline__ void grad_end(float* sh, double* row, int n_prim_entr
             if (sh[k] != 0.0f) row[k] += (double)sh[k];
 }
 
-// One bounce of the replay (the structure of k_shade, GRK:3185-3686).
-template <bool SHARED>
-__global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+// One bounce of the replay (the structure of k_shade, GRK:3185-3686). BATCH: the replay runs in
+// waves of the handle's passes (path = wave slot; pixel and pass from the slot key); otherwise one
+// pass at a time (path = pixel, the pass index from the device counter).
+template <bool BATCH, bool SHARED>
+__global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     extern __shared__ float dyn_sh[];
     __shared__ float red[32 * 4];
     const DevParams& P = *Pp;
     const int n = B.counts[bounce];
-    const int qi = bounce & 1;
-    const uint32_t pass = (uint32_t)*B.pass_index;
-    const size_t sample = (size_t)((int)pass - P.diff_pass0);
+    const int qi = B.sorted_queues ? 0 : (bounce & 1);
+    const uint32_t pass_now = BATCH ? 0u : (uint32_t)*B.pass_index;
+    const size_t npix = (size_t)P.width * (size_t)P.height;
     const float inv_spp = 1.0f / (float)P.diff_spp;
     const int n_prim_entries = S.primitive_count * DFPT_DIFF_PER_PRIM;
     GradAcc acc;
@@ -246,6 +248,13 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
         if (i < n) {
             const float4 o4 = B.q_o[qi][i], d4 = B.q_d[qi][i];
             const int path = __float_as_int(o4.w);
+            uint32_t pixel = (uint32_t)path, pass = pass_now;
+            if constexpr (BATCH) {
+                const int4 key = Q.slot_key[path];
+                pixel = (uint32_t)key.y;
+                pass = (uint32_t)key.z;
+            }
+            const size_t sample = (size_t)((int)pass - P.diff_pass0);
             const int4 hr = B.q_hit[i];
             Hit h;
             h.t = __int_as_float(hr.x);
@@ -254,8 +263,8 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
             h.shape_offset = hr.w;
             float4 T = B.throughput[path];
             float4 Lu = B.radiance[path];  // radiance gathered so far along the replay
-            const float4 Lt = B.diff_L[sample * B.n_pixels + path];
-            float4 w = B.diff_dldi[path];
+            const float4 Lt = B.diff_L[sample * npix + pixel];
+            float4 w = B.diff_dldi[pixel];
             w.x *= inv_spp; w.y *= inv_spp; w.z *= inv_spp;
             if (h.t == INF || h.prim == -1) {
                 D4 sr, sg, sb;
@@ -264,7 +273,7 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
                 for (int j = 0; j < 4; ++j) gsky[j] += (w.x * T.x * sr.d[j] + w.y * T.y * sg.d[j] + w.z * T.z * sb.d[j]) * INV_PI;
                 B.radiance[path] = Lu;
             } else {
-                Rng rng = make_rng(P, (uint32_t)path, pass, B.rng[path]);
+                Rng rng = make_rng(P, pixel, pass, B.rng[path]);
                 const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
                 const int so_off = __ldg(S.prim_info + h.prim).z;
                 const float dp = s.nx * d4.x + s.ny * d4.y + s.nz * d4.z;
@@ -289,7 +298,7 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
                     P.sun_active == 1) {
                     const float u = rng.next(), v = rng.next();
                     float lx, ly, lz, dot1;
-                    const int seen = (B.diff_vis[sample * B.n_pixels + path] >> bounce) & 1;
+                    const int seen = (B.diff_vis[sample * npix + pixel] >> bounce) & 1;
                     if (sun_sample(P, s.px, s.py, s.pz, wx, wy, wz, u, v, lx, ly, lz, dot1) && seen) {
                         const float k = dot1 * INV_PI;
                         Lu.x += T.x * (ar * 1.0f * k); Lu.y += T.y * (ag * 1.0f * k); Lu.z += T.z * (ab * 1.0f * k);
@@ -344,12 +353,12 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
 }
 
 // After the last bounce: the continuation ray's any-hit test; escaping rays add sky tangents.
-template <int V>
-__global__ void __launch_bounds__(256) k_final_adj(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int bounce) {
+template <bool BATCH, int V>
+__global__ void __launch_bounds__(256) k_final_adj(DevScene S, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     __shared__ float red[32 * 4];
     const DevParams& P = *Pp;
     const int n = B.counts[bounce];
-    const int qi = bounce & 1;
+    const int qi = B.sorted_queues ? 0 : (bounce & 1);
     const int n_prim_entries = S.primitive_count * DFPT_DIFF_PER_PRIM;
     const float inv_spp = 1.0f / (float)P.diff_spp;
     float gsky[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -365,7 +374,9 @@ __global__ void __launch_bounds__(256) k_final_adj(DevScene S, const DevParams* 
         if (valid && !(h.t < INF)) {
             const int path = __float_as_int(o.w);
             const float4 T = B.throughput[path];
-            float4 w = B.diff_dldi[path];
+            int pixel = path;
+            if constexpr (BATCH) pixel = Q.slot_key[path].y;
+            float4 w = B.diff_dldi[pixel];
             w.x *= inv_spp; w.y *= inv_spp; w.z *= inv_spp;
             D4 sr, sg, sb;
             sky_color_tan(P, d.x, d.y, d.z, sr, sg, sb);

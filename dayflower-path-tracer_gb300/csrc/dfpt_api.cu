@@ -474,6 +474,7 @@ struct dfpt_handle {
     bool shadow_defer = false;  // wide passes: one shadow launch per wave (queue of slots x depth)
     DevBuf<int> w_sort_bins;
     DevBuf<float4> w_s2_o, w_s2_d, w_s2_c;  // the binned copy of the shadow queue
+    DevBuf<int> w_vis;                       // differentiable mode: visibility bits per slot
     DevPass wpass_shadow{};                  // wpass with the shadow queue pointing at the copy
     LaunchCtx wctx_shadow{};
     uint64_t launches = 0;
@@ -502,7 +503,7 @@ void release(dfpt_handle* h) {
         h->w_q_hit.release(); h->w_slot_key.release(); h->w_rng.release(); h->w_pixel_flags.release(); h->w_counts.release();
         h->w_wave_entries.release(); h->w_scene.release(); h->w_sample_begin.release(); h->w_film_begin.release();
         h->w_wave_base.release(); h->w_wave_tab.release(); h->w_sort_bins.release();
-        h->w_s2_o.release(); h->w_s2_d.release(); h->w_s2_c.release();
+        h->w_s2_o.release(); h->w_s2_d.release(); h->w_s2_c.release(); h->w_vis.release();
     }
     h->sc.release();
     h->diff_albedo.release(); h->diff_emission.release(); h->diff_L.release(); h->diff_dldi.release();
@@ -755,7 +756,7 @@ int bounces_of(const dfpt_handle* h);
 
 bool wide_eligible(const dfpt_handle* h) {
     return h->wide_samples > 1 && !is_simple_mode(h->params.renderer_type) && h->params.rng_kind == DFPT_RNG_COUNTER &&
-           h->params.wireframes != 1 && !h->record_hits && !h->diff_on && !h->use_strict && h->fast.b_camera != nullptr;
+           h->params.wireframes != 1 && !h->record_hits && !h->use_strict && h->fast.b_camera != nullptr;
 }
 
 int wide_prepare(dfpt_handle* h) {
@@ -772,7 +773,7 @@ int wide_prepare(dfpt_handle* h) {
         CUDA_TRY(h->w_q_hit.alloc(c)); CUDA_TRY(h->w_slot_key.alloc(c));
         CUDA_TRY(h->w_throughput.alloc(c)); CUDA_TRY(h->w_radiance.alloc(c)); CUDA_TRY(h->w_rng.alloc(c)); CUDA_TRY(h->w_pixel_flags.alloc(c));
         CUDA_TRY(h->w_s_o.alloc(shadow)); CUDA_TRY(h->w_s_d.alloc(shadow)); CUDA_TRY(h->w_s_c.alloc(shadow));
-        h->w_s2_o.release(); h->w_s2_d.release(); h->w_s2_c.release();
+        h->w_s2_o.release(); h->w_s2_d.release(); h->w_s2_c.release(); h->w_vis.release();
         h->wide_capacity = cap;
         h->wide_shadow = shadow;
         h->wide_graph_valid = false;
@@ -801,6 +802,13 @@ int wide_prepare(dfpt_handle* h) {
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
     B.sorted_queues = (h->ray_sort && h->fast.b_sort) ? 1 : 0;
     B.sort_bins = h->w_sort_bins.p;
+    if (h->diff_on) {
+        // The differentiable forward / replay: visibility bits per slot, the per-sample records.
+        if (!h->w_vis.p) CUDA_TRY(h->w_vis.alloc((size_t)h->wide_capacity));
+        B.vis = h->w_vis.p;
+        B.diff_L = h->pass.diff_L; B.diff_vis = h->pass.diff_vis; B.diff_dldi = h->pass.diff_dldi;
+        B.diff_rows = h->pass.diff_rows; B.diff_row_len = h->pass.diff_row_len;
+    }
     if (B.sorted_queues && !h->w_s2_o.p) {
         CUDA_TRY(h->w_s2_o.alloc(h->wide_shadow));
         CUDA_TRY(h->w_s2_d.alloc(h->wide_shadow));
@@ -826,7 +834,7 @@ int wide_prepare(dfpt_handle* h) {
     Q.wave_entries = h->w_wave_entries.p;
     LaunchCtx& c = h->wctx;
     c = h->ctx;
-    c.scene = nullptr;
+    c.scene = &h->sc.scene;  // the wave replay's adjoint kernels take the scene directly
     c.pass = &h->wpass;
     c.batch = &h->wq;
     h->wctx_shadow = c;
@@ -1595,8 +1603,36 @@ int dfpt_diff_backward(dfpt_handle* h, const float* dloss_dimage, double* grad_a
     CUDA_TRY(cudaMemsetAsync(h->diff_rows.p, 0, h->diff_rows.n * sizeof(double), h->stream));
     // Replay the forward's passes: same pass indices, so the same RNG streams.
     const int pass0 = h->diff_pass0;
-    CUDA_TRY(cudaMemcpyAsync(h->pass_index.p, &pass0, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    for (int j = 0; j < h->diff_spp; ++j) h->launches += (uint64_t)issue_replay_pass(h);
+    if (h->diff_spp >= 2 && wide_eligible(h) && h->fast.b_shade_adj) {
+        // In waves of wide_samples passes through the batch stages (slot keys give pixel and pass).
+        int r = wide_prepare(h);
+        if (r) return r;
+        h->wide_range[0] = 0;
+        h->wide_range[1] = (long long)h->diff_spp * h->n_pixels;
+        h->wide_range[2] = pass0;
+        h->wide_range[3] = -1;
+        CUDA_TRY(cudaMemcpyAsync(h->w_wave_base.p, h->wide_range, 4 * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+        const long long waves = (h->wide_range[1] + h->wide_capacity - 1) / h->wide_capacity;
+        const KernelSet& K = h->fast;
+        const LaunchCtx& c = h->wctx;
+        const int nb = bounces_of(h);
+        for (long long wv = 0; wv < waves; ++wv) {
+            cudaMemsetAsync(h->w_counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), h->stream);
+            K.b_wave(c, 0);
+            K.b_camera(c, 0);
+            for (int b = 0; b < nb; ++b) {
+                K.b_trace_closest(c, b);
+                K.b_shade_adj(c, b);
+                if (h->wpass.sorted_queues) K.b_sort(c, b);
+            }
+            K.b_final_adj(c, nb);
+            K.b_end(c, 0);
+            h->launches += (uint64_t)(2 * nb + 4 + (h->wpass.sorted_queues ? 3 * nb : 0));
+        }
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(h->pass_index.p, &pass0, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        for (int j = 0; j < h->diff_spp; ++j) h->launches += (uint64_t)issue_replay_pass(h);
+    }
     h->fast.diff_reduce(h->ctx, h->diff_rows.p, rows, row_len, h->diff_out.p);
     h->launches += 1;
     CUDA_TRY(cudaGetLastError());

@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
             B.pixel_flags[i] = live ? 0 : 1;
             B.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
             B.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (!BATCH && P.diff) B.vis[i] = 0;
+            if (P.diff) B.vis[i] = 0;
             if (!BATCH && P.wireframes == 1) {
                 B.primary_o[i] = o;
                 B.primary_d[i] = d;
@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __r
                 float er = cr(emission), eg = cg(emission), eb = cb(emission);
                 const int material = f2i(__ldg(S.surfaces + so_off + 0));
                 float exponent = 50.0f;  // the reference's fixed Phong exponent (GRK:3524)
-                if (!BATCH && P.diff) diff_surface(P, h.prim, ar, ag, ab, er, eg, eb, exponent);
+                if (P.diff) diff_surface(P, h.prim, ar, ag, ab, er, eg, eb, exponent);
                 if ((material == DFPT_MATERIAL_CLEAR_COAT || material == DFPT_MATERIAL_LAMBERTIAN || material == DFPT_MATERIAL_PHONG) &&
                     P.sun_active == 1) {
                     const float u = rng.next(), v = rng.next();
@@ -863,7 +863,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevPa
         atomicAdd(L, c.x);
         atomicAdd(L + 1, c.y);
         atomicAdd(L + 2, c.z);
-        if (!BATCH && P.diff) atomicOr(B.vis + path, 1 << __float_as_int(c.w));
+        if (P.diff) atomicOr(B.vis + path, 1 << __float_as_int(c.w));
     };
     if constexpr (V == 3) {
         TraceStats st{0, 0};
@@ -1299,9 +1299,19 @@ __global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
         const long long slot0 = Q.sample_begin[s] - base;
         float4 sum = B.film_sum[f], comp = B.film_comp[f];
         int cnt = B.film_n[f];
+        const DevParams& P = Q.params[s];
+        const long long pass0 = Q.wave_base[2];
         for (long long loc = first; loc < b; loc += np) {
             const int slot = (int)(slot0 + loc);
             film_add(B.radiance[slot], B.pixel_flags[slot], loc / np == clear_sample, sum, comp, cnt);
+            if (P.diff) {
+                // The differentiable forward's per-sample records (as k_film keeps them per pass).
+                const long long k = pass0 + loc / np - P.diff_pass0;
+                if (k >= 0 && k < P.diff_spp) {
+                    B.diff_L[k * np + pixel] = B.radiance[slot];
+                    B.diff_vis[k * np + pixel] = (B.pixel_flags[slot] & 1) ? 0 : B.vis[slot];
+                }
+            }
         }
         B.film_sum[f] = sum; B.film_comp[f] = comp; B.film_n[f] = cnt;
     }
@@ -1630,15 +1640,23 @@ static void launch_b_sort_shadow(const LaunchCtx& c, const DevPass& to) {
 }
 
 // Path-replay adjoint. Per-primitive partials live in shared memory when they fit in 44 KB.
-static void launch_shade_adj(const LaunchCtx& c, int bounce) {
+template <bool BATCH>
+static void launch_shade_adj_t(const LaunchCtx& c, int bounce) {
+    const DevBatch Q = BATCH ? *c.batch : DevBatch{};
     const size_t bytes = (size_t)c.scene->primitive_count * DFPT_DIFF_PER_PRIM * sizeof(float);
-    if (bytes <= 44 * 1024) k_shade_adj<true><<<c.grid, 256, bytes, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
-    else k_shade_adj<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+    if (bytes <= 44 * 1024) k_shade_adj<BATCH, true><<<c.grid, 256, bytes, c.stream>>>(*c.scene, c.params, *c.pass, Q, bounce);
+    else k_shade_adj<BATCH, false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, Q, bounce);
 }
-static void launch_final_adj(const LaunchCtx& c, int bounce) {
+template <bool BATCH>
+static void launch_final_adj_t(const LaunchCtx& c, int bounce) {
     // Per-lane walks (variant 1 prefetches); one block per gradient row.
-    k_final_adj<1><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, bounce);
+    const DevBatch Q = BATCH ? *c.batch : DevBatch{};
+    k_final_adj<BATCH, 1><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, Q, bounce);
 }
+static void launch_shade_adj(const LaunchCtx& c, int bounce) { launch_shade_adj_t<false>(c, bounce); }
+static void launch_final_adj(const LaunchCtx& c, int bounce) { launch_final_adj_t<false>(c, bounce); }
+static void launch_b_shade_adj(const LaunchCtx& c, int bounce) { launch_shade_adj_t<true>(c, bounce); }
+static void launch_b_final_adj(const LaunchCtx& c, int bounce) { launch_final_adj_t<true>(c, bounce); }
 static void launch_diff_reduce(const LaunchCtx& c, const double* rows, int n_rows, int row_len, double* out) {
     k_diff_reduce<<<(row_len + 255) / 256, 256, 0, c.stream>>>(rows, n_rows, row_len, out);
 }
@@ -1694,6 +1712,8 @@ KernelSet kernel_set() {
     k.b_shadow_reset = launch_b_shadow_reset;
     k.shade_adj = launch_shade_adj;
     k.final_adj = launch_final_adj;
+    k.b_shade_adj = launch_b_shade_adj;
+    k.b_final_adj = launch_b_final_adj;
     k.diff_reduce = launch_diff_reduce;
 #endif
     return k;

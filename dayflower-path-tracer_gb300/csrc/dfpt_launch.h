@@ -47,6 +47,8 @@ struct KernelSet {
     // Path-replay adjoint (the fast kernel set only).
     void (*shade_adj)(const LaunchCtx&, int bounce) = nullptr;
     void (*final_adj)(const LaunchCtx&, int bounce) = nullptr;
+    void (*b_shade_adj)(const LaunchCtx&, int bounce) = nullptr;  // the replay in waves (one scene)
+    void (*b_final_adj)(const LaunchCtx&, int bounce) = nullptr;
     void (*diff_reduce)(const LaunchCtx&, const double* rows, int n_rows, int row_len, double* out) = nullptr;
 };
 

@@ -179,3 +179,30 @@ def test_inverse_rendering_step_reduces_loss():
             turb.grad = None
     assert losses[-1] < losses[0], losses
     k.dispose()
+
+
+def test_wave_adjoint_equals_pass_by_pass_adjoint():
+    """The forward and the replay in waves of passes (wide_samples 8) give the gradients of the
+    pass-by-pass forward and replay (wide_samples 1): same paths, same records; float atomics and
+    summation order leave small differences (rtol 1e-4 per group norm)."""
+    from dfpt.diff import DiffRenderer
+    from dfpt.kernel import RendererKernel
+    from dfpt.scene import SkyState
+
+    cs, params, w, h, theta = _scene(plane=True, rr=True)
+    W = np.random.default_rng(9).normal(size=(h, w, 3)).astype(np.float32)
+    out = []
+    for wide in (1, 8):
+        k = RendererKernel(cs, SkyState(tuple(theta["sun_direction"]), theta["turbidity"]), params)
+        k.update(w, h)
+        k.set_tuning("wide_samples", wide)
+        d = DiffRenderer(k)
+        img = d.forward(theta["albedo"], theta["emission"], theta["phong_exponent"], theta["turbidity"], theta["sun_direction"], 6)
+        out.append((img.copy(), d.backward(W)))
+        k.dispose()
+    (ia, ga), (ib, gb) = out
+    np.testing.assert_allclose(ia, ib, rtol=1e-5, atol=1e-6)
+    for key in ("albedo", "emission", "phong_exponent", "sun_direction"):
+        a, b = np.asarray(ga[key]).ravel(), np.asarray(gb[key]).ravel()
+        assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(a) + 1e-6, key
+    assert abs(ga["turbidity"] - gb["turbidity"]) <= 1e-4 * abs(ga["turbidity"]) + 1e-6
