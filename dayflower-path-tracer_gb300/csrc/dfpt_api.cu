@@ -784,7 +784,9 @@ int wide_prepare(dfpt_handle* h) {
         CUDA_TRY(h->w_scene.alloc(1));
         CUDA_TRY(h->w_wave_base.alloc(4));
         CUDA_TRY(h->w_wave_tab.alloc(8));
-        CUDA_TRY(h->w_sort_bins.alloc(DFPT_SORT_BINS));
+        // Offsets, then the ray and the shadow-ray counts (zero at rest).
+        CUDA_TRY(h->w_sort_bins.alloc(3 * DFPT_SORT_BINS));
+        CUDA_TRY(cudaMemsetAsync(h->w_sort_bins.p, 0, 3 * DFPT_SORT_BINS * sizeof(int), h->stream));
         const std::vector<long long> sb = {0, 1ll << 62}, fb = {0, (long long)n};
         CUDA_TRY(upload(h->w_sample_begin, sb, h->stream));
         CUDA_TRY(upload(h->w_film_begin, fb, h->stream));
@@ -802,6 +804,8 @@ int wide_prepare(dfpt_handle* h) {
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
     B.sorted_queues = (h->ray_sort && h->fast.b_sort) ? 1 : 0;
     B.sort_bins = h->w_sort_bins.p;
+    B.sort_count = h->w_sort_bins.p + DFPT_SORT_BINS;
+    B.sort_count_shadow = h->w_sort_bins.p + 2 * DFPT_SORT_BINS;
     if (h->diff_on) {
         // The differentiable forward / replay: visibility bits per slot, the per-sample records.
         if (!h->w_vis.p) CUDA_TRY(h->w_vis.alloc((size_t)h->wide_capacity));
@@ -856,7 +860,7 @@ int issue_wide_wave(dfpt_handle* h) {
     auto shadows = [&]() {
         if (h->sky.is_sun_active != 1) return;
         if (h->wpass.sorted_queues) {
-            mark(h, KIND_SORT); K.b_sort_shadow(c, h->wpass_shadow); k += 3;
+            mark(h, KIND_SORT); k += K.b_sort_shadow(c, h->wpass_shadow);
             mark(h, KIND_SHADOW); K.b_shadow(h->wctx_shadow, 0); ++k;
         } else {
             mark(h, KIND_SHADOW); K.b_shadow(c, 0); ++k;
@@ -866,7 +870,7 @@ int issue_wide_wave(dfpt_handle* h) {
     for (int b = 0; b < nb; ++b) {
         mark(h, KIND_TRACE); K.b_trace_closest(c, b); ++k;
         mark(h, KIND_SHADE); K.b_shade(c, b); ++k;
-        if (h->wpass.sorted_queues) { mark(h, KIND_SORT); K.b_sort(c, b); k += 3; }
+        if (h->wpass.sorted_queues) { mark(h, KIND_SORT); k += K.b_sort(c, b, true); }
         if (!h->shadow_defer) shadows();
     }
     mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
@@ -1623,11 +1627,11 @@ int dfpt_diff_backward(dfpt_handle* h, const float* dloss_dimage, double* grad_a
             for (int b = 0; b < nb; ++b) {
                 K.b_trace_closest(c, b);
                 K.b_shade_adj(c, b);
-                if (h->wpass.sorted_queues) K.b_sort(c, b);
+                if (h->wpass.sorted_queues) h->launches += (uint64_t)K.b_sort(c, b, false);
             }
             K.b_final_adj(c, nb);
             K.b_end(c, 0);
-            h->launches += (uint64_t)(2 * nb + 4 + (h->wpass.sorted_queues ? 3 * nb : 0));
+            h->launches += (uint64_t)(2 * nb + 4);
         }
     } else {
         CUDA_TRY(cudaMemcpyAsync(h->pass_index.p, &pass0, sizeof(int), cudaMemcpyHostToDevice, h->stream));

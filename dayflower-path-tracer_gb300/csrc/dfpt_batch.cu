@@ -164,7 +164,11 @@ int batch_prepare(dfpt_batch* b) {
     B.film_sum = b->film_sum.p; B.film_comp = b->film_comp.p; B.film_n = b->film_n.p; B.bgra = b->bgra.p;
     B.sorted_queues = (b->ray_sort && b->ks.b_sort) ? 1 : 0;
     if (B.sorted_queues) {
-        if (!b->sort_bins.p) CUDA_TRY(b->sort_bins.alloc(DFPT_SORT_BINS));
+        if (!b->sort_bins.p) {
+            // Offsets, then the ray and the shadow-ray counts (zero at rest).
+            CUDA_TRY(b->sort_bins.alloc(3 * DFPT_SORT_BINS));
+            CUDA_TRY(cudaMemsetAsync(b->sort_bins.p, 0, 3 * DFPT_SORT_BINS * sizeof(int), b->stream));
+        }
         if (!b->s2_o.p) {
             CUDA_TRY(b->s2_o.alloc(b->shadow_slots));
             CUDA_TRY(b->s2_d.alloc(b->shadow_slots));
@@ -172,6 +176,8 @@ int batch_prepare(dfpt_batch* b) {
         }
     }
     B.sort_bins = b->sort_bins.p;
+    B.sort_count = b->sort_bins.p ? b->sort_bins.p + DFPT_SORT_BINS : nullptr;
+    B.sort_count_shadow = b->sort_bins.p ? b->sort_bins.p + 2 * DFPT_SORT_BINS : nullptr;
     b->pass_shadow = B;
     if (B.sorted_queues) {
         b->pass_shadow.s_o = b->s2_o.p;
@@ -215,10 +221,10 @@ int issue_wave(dfpt_batch* b) {
     for (int i = 0; i < b->depth; ++i) {
         K.b_trace_closest(c, i); ++k;
         K.b_shade(c, i); ++k;
-        if (b->pass.sorted_queues) { K.b_sort(c, i); k += 3; }
+        if (b->pass.sorted_queues) k += K.b_sort(c, i, true);
         if (b->any_sun) {
             if (b->pass.sorted_queues) {
-                K.b_sort_shadow(c, b->pass_shadow); k += 3;
+                k += K.b_sort_shadow(c, b->pass_shadow);
                 K.b_shadow(b->ctx_shadow, 0); ++k;
             } else {
                 K.b_shadow(c, 0); ++k;

@@ -141,7 +141,9 @@ struct DevPass {
     // Ray binning between bounces (wide passes): with sorted_queues set, shading writes queue 1,
     // the binning pass moves it to queue 0 in bin order, and every bounce reads queue 0.
     int sorted_queues;
-    int* sort_bins;            // DFPT_SORT_BINS counters, then exclusive offsets
+    int* sort_bins;            // DFPT_SORT_BINS exclusive offsets (scan output, scatter cursors)
+    int* sort_count;           // DFPT_SORT_BINS ray counts of the next bounce; zero at rest (the scan clears them)
+    int* sort_count_shadow;    // the same for the sun shadow rays
 };
 #define DFPT_SORT_BINS 16384  // 2 bits of scene (within a wave) x 3 bits of octant x 9 bits of cell
 

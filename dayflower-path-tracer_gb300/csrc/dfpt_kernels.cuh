@@ -729,10 +729,63 @@ __device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx
     return out;
 }
 
+// Ray binning between bounces: the bin of a ray is its direction octant (3 bits) and its origin's
+// cell in an 8 x 8 x 8 grid over its scene's bounds, in Morton order (9 bits), under 2 bits of its
+// scene's place in the wave (a wave holds consecutive scenes). Rays of a bin start near each other
+// and head the same way, so a warp of them walks much the same nodes. Only the processing order
+// changes: every ray keeps its path id and its own result.
+__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d);
+__device__ __forceinline__ int wave_first_scene(const DevBatch& Q) { return (int)Q.wave_tab[0]; }
+__device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
+    const int sid = __float_as_int(d.w);
+    return (((sid - first) & 3) << 12) | ray_bin(Q.scenes[sid], o, d);
+}
+__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d) {
+    int cell = 0;
+    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
+    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
+    const float p[3] = {o.x, o.y, o.z};
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 8.0f;
+        c[a] = u >= 0.0f ? (u < 7.0f ? (int)u : 7) : 0;  // NaN and below: 0
+    }
+    for (int b = 0; b < 3; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
+    const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
+    return (oct << 9) | cell;
+}
+
+// Bin counts with one atomic per distinct bin of a warp.
+__device__ __forceinline__ void bin_count(int* bins, int key) {
+    const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
+    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(bins + key, __popc(same));
+}
+
+// Shadow rays all head for the sun: their bin is the origin's cell in a 16 x 16 x 16 grid over the
+// scene bounds (Morton order, 12 bits).
+__device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
+    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
+    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
+    const float p[3] = {o.x, o.y, o.z};
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 16.0f;
+        c[a] = u >= 0.0f ? (u < 15.0f ? (int)u : 15) : 0;
+    }
+    int cell = 0;
+    for (int b = 0; b < 4; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
+    return cell;
+}
+
+__device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
+    const int sid = __float_as_int(d.w);
+    return (((sid - first) & 3) << 12) | shadow_bin(Q.scenes[sid], o);
+}
+
 // One bounce of shading: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
 // roulette, material sampling and the next ray (GRK:3185-3686).
 template <bool BATCH>
-__global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
+__global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     const int n = B.counts[bounce];
     const int qi = B.sorted_queues ? 0 : (bounce & 1);
     const uint32_t pass = BATCH ? 0u : (uint32_t)*B.pass_index;
@@ -836,6 +889,14 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S0, const DevParams* __r
         if (slot >= 0) {
             B.q_o[qi ^ 1][slot] = no;
             B.q_d[qi ^ 1][slot] = nd;
+        }
+        if constexpr (BATCH) {
+            // Ray binning: the histograms of the next bounce's rays and of the shadow rays.
+            if (B.sorted_queues) {
+                const int first = wave_first_scene(Q);
+                bin_count(B.sort_count, emit_next ? ray_bin_in_wave(Q, first, no, nd) : -1);
+                bin_count(B.sort_count_shadow, emit_shadow ? shadow_bin_in_wave(Q, first, so, sd) : -1);
+            }
         }
         const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
         if (sslot >= 0) {
@@ -1344,69 +1405,10 @@ __global__ void k_bend_wave(DevBatch Q) {
     if (threadIdx.x == 0 && blockIdx.x == 0) Q.wave_base[0] += Q.capacity;
 }
 
-// Ray binning between bounces: the bin of a ray is its direction octant (3 bits) and its origin's
-// cell in an 8 x 8 x 8 grid over its scene's bounds, in Morton order (9 bits), under 2 bits of its
-// scene's place in the wave (a wave holds consecutive scenes). Rays of a bin start near each other
-// and head the same way, so a warp of them walks much the same nodes. Only the processing order
-// changes: every ray keeps its path id and its own result.
-__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d);
-__device__ __forceinline__ int wave_first_scene(const DevBatch& Q) { return (int)Q.wave_tab[0]; }
-__device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
-    const int sid = __float_as_int(d.w);
-    return (((sid - first) & 3) << 12) | ray_bin(Q.scenes[sid], o, d);
-}
-__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d) {
-    int cell = 0;
-    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
-    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
-    const float p[3] = {o.x, o.y, o.z};
-    int c[3];
-    for (int a = 0; a < 3; ++a) {
-        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 8.0f;
-        c[a] = u >= 0.0f ? (u < 7.0f ? (int)u : 7) : 0;  // NaN and below: 0
-    }
-    for (int b = 0; b < 3; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
-    const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
-    return (oct << 9) | cell;
-}
-
-// Bin counts with one atomic per distinct bin of a warp.
-__device__ __forceinline__ void bin_count(int* bins, int key) {
-    const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
-    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(bins + key, __popc(same));
-}
-
 __global__ void __launch_bounds__(256) k_sort_hist(DevBatch Q, DevPass B, int bounce) {
     const int n = B.counts[bounce + 1];
     const int first = wave_first_scene(Q);
-    GRID_STRIDE_UNIFORM(i, n) bin_count(B.sort_bins, i < n ? ray_bin_in_wave(Q, first, B.q_o[1][i], B.q_d[1][i]) : -1);
-}
-
-// Shadow rays all head for the sun: their bin is the origin's cell in a 16 x 16 x 16 grid over the
-// scene bounds (Morton order, 12 bits).
-__device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
-    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
-    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
-    const float p[3] = {o.x, o.y, o.z};
-    int c[3];
-    for (int a = 0; a < 3; ++a) {
-        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 16.0f;
-        c[a] = u >= 0.0f ? (u < 15.0f ? (int)u : 15) : 0;
-    }
-    int cell = 0;
-    for (int b = 0; b < 4; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
-    return cell;
-}
-
-__device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
-    const int sid = __float_as_int(d.w);
-    return (((sid - first) & 3) << 12) | shadow_bin(Q.scenes[sid], o);
-}
-
-__global__ void __launch_bounds__(256) k_sort_shadow_hist(DevBatch Q, DevPass B) {
-    const int n = B.counts[DFPT_COUNTS_SHADOW];
-    const int first = wave_first_scene(Q);
-    GRID_STRIDE_UNIFORM(i, n) bin_count(B.sort_bins, i < n ? shadow_bin_in_wave(Q, first, B.s_o[i], B.s_d[i]) : -1);
+    GRID_STRIDE_UNIFORM(i, n) bin_count(B.sort_count, i < n ? ray_bin_in_wave(Q, first, B.q_o[1][i], B.q_d[1][i]) : -1);
 }
 
 // Moves the shadow queue (B.s_*) into the second set (out) in bin order.
@@ -1436,13 +1438,14 @@ __global__ void __launch_bounds__(256) k_sort_shadow_scatter(DevBatch Q, DevPass
     }
 }
 
-// Exclusive scan of the bin counts (one block of 1024 threads, DFPT_SORT_BINS / 1024 bins each).
-__global__ void __launch_bounds__(1024) k_sort_scan(DevPass B) {
+// Exclusive scan of the bin counts into B.sort_bins (one block of 1024 threads, DFPT_SORT_BINS /
+// 1024 bins each); the counts are cleared for the next count.
+__global__ void __launch_bounds__(1024) k_sort_scan(DevPass B, int* counts) {
     constexpr int PER = DFPT_SORT_BINS / 1024;
     __shared__ int part[1024];
     const int t = threadIdx.x;
     int v[PER], sum = 0;
-    for (int j = 0; j < PER; ++j) { v[j] = B.sort_bins[PER * t + j]; sum += v[j]; }
+    for (int j = 0; j < PER; ++j) { v[j] = counts[PER * t + j]; sum += v[j]; counts[PER * t + j] = 0; }
     part[t] = sum;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {
@@ -1624,19 +1627,21 @@ static void launch_b_film(const LaunchCtx& c, int) { k_bfilm<<<c.grid, 256, 0, c
 static void launch_b_resolve(const LaunchCtx& c, int) { k_bresolve<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_end(const LaunchCtx& c, int) { k_bend_wave<<<1, 32, 0, c.stream>>>(*c.batch); }
 static void launch_b_shadow_reset(const LaunchCtx& c, int) { k_shadow_reset<<<1, 32, 0, c.stream>>>(*c.pass); }
-// Bins the rays shading queued for bounce + 1 (queue 1 -> queue 0).
-static void launch_b_sort(const LaunchCtx& c, int bounce) {
-    cudaMemsetAsync(c.pass->sort_bins, 0, DFPT_SORT_BINS * sizeof(int), c.stream);
-    k_sort_hist<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
-    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass);
+// Bins the rays shading queued for bounce + 1 (queue 1 -> queue 0). k_shade counts the bins as it
+// queues the rays (counted); the replay's shading does not, and a histogram pass counts them.
+// Returns the kernels launched.
+static int launch_b_sort(const LaunchCtx& c, int bounce, bool counted) {
+    if (!counted) k_sort_hist<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
+    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass, c.pass->sort_count);
     k_sort_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
+    return counted ? 2 : 3;
 }
-// Bins the deferred shadow queue into `to` (a pass record whose s_* point at the second set).
-static void launch_b_sort_shadow(const LaunchCtx& c, const DevPass& to) {
-    cudaMemsetAsync(c.pass->sort_bins, 0, DFPT_SORT_BINS * sizeof(int), c.stream);
-    k_sort_shadow_hist<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass);
-    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass);
+// Bins the shadow queue into `to` (a pass record whose s_* point at the second set); k_shade
+// counted the bins.
+static int launch_b_sort_shadow(const LaunchCtx& c, const DevPass& to) {
+    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass, c.pass->sort_count_shadow);
     k_sort_shadow_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, to.s_o, to.s_d, to.s_c);
+    return 2;
 }
 
 // Path-replay adjoint. Per-primitive partials live in shared memory when they fit in 44 KB.

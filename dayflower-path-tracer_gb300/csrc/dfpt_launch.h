@@ -41,8 +41,8 @@ struct KernelSet {
     void (*b_film)(const LaunchCtx&, int) = nullptr;
     void (*b_resolve)(const LaunchCtx&, int) = nullptr;
     void (*b_end)(const LaunchCtx&, int) = nullptr;
-    void (*b_sort)(const LaunchCtx&, int bounce) = nullptr;  // ray binning (one scene, sorted queues)
-    void (*b_sort_shadow)(const LaunchCtx&, const DevPass& to) = nullptr;  // shadow-ray binning into to.s_*
+    int (*b_sort)(const LaunchCtx&, int bounce, bool counted) = nullptr;  // ray binning (sorted queues); kernels launched
+    int (*b_sort_shadow)(const LaunchCtx&, const DevPass& to) = nullptr;   // shadow-ray binning into to.s_*
     void (*b_shadow_reset)(const LaunchCtx&, int) = nullptr;               // empties the shadow queue
     // Path-replay adjoint (the fast kernel set only).
     void (*shade_adj)(const LaunchCtx&, int bounce) = nullptr;
