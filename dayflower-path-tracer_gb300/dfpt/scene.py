@@ -127,6 +127,21 @@ class CompiledScene:
         return CompiledScene(name, **arrays)
 
 
+def camera_set_resolution(camera: np.ndarray, width, height) -> np.ndarray:
+    """Camera.setResolution (scene/Camera.java:806-816) on a 19-float camera record, in place: the
+    resolution, then the vertical field of view from the horizontal one (setFieldOfViewX,
+    Camera.java:743-748, with Math4J's float-rounded trigonometry). DayflowerApplication sets the
+    camera to the kernel's size before rendering (DayflowerApplication.java:334)."""
+    rx, ry = np.float32(width), np.float32(height)
+    camera[16], camera[17] = rx, ry
+    fov_x = np.float32(camera[4])
+    rad = np.float32(np.float64(fov_x) * (np.pi / 180.0))
+    tn = np.float32(np.tan(np.float64(np.float32(rad * np.float32(0.5)))))
+    at = np.float32(np.arctan(np.float64(np.float32(tn * np.float32(ry / rx)))))
+    camera[5] = np.float32(np.float64(np.float32(np.float32(2.0) * at)) * (180.0 / np.pi))
+    return camera
+
+
 class SkyState:
     """Sky.set(sunDirectionWorld, turbidity) (scene/Sky.java:295-333) as a dfpt_sky."""
 
@@ -190,12 +205,45 @@ class SceneBuilder:
         return self.texture([TEX_CONSTANT, 3, pack_argb(r, g, b)])
 
     def checkerboard(self, c0, c1, degrees=0.0, scale_u=1.0, scale_v=1.0) -> int:
-        rad = np.float32(np.float32(degrees) * np.float32(np.pi / 180.0))
+        rad = np.float32(np.float64(np.float32(degrees)) * (np.pi / 180.0))  # MathF.toRadians
         return self.texture([TEX_CHECKERBOARD, 8, pack_argb(*c0), pack_argb(*c1), float(np.cos(np.float64(rad))),
                              float(np.sin(np.float64(rad))), scale_u, scale_v])
 
     def fbm(self, addend, multiplier, frequency, gain, octaves) -> int:
         return self.texture([TEX_FBM, 7, pack_argb(*addend), pack_argb(*multiplier), frequency, gain, octaves])
+
+    def blend(self, texture_a, texture_b, factor=0.5) -> int:
+        """BlendTexture (texture/BlendTexture.java:206-214): the children are earlier builder
+        textures; the compiler writes their offsets into the record."""
+        return self.texture([TEX_BLEND, 5, texture_a, texture_b, factor])
+
+    def bullseye(self, color_a=(1.0, 0.0, 0.0), color_b=(0.0, 0.0, 0.0)) -> int:
+        return self.texture([TEX_BULLSEYE, 4, pack_argb(*color_a), pack_argb(*color_b)])
+
+    def surface_normal_texture(self, tangent_space=False) -> int:
+        return self.texture([TEX_SURFACE_NORMAL, 3, 1.0 if tangent_space else 0.0])
+
+    def uv_texture(self) -> int:
+        return self.texture([TEX_UV, 2])
+
+    def image(self, width, height, rgb, degrees=0.0, scale_u=1.0, scale_v=1.0) -> int:
+        """ImageTexture (texture/ImageTexture.java:337-357): `rgb` holds width x height 0x00RRGGBB
+        ints, top row first (see dfpt.images.load)."""
+        data = np.asarray(rgb, dtype=np.int64).reshape(-1)
+        if data.size != int(width) * int(height):
+            raise ValueError("image data does not match width x height")
+        rad = np.float32(np.float64(np.float32(degrees)) * (np.pi / 180.0))  # MathF.toRadians
+        head = [TEX_IMAGE, 8 + data.size, float(np.cos(np.float64(rad))), float(np.sin(np.float64(rad))), width, height,
+                scale_u, scale_v]
+        rec = np.concatenate([np.asarray(head, np.float32), data.astype(np.float32)])
+        return self.texture(rec)
+
+    def image_file(self, path, degrees=0.0, scale_u=1.0, scale_v=1.0) -> int:
+        """ImageTexture.load(file, degrees, scaleU, scaleV)."""
+        from . import images
+
+        w, h, rgb = images.load(path)
+        return self.image(w, h, rgb, degrees, scale_u, scale_v)
 
     def surface(self, material, albedo, emission, normal, noise_amount=0.0, noise_scale=0.0) -> int:
         return check(self._lib.dfpt_builder_add_surface(self._h, material, albedo, emission, normal,
