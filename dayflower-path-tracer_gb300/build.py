@@ -38,6 +38,7 @@ def _units():
     gxx = shutil.which("g++") or "g++"
     return [
         ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_kernels_fast.cu")], BUILD_DIR / "dfpt_kernels_fast.o"),
+        ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_kernels_wide.cu")], BUILD_DIR / "dfpt_kernels_wide.o"),
         ([nvcc, *ARCH, *NVCC_COMMON, "-fmad=false", "-c", str(CSRC / "dfpt_kernels_strict.cu")], BUILD_DIR / "dfpt_kernels_strict.o"),
         ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_api.cu")], BUILD_DIR / "dfpt_api.o"),
         ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_noalloc.cu")], BUILD_DIR / "dfpt_noalloc.o"),

@@ -413,7 +413,7 @@ struct dfpt_handle {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int sms = 0;
-    KernelSet fast{}, strict{};
+    KernelSet fast{}, strict{}, wide{};  // wide: the batch stages over this handle's scene
     bool use_strict = false;
     // Parameters.
     dfpt_params params{};
@@ -676,7 +676,11 @@ int reset_rng(dfpt_handle* h) {
     return DFPT_OK;
 }
 
-const KernelSet& kset(dfpt_handle* h) { return h->use_strict ? h->strict : h->fast; }
+// The kernel set of a pass: the strict set when selected, and always for the ray caster, whose hit
+// ids are the reference's bit for bit (one rounding per float operation); the fast set otherwise.
+const KernelSet& kset(dfpt_handle* h) {
+    return (h->use_strict || h->params.renderer_type == DFPT_RENDERER_RAY_CASTER) ? h->strict : h->fast;
+}
 
 bool is_simple_mode(int rt) {
     return rt == DFPT_RENDERER_AMBIENT_OCCLUSION || rt == DFPT_RENDERER_RAY_CASTER || rt == DFPT_RENDERER_RAY_MARCHER ||
@@ -756,7 +760,7 @@ int bounces_of(const dfpt_handle* h);
 
 bool wide_eligible(const dfpt_handle* h) {
     return h->wide_samples > 1 && !is_simple_mode(h->params.renderer_type) && h->params.rng_kind == DFPT_RNG_COUNTER &&
-           h->params.wireframes != 1 && !h->record_hits && !h->use_strict && h->fast.b_camera != nullptr;
+           h->params.wireframes != 1 && !h->record_hits && !h->use_strict && h->wide.b_camera != nullptr;
 }
 
 int wide_prepare(dfpt_handle* h) {
@@ -802,7 +806,7 @@ int wide_prepare(dfpt_handle* h) {
     B.throughput = h->w_throughput.p; B.radiance = h->w_radiance.p; B.rng = h->w_rng.p; B.pixel_flags = h->w_pixel_flags.p;
     B.counts = h->w_counts.p; B.stats = h->stats.p; B.pass_index = h->pass_index.p;
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
-    B.sorted_queues = (h->ray_sort && h->fast.b_sort) ? 1 : 0;
+    B.sorted_queues = (h->ray_sort && h->wide.b_sort) ? 1 : 0;
     B.sort_bins = h->w_sort_bins.p;
     B.sort_count = h->w_sort_bins.p + DFPT_SORT_BINS;
     B.sort_count_shadow = h->w_sort_bins.p + 2 * DFPT_SORT_BINS;
@@ -838,7 +842,9 @@ int wide_prepare(dfpt_handle* h) {
     Q.wave_entries = h->w_wave_entries.p;
     LaunchCtx& c = h->wctx;
     c = h->ctx;
-    c.scene = &h->sc.scene;  // the wave replay's adjoint kernels take the scene directly
+    c.scene = &h->sc.scene;  // the one-scene batch kernels take the scene record as their parameter
+    h->wide.occupancy(h->sms, c.grid, c.grid_trace, c.grid_simple);
+    c.grid_trace = h->wide.trace_grid(c.trace_config, h->sms);
     c.pass = &h->wpass;
     c.batch = &h->wq;
     h->wctx_shadow = c;
@@ -848,7 +854,7 @@ int wide_prepare(dfpt_handle* h) {
 
 // One wave; returns the number of kernels launched.
 int issue_wide_wave(dfpt_handle* h) {
-    const KernelSet& K = h->fast;
+    const KernelSet& K = h->wide;
     const LaunchCtx& c = h->wctx;
     int k = 0;
     cudaMemsetAsync(h->w_counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), h->stream);
@@ -1186,6 +1192,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     h->n_pixels = width * height;
     h->fast = dfpt_fast::kernel_set();
     h->strict = dfpt_strict::kernel_set();
+    h->wide = dfpt_wide::kernel_set();
     h->sky = *sky;
     dfpt_params_default(&h->params);
     int dev = 0;
@@ -1232,6 +1239,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     // Noise tables (both kernel sets own a copy).
     r = noise_tables_init(h->fast, st);
     if (!r) r = noise_tables_init(h->strict, st);
+    if (!r) r = noise_tables_init(h->wide, st);
     if (r) { release(h); delete h; return r; }
     TRY_R(cudaStreamSynchronize(st));
 #undef TRY_R
@@ -1355,7 +1363,7 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->ctx.trace_config = value;
         h->ctx.grid_trace = kset(h).trace_grid(value, h->sms);
         h->graph_valid = false;
-    h->wide_graph_valid = false;
+        h->wide_graph_valid = false;
         return DFPT_OK;
     }
     if (std::strcmp(key, "ray_sort") == 0) {
@@ -1383,7 +1391,7 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
         scene_set_culling(h->sc, value);
         h->graph_valid = false;
-    h->wide_graph_valid = false;
+        h->wide_graph_valid = false;
         return DFPT_OK;
     }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
@@ -1607,7 +1615,7 @@ int dfpt_diff_backward(dfpt_handle* h, const float* dloss_dimage, double* grad_a
     CUDA_TRY(cudaMemsetAsync(h->diff_rows.p, 0, h->diff_rows.n * sizeof(double), h->stream));
     // Replay the forward's passes: same pass indices, so the same RNG streams.
     const int pass0 = h->diff_pass0;
-    if (h->diff_spp >= 2 && wide_eligible(h) && h->fast.b_shade_adj) {
+    if (h->diff_spp >= 2 && wide_eligible(h) && h->wide.b_shade_adj) {
         // In waves of wide_samples passes through the batch stages (slot keys give pixel and pass).
         int r = wide_prepare(h);
         if (r) return r;
@@ -1617,7 +1625,7 @@ int dfpt_diff_backward(dfpt_handle* h, const float* dloss_dimage, double* grad_a
         h->wide_range[3] = -1;
         CUDA_TRY(cudaMemcpyAsync(h->w_wave_base.p, h->wide_range, 4 * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
         const long long waves = (h->wide_range[1] + h->wide_capacity - 1) / h->wide_capacity;
-        const KernelSet& K = h->fast;
+        const KernelSet& K = h->wide;
         const LaunchCtx& c = h->wctx;
         const int nb = bounces_of(h);
         for (long long wv = 0; wv < waves; ++wv) {

@@ -296,6 +296,42 @@ struct TraceStats {
     uint32_t nodes, tris;
 };
 
+// Slab distances of the node test, (b - o) * (1 / d) per axis (GRK:1093-1095, 1122-1129). The strict kernel
+// set keeps that form. The fast set computes b * inv + (-o * inv), one FMA per slab with -o * inv
+// taken once per mesh, and clamps inv to +-1e30 so that a zero direction component gives huge
+// distances of the right sign rather than inf - inf; distances differ from the strict form by
+// rounding only (the fast set is held to statistical parity).
+struct SlabRay {
+    float ix, iy, iz;  // 1 / d per axis
+    float px, py, pz;  // fast: -o * inv; strict: o
+};
+__device__ __forceinline__ SlabRay slab_ray(float ox, float oy, float oz, float dx, float dy, float dz) {
+    SlabRay r;
+    r.ix = 1.0f / dx;
+    r.iy = 1.0f / dy;
+    r.iz = 1.0f / dz;
+#ifdef DFPT_FMA_SLABS
+    r.ix = copysignf(fminf(fabsf(r.ix), 1.0e30f), r.ix);
+    r.iy = copysignf(fminf(fabsf(r.iy), 1.0e30f), r.iy);
+    r.iz = copysignf(fminf(fabsf(r.iz), 1.0e30f), r.iz);
+    r.px = -ox * r.ix;
+    r.py = -oy * r.iy;
+    r.pz = -oz * r.iz;
+#else
+    r.px = ox;
+    r.py = oy;
+    r.pz = oz;
+#endif
+    return r;
+}
+__device__ __forceinline__ float slab(float b, float inv, float p) {
+#ifdef DFPT_FMA_SLABS
+    return fmaf(b, inv, p);
+#else
+    return (b - p) * inv;
+#endif
+}
+
 // Threaded-BVH walk of one mesh (GRK:1097-1194) in the reference's preorder: a node's box is
 // tested when it is visited, with the closest distance found so far; descend to the next node
 // (its left child) or skip to `next`. Returns true when an any-hit query found its hit.
@@ -305,7 +341,7 @@ struct TraceStats {
 template <bool ANY, int V>
 __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo, float dxo,
                                           float dyo, float dzo, Hit& h, TraceStats& st) {
-    const float ix = 1.0f / dxo, iy = 1.0f / dyo, iz = 1.0f / dzo;
+    const SlabRay sr = slab_ray(oxo, oyo, ozo, dxo, dyo, dzo);
     int node = root;
     float4 n0 = __ldg(S.nodes + 2 * node), n1 = __ldg(S.nodes + 2 * node + 1);
     while (node != -1) {
@@ -322,8 +358,8 @@ __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim,
             s0 = __ldg(S.nodes + 2 * sn);
             s1 = __ldg(S.nodes + 2 * sn + 1);
         }
-        const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
-        const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
+        const float t0x = slab(n0.x, sr.ix, sr.px), t0y = slab(n0.y, sr.iy, sr.py), t0z = slab(n0.z, sr.iz, sr.pz);
+        const float t1x = slab(n1.x, sr.ix, sr.px), t1y = slab(n1.y, sr.iy, sr.py), t1z = slab(n1.z, sr.iz, sr.pz);
         const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
         const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
         const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
@@ -368,7 +404,7 @@ __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim,
 template <bool ANY>
 __device__ __forceinline__ bool mesh_walk_warp(const DevScene& S, int root, int prim, bool active, float oxo, float oyo, float ozo,
                                                float dxo, float dyo, float dzo, Hit& h, TraceStats& st) {
-    const float ix = 1.0f / dxo, iy = 1.0f / dyo, iz = 1.0f / dzo;
+    const SlabRay sr = slab_ray(oxo, oyo, ozo, dxo, dyo, dzo);
     int cur = active ? root : -1;
     bool found = false;
     for (;;) {
@@ -381,8 +417,8 @@ __device__ __forceinline__ bool mesh_walk_warp(const DevScene& S, int root, int 
             st.nodes++;
             const int next = __float_as_int(n0.w);
             const int leaf = __float_as_int(n1.w);
-            const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
-            const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
+            const float t0x = slab(n0.x, sr.ix, sr.px), t0y = slab(n0.y, sr.iy, sr.py), t0z = slab(n0.z, sr.iz, sr.pz);
+            const float t1x = slab(n1.x, sr.ix, sr.px), t1y = slab(n1.y, sr.iy, sr.py), t1z = slab(n1.z, sr.iz, sr.pz);
             const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
             const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
             const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
@@ -640,7 +676,8 @@ __device__ __forceinline__ void trace_refill(int n, int* fetch, SceneOf scene, L
     const int lane = threadIdx.x & 31;
     int idx = -1, prim = 0, node = -1;
     float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
-    float oxo = 0, oyo = 0, ozo = 0, dxo = 0, dyo = 0, dzo = 1, ix = 0, iy = 0, iz = 1;
+    float oxo = 0, oyo = 0, ozo = 0, dxo = 0, dyo = 0, dzo = 1;
+    SlabRay sr{0, 0, 1, 0, 0, 0};
     float4 n0 = make_float4(0, 0, 0, 0), n1 = make_float4(0, 0, 0, 0);
     Hit h;
     h.t = INF; h.prim = -1; h.shape_type = -1; h.shape_offset = -1;
@@ -705,7 +742,7 @@ __device__ __forceinline__ void trace_refill(int n, int* fetch, SceneOf scene, L
             dxo = r0.x * d.x + r0.y * d.y + r0.z * d.z;
             dyo = r1.x * d.x + r1.y * d.y + r1.z * d.z;
             dzo = r2.x * d.x + r2.y * d.y + r2.z * d.z;
-            ix = 1.0f / dxo; iy = 1.0f / dyo; iz = 1.0f / dzo;
+            sr = slab_ray(oxo, oyo, ozo, dxo, dyo, dzo);
             node = info.w;
             n0 = __ldg(S.nodes + 2 * node);
             n1 = __ldg(S.nodes + 2 * node + 1);
@@ -715,8 +752,8 @@ __device__ __forceinline__ void trace_refill(int n, int* fetch, SceneOf scene, L
         st.nodes++;
         const int next = __float_as_int(n0.w);
         const int leaf = __float_as_int(n1.w);
-        const float t0x = (n0.x - oxo) * ix, t0y = (n0.y - oyo) * iy, t0z = (n0.z - ozo) * iz;
-        const float t1x = (n1.x - oxo) * ix, t1y = (n1.y - oyo) * iy, t1z = (n1.z - ozo) * iz;
+        const float t0x = slab(n0.x, sr.ix, sr.px), t0y = slab(n0.y, sr.iy, sr.py), t0z = slab(n0.z, sr.iz, sr.pz);
+        const float t1x = slab(n1.x, sr.ix, sr.px), t1y = slab(n1.y, sr.iy, sr.py), t1z = slab(n1.z, sr.iz, sr.pz);
         const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
         const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
         const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;

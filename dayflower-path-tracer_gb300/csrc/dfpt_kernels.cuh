@@ -475,15 +475,28 @@ __device__ __forceinline__ void warp_add_stats(const DevParams& P, unsigned long
         for (int i = i##_base + (int)threadIdx.x, i##_once = 1; i##_once; i##_once = 0)
 
 // Scene and parameters of a work item: the kernel's own (one scene) or the item's scene of a batch.
+// A translation unit compiled with DFPT_ONE_SCENE runs the batch stages over one scene (waves of
+// passes): its scene record is the kernel parameter, read from the constant bank, not a record in
+// global memory per ray (which costs registers inside the traversal loop).
 template <bool BATCH>
 __device__ __forceinline__ const DevScene& scene_of(const DevScene& S0, const DevBatch& Q, int sid) {
+#ifdef DFPT_ONE_SCENE
+    (void)Q; (void)sid;
+    return S0;
+#else
     if constexpr (BATCH) return Q.scenes[sid];
     else { (void)Q; (void)sid; return S0; }
+#endif
 }
 template <bool BATCH>
 __device__ __forceinline__ const DevParams& params_of(const DevParams* P0, const DevBatch& Q, int sid) {
+#ifdef DFPT_ONE_SCENE
+    (void)Q; (void)sid;
+    return *P0;
+#else
     if constexpr (BATCH) return Q.params[sid];
     else { (void)Q; (void)sid; return *P0; }
+#endif
 }
 // The scene holding global sample g: the last scene whose first sample is <= g.
 __device__ __forceinline__ int batch_scene_of(const DevBatch& Q, long long g) {
@@ -1535,8 +1548,17 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
     X(7, 3, 256, 4) X(8, 3, 128, 8) X(9, 3, 256, 3) X(10, 3, 256, 2) \
     X(11, 0, 256, 6) X(12, 1, 256, 6) X(13, 0, 256, 8) X(14, 1, 256, 8)
 
+// The scene argument of the batch stages: the context's scene in a one-scene set, else none (the
+// kernels read each item's scene from the batch).
+#ifdef DFPT_ONE_SCENE
+#define BATCH_SCENE(c) (*(c).scene)
+#else
+#define BATCH_SCENE(c) DevScene{}
+#endif
+
 template <int V, int BLOCK, int MINB>
 struct TraceCfg {
+#ifndef DFPT_ONE_SCENE
     static void closest(const LaunchCtx& c, int bounce) {
         k_trace<false, false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce, c.pass->sorted_queues ? 0 : (bounce & 1));
     }
@@ -1551,21 +1573,30 @@ struct TraceCfg {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<false, false, V, BLOCK, MINB>, BLOCK, 0);
         return sms * (b > 0 ? b : 1);
     }
+#endif
 #ifdef DFPT_EXTENDED_KERNELS
     // Batch traversal: per-lane walks only (a warp may hold rays of several scenes).
     static constexpr int BV = V == 2 ? 1 : V;
     static void b_closest(const LaunchCtx& c, int bounce) {
-        k_trace<true, false, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce, c.pass->sorted_queues ? 0 : (bounce & 1));
+        k_trace<true, false, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch, bounce, c.pass->sorted_queues ? 0 : (bounce & 1));
     }
     static void b_shadow(const LaunchCtx& c, int bounce) {
-        k_shadow<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce);
+        k_shadow<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch, bounce);
     }
     static void b_final(const LaunchCtx& c, int bounce) {
-        k_final<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce);
+        k_final<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch, bounce);
     }
+#ifdef DFPT_ONE_SCENE
+    static int grid(int sms) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<true, false, BV, BLOCK, MINB>, BLOCK, 0);
+        return sms * (b > 0 ? b : 1);
+    }
+#endif
 #endif
 };
 
+#ifndef DFPT_ONE_SCENE
 static void launch_trace_closest(const LaunchCtx& c, int bounce) {
     switch (c.trace_config) {
 #define X(id, v, b, m) case id: TraceCfg<v, b, m>::closest(c, bounce); break;
@@ -1590,6 +1621,7 @@ static void launch_final(const LaunchCtx& c, int bounce) {
         default: TraceCfg<0, 256, 4>::final_(c, bounce);
     }
 }
+#endif
 static int trace_grid(int config, int sms) {
     switch (config) {
 #define X(id, v, b, m) case id: return TraceCfg<v, b, m>::grid(sms);
@@ -1599,8 +1631,10 @@ static int trace_grid(int config, int sms) {
     }
 }
 
+#ifndef DFPT_ONE_SCENE
 static void launch_camera(const LaunchCtx& c) { k_camera<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}); }
 static void launch_shade(const LaunchCtx& c, int bounce) { k_shade<false><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce); }
+#endif
 
 #ifdef DFPT_EXTENDED_KERNELS
 #define BATCH_DISPATCH(fn)                                                                     \
@@ -1620,8 +1654,8 @@ BATCH_DISPATCH(final)
 #undef BATCH_CASE_closest
 #undef BATCH_CASE_shadow
 #undef BATCH_CASE_final
-static void launch_b_camera(const LaunchCtx& c, int) { k_camera<true><<<c.grid, 256, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch); }
-static void launch_b_shade(const LaunchCtx& c, int bounce) { k_shade<true><<<c.grid, 256, 0, c.stream>>>(DevScene{}, c.params, *c.pass, *c.batch, bounce); }
+static void launch_b_camera(const LaunchCtx& c, int) { k_camera<true><<<c.grid, 256, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch); }
+static void launch_b_shade(const LaunchCtx& c, int bounce) { k_shade<true><<<c.grid, 256, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch, bounce); }
 static void launch_b_wave(const LaunchCtx& c, int) { k_bwave<<<1, 32, 0, c.stream>>>(*c.batch); }
 static void launch_b_film(const LaunchCtx& c, int) { k_bfilm<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_resolve(const LaunchCtx& c, int) { k_bresolve<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
@@ -1658,14 +1692,17 @@ static void launch_final_adj_t(const LaunchCtx& c, int bounce) {
     const DevBatch Q = BATCH ? *c.batch : DevBatch{};
     k_final_adj<BATCH, 1><<<c.grid, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, Q, bounce);
 }
+#ifndef DFPT_ONE_SCENE
 static void launch_shade_adj(const LaunchCtx& c, int bounce) { launch_shade_adj_t<false>(c, bounce); }
 static void launch_final_adj(const LaunchCtx& c, int bounce) { launch_final_adj_t<false>(c, bounce); }
+#endif
 static void launch_b_shade_adj(const LaunchCtx& c, int bounce) { launch_shade_adj_t<true>(c, bounce); }
 static void launch_b_final_adj(const LaunchCtx& c, int bounce) { launch_final_adj_t<true>(c, bounce); }
 static void launch_diff_reduce(const LaunchCtx& c, const double* rows, int n_rows, int row_len, double* out) {
     k_diff_reduce<<<(row_len + 255) / 256, 256, 0, c.stream>>>(rows, n_rows, row_len, out);
 }
 #endif
+#ifndef DFPT_ONE_SCENE
 static void launch_simple(const LaunchCtx& c) { k_simple<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_wireframe(const LaunchCtx& c) { k_wireframe<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_film(const LaunchCtx& c) { k_film<<<c.grid, 256, 0, c.stream>>>(c.params, *c.pass); }
@@ -1674,12 +1711,18 @@ static void launch_film_mean(const LaunchCtx& c, double* out3) { k_film_mean<<<c
 static void launch_film_average(const LaunchCtx& c, float* rgb, int* samples) {
     k_film_average<<<c.grid, 256, 0, c.stream>>>(*c.pass, rgb, samples);
 }
+#endif
 static void launch_init_tables(cudaStream_t s, const int* perm, const float* grad) { k_init_tables<<<1, 512, 0, s>>>(perm, grad); }
 
 static void occupancy(int sms, int& grid, int& grid_trace, int& grid_simple) {
     int b1 = 0, b3 = 0;
+#ifdef DFPT_ONE_SCENE
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_shade<true>, 256, 0);
+    b3 = b1;
+#else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_shade<false>, 256, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_simple, 128, 0);
+#endif
     grid = sms * (b1 > 0 ? b1 : 1);
     grid_trace = trace_grid(0, sms);
     grid_simple = sms * (b3 > 0 ? b3 : 1);
@@ -1687,6 +1730,7 @@ static void occupancy(int sms, int& grid, int& grid_trace, int& grid_simple) {
 
 KernelSet kernel_set() {
     KernelSet k;
+#ifndef DFPT_ONE_SCENE
     k.camera = launch_camera;
     k.trace_closest = launch_trace_closest;
     k.shade = launch_shade;
@@ -1698,6 +1742,7 @@ KernelSet kernel_set() {
     k.end_pass = launch_end_pass;
     k.film_mean = launch_film_mean;
     k.film_average = launch_film_average;
+#endif
     k.init_tables = launch_init_tables;
     k.occupancy = occupancy;
     k.trace_grid = trace_grid;
@@ -1715,8 +1760,10 @@ KernelSet kernel_set() {
     k.b_sort = launch_b_sort;
     k.b_sort_shadow = launch_b_sort_shadow;
     k.b_shadow_reset = launch_b_shadow_reset;
+#ifndef DFPT_ONE_SCENE
     k.shade_adj = launch_shade_adj;
     k.final_adj = launch_final_adj;
+#endif
     k.b_shade_adj = launch_b_shade_adj;
     k.b_final_adj = launch_b_final_adj;
     k.diff_reduce = launch_diff_reduce;

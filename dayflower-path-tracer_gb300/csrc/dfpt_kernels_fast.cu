@@ -2,4 +2,5 @@
 // the batch stages and the path-replay adjoint.
 #define DFPT_NS dfpt_fast
 #define DFPT_EXTENDED_KERNELS
+#define DFPT_FMA_SLABS
 #include "dfpt_kernels.cuh"

@@ -54,3 +54,4 @@ struct KernelSet {
 
 namespace dfpt_fast { KernelSet kernel_set(); }
 namespace dfpt_strict { KernelSet kernel_set(); }
+namespace dfpt_wide { KernelSet kernel_set(); }  // batch stages over one scene (waves of passes)
