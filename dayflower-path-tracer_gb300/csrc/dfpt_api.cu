@@ -468,7 +468,7 @@ struct dfpt_handle {
     cudaGraphExec_t wide_graph = nullptr;
     bool wide_graph_valid = false;
     int wide_graph_kernels = 0;
-    long long wide_range[4] = {0, 0, 0, -1};  // wave base, range end, pass of sample 0, clear sample
+    long long wide_range[5] = {0, 0, 0, -1, -1};  // wave base, range end, pass of sample 0, clear sample, selection pass
     int pass_index_host = 0;  // source of pass-index copies (pageable: consumed on return)
     bool ray_sort = true;     // bin rays between bounces in wide passes
     bool shadow_defer = false;  // wide passes: one shadow launch per wave (queue of slots x depth)
@@ -786,7 +786,7 @@ int wide_prepare(dfpt_handle* h) {
         CUDA_TRY(h->w_counts.alloc(DFPT_COUNTS_SIZE));
         CUDA_TRY(h->w_wave_entries.alloc(1));
         CUDA_TRY(h->w_scene.alloc(1));
-        CUDA_TRY(h->w_wave_base.alloc(4));
+        CUDA_TRY(h->w_wave_base.alloc(5));
         CUDA_TRY(h->w_wave_tab.alloc(8));
         // Offsets, then the ray and the shadow-ray counts (zero at rest).
         CUDA_TRY(h->w_sort_bins.alloc(3 * DFPT_SORT_BINS));
@@ -808,6 +808,7 @@ int wide_prepare(dfpt_handle* h) {
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
     B.sorted_queues = (h->ray_sort && h->wide.b_sort) ? 1 : 0;
     B.sort_bins = h->w_sort_bins.p;
+    B.primitive_offsets = h->primitive_offsets.p;  // selection buffer: first hits of the call's last pass
     B.sort_count = h->w_sort_bins.p + DFPT_SORT_BINS;
     B.sort_count_shadow = h->w_sort_bins.p + 2 * DFPT_SORT_BINS;
     if (h->diff_on) {
@@ -898,7 +899,8 @@ int render_wide(dfpt_handle* h, int passes) {
     h->wide_range[1] = (long long)passes * n;
     h->wide_range[2] = h->host_pass;
     h->wide_range[3] = (cs >= 0 && cs < passes) ? cs : -1;
-    CUDA_TRY(cudaMemcpyAsync(h->w_wave_base.p, h->wide_range, 4 * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+    h->wide_range[4] = h->host_pass + passes - 1;  // the selection buffer shows the last pass
+    CUDA_TRY(cudaMemcpyAsync(h->w_wave_base.p, h->wide_range, 5 * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
     const long long waves = (h->wide_range[1] + h->wide_capacity - 1) / h->wide_capacity;
     if (h->use_graph && !h->profiling) {
         if (!h->wide_graph_valid) {
@@ -926,6 +928,12 @@ int render_wide(dfpt_handle* h, int passes) {
         for (long long w = 0; w < waves; ++w) h->launches += (uint64_t)issue_wide_wave(h);
         CUDA_TRY(cudaGetLastError());
     }
+    // The image: the film tone mapped, with the selection highlight of the last pass's first hits.
+    mark(h, KIND_FILM);
+    h->wide.b_resolve(h->wctx, 0);
+    h->launches += 1;
+    mark(h, KIND_COUNT);
+    CUDA_TRY(cudaGetLastError());
     // The device pass counter follows (the next normal pass reads it).
     h->host_pass += passes;
     h->pass_index_host = h->host_pass;
@@ -1444,9 +1452,8 @@ int dfpt_render(dfpt_handle* h, int32_t passes) {
         if (r) return r;
     }
     if (passes >= 2 && wide_eligible(h)) {
-        int r = render_wide(h, passes - 1);
-        if (r) return r;
-        passes = 1;
+        // Every pass in waves; the selection buffer and the image come from the last one.
+        return render_wide(h, passes);
     }
     if (h->use_graph && !h->profiling) {
         if (!h->graph_valid) {
@@ -1623,7 +1630,8 @@ int dfpt_diff_backward(dfpt_handle* h, const float* dloss_dimage, double* grad_a
         h->wide_range[1] = (long long)h->diff_spp * h->n_pixels;
         h->wide_range[2] = pass0;
         h->wide_range[3] = -1;
-        CUDA_TRY(cudaMemcpyAsync(h->w_wave_base.p, h->wide_range, 4 * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+        h->wide_range[4] = -1;
+        CUDA_TRY(cudaMemcpyAsync(h->w_wave_base.p, h->wide_range, 5 * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
         const long long waves = (h->wide_range[1] + h->wide_capacity - 1) / h->wide_capacity;
         const KernelSet& K = h->wide;
         const LaunchCtx& c = h->wctx;

@@ -161,7 +161,8 @@ struct DevBatch {
     long long* wave_base;             // device: [0] global sample of slot 0 of the current wave,
                                       // [1] end of the sample range being rendered, [2] RNG pass
                                       // index of sample 0, [3] sample whose film update replaces
-                                      // the pixel (-1: none)
+                                      // the pixel (-1: none), [4] RNG pass whose first hits fill
+                                      // the selection buffer (one-scene waves; -1: none)
     int4* slot_key;                   // per slot {scene, pixel, RNG pass index, 0}
     long long* wave_tab;              // per scene in the wave {scene, local begin, local end, film-task prefix}
     int* wave_entries;                // entries in wave_tab

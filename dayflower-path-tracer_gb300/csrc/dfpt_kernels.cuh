@@ -829,6 +829,10 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
             float4 T = B.throughput[path];
             float4 L = B.radiance[path];
             if (!BATCH && bounce == 0) B.primitive_offsets[path] = h.prim >= 0 ? h.prim * 3 : -1;
+            // A handle's waves of passes: the selection buffer holds the first hits of the call's
+            // last pass (wave record entry 4; batches of scenes have no selection buffer).
+            if (BATCH && bounce == 0 && B.primitive_offsets != nullptr && (long long)rng_pass == Q.wave_base[4])
+                B.primitive_offsets[rng_pixel] = h.prim >= 0 ? h.prim * 3 : -1;
             if (h.t == INF || h.prim == -1) {
                 const float3 sky = sky_color(P, d4.x, d4.y, d4.z);
                 L.x += T.x * sky.x * INV_PI;
@@ -1402,7 +1406,8 @@ __global__ void __launch_bounds__(256) k_bresolve(DevBatch Q, DevPass B) {
             else hi = mid - 1;
         }
         const int cnt = B.film_n[f];
-        reinterpret_cast<uchar4*>(B.bgra)[f] = cnt > 0 ? tone_map_bgra(Q.params[lo], B.film_sum[f], cnt, -1) : make_uchar4(0, 0, 0, 255);
+        const int po = B.primitive_offsets != nullptr ? B.primitive_offsets[f] : -1;  // selection highlight (one scene)
+        reinterpret_cast<uchar4*>(B.bgra)[f] = cnt > 0 ? tone_map_bgra(Q.params[lo], B.film_sum[f], cnt, po) : make_uchar4(0, 0, 0, 255);
     }
 }
 
