@@ -514,6 +514,20 @@ __device__ __forceinline__ int batch_scene_of(const DevBatch& Q, long long g) {
 // both forms: one scene (BATCH = false; a path is a pixel, the pass index keys the RNG) and a batch
 // of scenes (BATCH = true; a path is a wave slot, {scene, pixel, sample} come from the slot key).
 
+// Waves with the counter RNG and no differentiation start their paths lean: the camera writes no
+// throughput, radiance or RNG state, and shading at bounce 0 starts from throughput 1, radiance 0
+// and the camera's draw count (two for the pixel jitter, two more with an aperture). The film
+// ignores a rejected (fisheye) slot's radiance.
+template <bool BATCH>
+__device__ __forceinline__ bool lean_start(const DevParams& P) {
+    return BATCH && P.rng_kind == DFPT_RNG_COUNTER && !P.diff;
+}
+__device__ __forceinline__ uint32_t camera_draws(const DevScene& S, const DevParams& P) {
+    const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
+                    (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
+    return (pt ? 2u : 0u) + (__ldg(S.camera) > 0.00001f ? 2u : 0u);
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q) {
     const int n = BATCH ? Q.capacity : B.n_pixels;
@@ -523,6 +537,14 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
         base = Q.wave_base[0];
         end = Q.wave_base[1];
         pass0 = Q.wave_base[2];
+    }
+    // A thin lens keeps every pixel, so with one scene the queue is the slots in order (no atomics):
+    // the valid slots are a prefix.
+    const bool dense = (!BATCH || Q.n_scenes == 1) && __ldg(scene_of<BATCH>(S0, Q, 0).camera + 18) != 2.0f;
+    if (dense && blockIdx.x == 0 && threadIdx.x == 0) {
+        long long valid = n;
+        if constexpr (BATCH) valid = end - base < (long long)n ? (end - base > 0 ? end - base : 0) : (long long)n;
+        B.counts[0] = (int)valid;
     }
     GRID_STRIDE_UNIFORM(i, n) {
         bool valid = i < n;
@@ -560,17 +582,19 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
                             (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
             Rng rng = make_rng(P, (uint32_t)pixel, sample, (!BATCH && P.rng_kind == DFPT_RNG_LCG) ? B.rng[i] : 0ull);
             live = primary_ray(S, P, pixel, pt, rng, o, d);
-            B.rng[i] = rng.state;
             B.pixel_flags[i] = live ? 0 : 1;
-            B.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-            B.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (!lean_start<BATCH>(P)) {
+                B.rng[i] = rng.state;
+                B.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+                B.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
             if (P.diff) B.vis[i] = 0;
             if (!BATCH && P.wireframes == 1) {
                 B.primary_o[i] = o;
                 B.primary_d[i] = d;
             }
         }
-        const int slot = warp_push(B.counts + 0, live);
+        const int slot = dense ? (live ? i : -1) : warp_push(B.counts + 0, live);
         if (slot >= 0) {
             o.w = __int_as_float(i);
             d.w = BATCH ? __int_as_float(sid) : 0.0f;
@@ -826,8 +850,9 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
             h.prim = hr.y;
             h.shape_type = hr.z;
             h.shape_offset = hr.w;
-            float4 T = B.throughput[path];
-            float4 L = B.radiance[path];
+            const bool fresh = bounce == 0 && lean_start<BATCH>(P);
+            float4 T = fresh ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : B.throughput[path];
+            float4 L = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : B.radiance[path];
             if (!BATCH && bounce == 0) B.primitive_offsets[path] = h.prim >= 0 ? h.prim * 3 : -1;
             // A handle's waves of passes: the selection buffer holds the first hits of the call's
             // last pass (wave record entry 4; batches of scenes have no selection buffer).
@@ -844,7 +869,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
                     B.hit_distance[path] = INF;
                 }
             } else {
-                Rng rng = make_rng(P, rng_pixel, rng_pass, B.rng[path]);
+                Rng rng = make_rng(P, rng_pixel, rng_pass, fresh ? (uint64_t)camera_draws(S, P) : B.rng[path]);
                 const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
                 if (!BATCH && bounce == 0 && P.record_hits) {
                     B.hit_prim_offset[path] = h.prim * 3; B.hit_shape_type[path] = h.shape_type; B.hit_shape_offset[path] = h.shape_offset;
