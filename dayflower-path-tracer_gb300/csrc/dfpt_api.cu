@@ -108,6 +108,12 @@ float int_bits(int i) {
     return f;
 }
 
+int float_bits_int(float f) {
+    int i;
+    std::memcpy(&i, &f, 4);
+    return i;
+}
+
 int add_tri_record(const HostScene& s, Derived& d, int off, bool last) {
     const float* P = s.point3fs.data();
     const int a = s.triangles[off], b = s.triangles[off + 1], c = s.triangles[off + 2];
@@ -1047,7 +1053,7 @@ void SceneStore::release() {
     for (auto* b : fb) b->release();
     DevBuf<int>* ib[] = {&planes, &triangles, &primitives};
     for (auto* b : ib) b->release();
-    DevBuf<float4>* f4[] = {&trav, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
+    DevBuf<float4>* f4[] = {&trav, &pairs, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
     for (auto* b : f4) b->release();
     prim_info.release();
     cull_prims.release();
@@ -1112,6 +1118,30 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
         CUDA_TRY(upload(st.trav, trav, s));
         CUDA_TRY(cudaStreamSynchronize(s));
     }
+    {
+        // Pair records. The walk over them assumes every inner node N has two children: L = N + 1,
+        // R = next(L), and R's subtree ends where N's does (next(R) == next(N)); otherwise the
+        // scene keeps the threaded walk alone.
+        const size_t nn = d.nodes.size() / 2;
+        std::vector<float4> pairs(4 * nn, make_float4(0, 0, 0, 0));
+        bool full_binary = true;
+        auto next_of = [&](size_t n) { return float_bits_int(d.nodes[2 * n].w); };
+        auto leaf_of = [&](size_t n) { return float_bits_int(d.nodes[2 * n + 1].w); };
+        for (size_t n = 0; n < nn && full_binary; ++n) {
+            if (leaf_of(n) != -1) continue;
+            const size_t l = n + 1;
+            const int r = l < nn ? next_of(l) : -1;
+            if (l >= nn || r < 0 || (size_t)r >= nn || next_of((size_t)r) != next_of(n)) { full_binary = false; break; }
+            const float4 lo = d.nodes[2 * l], lh = d.nodes[2 * l + 1], ro = d.nodes[2 * (size_t)r], rh = d.nodes[2 * (size_t)r + 1];
+            pairs[4 * n] = make_float4(lo.x, lo.y, lo.z, lh.x);
+            pairs[4 * n + 1] = make_float4(lh.y, lh.z, ro.x, ro.y);
+            pairs[4 * n + 2] = make_float4(ro.z, rh.x, rh.y, rh.z);
+            pairs[4 * n + 3] = make_float4(lh.w, rh.w, int_bits(r), 0.0f);
+        }
+        st.scene.use_pairs = full_binary ? 1 : 0;
+        CUDA_TRY(upload(st.pairs, pairs, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+    }
     CUDA_TRY(upload(st.sphere4, d.sphere4, s));
     CUDA_TRY(upload(st.plane_a, d.plane_a, s));
     CUDA_TRY(upload(st.plane_n, d.plane_n, s));
@@ -1124,6 +1154,7 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     S.textures = st.textures.p; S.surfaces = st.surfaces.p; S.primitives = st.primitives.p;
     S.o2w = st.o2w.p; S.w2o = st.w2o.p; S.camera = st.camera.p;
     S.prim_info = st.prim_info.p; S.nodes = st.trav.p; S.tris = st.trav.p + st.trav_nodes; S.sphere4 = st.sphere4.p;
+    S.pairs = st.pairs.p;
     S.plane_a = st.plane_a.p; S.plane_n = st.plane_n.p;
     st.derived = Derived();
     return DFPT_OK;

@@ -338,9 +338,20 @@ __device__ __forceinline__ float slab(float b, float inv, float p) {
 // V selects the implementation: 0 loads each node when it is reached; 1 issues the loads of both
 // possible successors (node + 1 and next) before the current node's slab test, so the dependent
 // load of the walk overlaps the test. Both visit the same nodes in the same order.
+template <bool ANY, int K>
+__device__ __forceinline__ bool mesh_walk_pair(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo,
+                                               float dxo, float dyo, float dzo, Hit& h, TraceStats& st);
+
 template <bool ANY, int V>
 __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo, float dxo,
                                           float dyo, float dzo, Hit& h, TraceStats& st) {
+    // Variant 4: pair records with an 8-entry stack for closest-hit queries (when the scene's trees
+    // allow it). Any-hit queries keep the threaded walk: with no closest distance yet they enter
+    // every box on the ray, the pending right children outgrow the stack, and they gain nothing
+    // from the cached intervals.
+    if constexpr (V == 4 && !ANY) {
+        if (S.use_pairs) return mesh_walk_pair<ANY, 8>(S, root, prim, oxo, oyo, ozo, dxo, dyo, dzo, h, st);
+    }
     const SlabRay sr = slab_ray(oxo, oyo, ozo, dxo, dyo, dzo);
     int node = root;
     float4 n0 = __ldg(S.nodes + 2 * node), n1 = __ldg(S.nodes + 2 * node + 1);
@@ -393,6 +404,130 @@ __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim,
         }
     }
     return false;
+}
+
+// The reference's box test (GRK:1132-1134) on a slab interval: the node is entered when the
+// interval is not empty and its entry, or else its exit, lies in (0.001, closest). For fixed
+// (tmin, tmax) it can only turn from true to false as the closest distance shrinks.
+__device__ __forceinline__ bool box_accepts(float tmin, float tmax, float closest) {
+    return !(tmin > tmax) && ((tmin > 0.001f && tmin < closest) || (tmax > 0.001f && tmax < closest));
+}
+__device__ __forceinline__ void slab_interval(float ax, float ay, float az, float bx, float by, float bz, const SlabRay& sr,
+                                              float& tmin, float& tmax) {
+    const float t0x = slab(ax, sr.ix, sr.px), t0y = slab(ay, sr.iy, sr.py), t0z = slab(az, sr.iz, sr.pz);
+    const float t1x = slab(bx, sr.ix, sr.px), t1y = slab(by, sr.iy, sr.py), t1z = slab(bz, sr.iz, sr.pz);
+    tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
+    tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+}
+
+// The threaded walk over pair records (DevScene::pairs), with a short stack in shared memory. An
+// entered inner node's record gives both children's boxes in one load. The left child is tested
+// at once (it follows its parent in preorder, with the same closest distance); the right child's
+// slab interval is computed now and its test is decided when the walk reaches it in preorder -
+// after the left subtree - with the closest distance of that moment, so every test has exactly
+// the operands of mesh_walk's. A right child that fails already is never pushed (it would fail
+// then too). When the K-entry stack overflows its oldest entries are dropped; once it runs empty
+// the walk continues from next() of the last finished node in the threaded records. Each lane
+// may call it alone.
+template <bool ANY, int K>
+__device__ __forceinline__ bool mesh_walk_pair(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo,
+                                               float dxo, float dyo, float dzo, Hit& h, TraceStats& st) {
+    __shared__ int4 stk[K * 256];  // [entry][thread]: {first triangle, node, tmin bits, tmax bits}
+    const int tid = threadIdx.x;
+    const SlabRay sr = slab_ray(oxo, oyo, ozo, dxo, dyo, dzo);
+    int cur, leaf, last = root;
+    int top = 0, bottom = 0;  // live entries [bottom, top), slot e % K; bottom > 0 once any was dropped
+    {
+        const float4 n0 = __ldg(S.nodes + 2 * root), n1 = __ldg(S.nodes + 2 * root + 1);
+        st.nodes++;
+        float tmin, tmax;
+        slab_interval(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, sr, tmin, tmax);
+        if (!box_accepts(tmin, tmax, h.t)) return false;  // a mesh root's next is -1
+        cur = root;
+        leaf = __float_as_int(n1.w);
+    }
+    for (;;) {
+        // `cur` was entered; `leaf` is its first triangle (-1 inner, -2 empty leaf).
+        bool descend = false;
+        if (leaf != -1) {
+            for (int k = leaf; k >= 0;) {
+                const float4 a = __ldg(S.tris + 3 * k);
+                const float4 e0 = __ldg(S.tris + 3 * k + 1);
+                const float4 e1 = __ldg(S.tris + 3 * k + 2);
+                st.tris++;
+                const float t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, a, e0, e1, h.t);
+                if (t < h.t) {
+                    h.t = t;
+                    h.prim = prim;
+                    h.shape_type = DFPT_SHAPE_TRIANGLE;
+                    h.shape_offset = __float_as_int(a.w);
+                }
+                if (ANY && h.prim != -1) return true;
+                k = __float_as_int(e0.w) != 0 ? -1 : k + 1;
+            }
+            last = cur;
+        } else {
+            const float4* P = S.pairs + 4 * (size_t)cur;
+            const float4 p0 = __ldg(P), p1 = __ldg(P + 1), p2 = __ldg(P + 2);
+            const int4 p3 = __ldg(reinterpret_cast<const int4*>(P + 3));
+            float lmin, lmax, rmin, rmax;
+            slab_interval(p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, sr, lmin, lmax);
+            slab_interval(p1.z, p1.w, p2.x, p2.y, p2.z, p2.w, sr, rmin, rmax);
+            st.nodes++;
+            const bool accept_r = box_accepts(rmin, rmax, h.t);
+            if (box_accepts(lmin, lmax, h.t)) {
+                if (accept_r) {
+                    if (top - bottom == K) ++bottom;
+                    stk[(top % K) * 256 + tid] = make_int4(p3.y, p3.z, __float_as_int(rmin), __float_as_int(rmax));
+                    ++top;
+                } else {
+                    st.nodes++;  // the right child's test, decided (rejected) already
+                }
+                cur = cur + 1;
+                leaf = p3.x;
+                descend = true;
+            } else {
+                st.nodes++;
+                if (accept_r) {
+                    cur = p3.z;
+                    leaf = p3.y;
+                    descend = true;
+                } else {
+                    last = p3.z;
+                }
+            }
+        }
+        if (descend) continue;
+        // The next node in preorder: the nearest pending right child, else next() of `last`.
+        for (;;) {
+            if (top > bottom) {
+                --top;
+                const int4 e = stk[(top % K) * 256 + tid];
+                st.nodes++;
+                if (box_accepts(__int_as_float(e.z), __int_as_float(e.w), h.t)) {
+                    cur = e.y;
+                    leaf = e.x;
+                    break;
+                }
+                last = e.y;
+            } else if (bottom > 0) {
+                const int nxt = __float_as_int(__ldg(S.nodes + 2 * last).w);
+                if (nxt == -1) return false;
+                const float4 n0 = __ldg(S.nodes + 2 * nxt), n1 = __ldg(S.nodes + 2 * nxt + 1);
+                st.nodes++;
+                float tmin, tmax;
+                slab_interval(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, sr, tmin, tmax);
+                if (box_accepts(tmin, tmax, h.t)) {
+                    cur = nxt;
+                    leaf = __float_as_int(n1.w);
+                    break;
+                }
+                last = nxt;
+            } else {
+                return false;
+            }
+        }
+    }
 }
 
 // Warp-synchronous form of the same walk: every lane keeps its own position in the preorder

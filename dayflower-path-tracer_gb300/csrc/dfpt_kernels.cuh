@@ -1576,7 +1576,8 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
 #define TRACE_CONFIGS(X) \
     X(0, 0, 256, 4) X(1, 1, 256, 4) X(2, 1, 256, 3) X(3, 0, 128, 8) X(4, 2, 256, 4) X(5, 2, 128, 8) X(6, 2, 256, 3) \
     X(7, 3, 256, 4) X(8, 3, 128, 8) X(9, 3, 256, 3) X(10, 3, 256, 2) \
-    X(11, 0, 256, 6) X(12, 1, 256, 6) X(13, 0, 256, 8) X(14, 1, 256, 8)
+    X(11, 0, 256, 6) X(12, 1, 256, 6) X(13, 0, 256, 8) X(14, 1, 256, 8) \
+    X(15, 4, 256, 4)
 
 // The scene argument of the batch stages: the context's scene in a one-scene set, else none (the
 // kernels read each item's scene from the batch).
@@ -1776,7 +1777,7 @@ KernelSet kernel_set() {
     k.init_tables = launch_init_tables;
     k.occupancy = occupancy;
     k.trace_grid = trace_grid;
-    k.trace_configs = 15;
+    k.trace_configs = 16;
 #ifdef DFPT_EXTENDED_KERNELS
     k.b_camera = launch_b_camera;
     k.b_trace_closest = launch_b_closest;
