@@ -3,8 +3,8 @@
 One step = one dfpt_render call of --spp-per-step passes (default 16) over the whole 1920x1080
 image; a pass is one sample per pixel, the unit of the reference's Kernel.execute
 (DayflowerApplication.java:853), so the default 16 timed steps render the 256 spp of the
-triangle-mesh configuration. Inside a call, all passes but the last run `wide_samples` at a time
-through the wave kernels (same samples, same film as pass-by-pass rendering, tested). The workload
+triangle-mesh configuration. Inside a call, the passes run `wide_samples` at a time through the
+wave kernels (same samples, same film and image as pass-by-pass rendering, tested). The workload
 is mesh_scene: an fBm-displaced geodesic icosphere (200,000 triangles, 4 Lambertian/Phong regions)
 over a 512x512 fBm heightfield (522,242 triangles), BVHs built by the restated reference builder,
 depth 8, ACES; seeded synthetic data (the reference publishes no scenes).
@@ -13,9 +13,10 @@ depth 8, ACES; seeded synthetic data (the reference publishes no scenes).
           stream, L2 flushed between steps with a 256 MiB write);
   e2e   : the same metric through the C-ABI as the reference's render loop uses it
           (dfpt_set_camera from host memory, dfpt_render, dfpt_read_bgra8 into host memory);
-  roofline : the dominant kernel (closest-hit traversal), algorithmic bytes per segment =
-          nodes*32 + triangles*48 + 64 with the mean visit counts measured by the CPU
-          restatement on the cpu_baseline sample, against MEASURED_PEAKS.json's HBM copy rate;
+  roofline : the dominant kernel (closest-hit traversal), algorithmic bytes per closest-hit
+          segment = nodes*32 + triangles*48 + 64 with the mean visit counts of closest-hit
+          segments measured by the CPU restatement on the cpu_baseline sample, against
+          MEASURED_PEAKS.json's HBM copy rate;
   cpu_baseline : the oracle's strict-FP32 restatement of the reference kernel on all host cores,
           over a bounded band of rows (the reference's Java thread-pool path needs a JVM).
 --impl reference times that CPU restatement alone on the same workload and metric.
@@ -25,6 +26,7 @@ the data path); value sums the ranks' samples over the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import math
 import json
 import os
 import subprocess
@@ -141,10 +143,17 @@ def cpu_baseline(scene, sky, params, width, height, seconds, threads=0):
     dt = time.perf_counter() - t0
     target = min(height, max(rows, int(rows * seconds / max(dt, 1e-3))))
     r0 = max(0, height // 2 - target // 2)
-    t0 = time.perf_counter()
-    out = oracle.render(scene, sky, p, width, height, passes=1, precision=32, threads=threads, rows=(r0, r0 + target))
-    dt = time.perf_counter() - t0
-    samples = target * width
+    passes = 1
+    for _ in range(3):
+        t0 = time.perf_counter()
+        out = oracle.render(scene, sky, p, width, height, passes=passes, precision=32, threads=threads,
+                            rows=(r0, r0 + target))
+        dt = time.perf_counter() - t0
+        # A whole frame that takes well under `seconds` is rendered for more passes (1 spp each).
+        if target < height or dt >= 0.5 * seconds or passes >= 256:
+            break
+        passes = min(256, int(math.ceil(passes * seconds / max(dt, 1e-3))))
+    samples = target * width * passes
     c = out["counters"].astype(float)
     segs = c[0] + c[1]
     return {
@@ -152,11 +161,13 @@ def cpu_baseline(scene, sky, params, width, height, seconds, threads=0):
         "unit": UNIT,
         "cores": threads,
         "kind": "port",
-        "sample": f"rows {r0}..{r0 + target} of {width}x{height}, 1 pass (1 spp), strict FP32 restatement, "
+        "sample": f"rows {r0}..{r0 + target} of {width}x{height}, {passes} pass(es) of 1 spp, strict FP32 restatement, "
                   f"{threads} threads, {dt:.1f} s",
         "segments_per_sample": segs / samples,
         "nodes_per_segment": c[2] / max(segs, 1),
         "tris_per_segment": c[3] / max(segs, 1),
+        "closest_nodes_per_segment": c[4] / max(c[0], 1),
+        "closest_tris_per_segment": c[5] / max(c[0], 1),
         "closest_per_sample": c[0] / samples,
     }
 
@@ -583,8 +594,10 @@ def main():
     peak_note = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
     closest_segments = cnt[0]
-    nodes_per_seg = cpu["nodes_per_segment"] if cpu else (cnt[2] / max(cnt[0] + cnt[1], 1))
-    tris_per_seg = cpu["tris_per_segment"] if cpu else (cnt[3] / max(cnt[0] + cnt[1], 1))
+    # Visits per closest-hit segment (the timed kernel's work): the CPU restatement's counts on its
+    # sample when it ran, else the GPU's own counters (the same algorithm visits the same nodes).
+    nodes_per_seg = cpu["closest_nodes_per_segment"] if cpu else cnt[4] / max(cnt[0], 1)
+    tris_per_seg = cpu["closest_tris_per_segment"] if cpu else cnt[5] / max(cnt[0], 1)
     bytes_per_seg = nodes_per_seg * 32 + tris_per_seg * 48 + 64
     # Closest-hit segments of one step (counters over a step) x algorithmic bytes per segment,
     # over the closest-hit traversal time of a step (events inside the profiled loop).

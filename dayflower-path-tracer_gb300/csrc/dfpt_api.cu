@@ -1250,7 +1250,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     TRY_R(h->q_hit.alloc(n));
     TRY_R(h->throughput.alloc(n)); TRY_R(h->radiance.alloc(n)); TRY_R(h->rng.alloc(n)); TRY_R(h->pixel_flags.alloc(n));
     TRY_R(h->primary_o.alloc(n)); TRY_R(h->primary_d.alloc(n));
-    TRY_R(h->counts.alloc(DFPT_COUNTS_SIZE)); TRY_R(h->stats.alloc(4)); TRY_R(h->pass_index.alloc(1)); TRY_R(h->mean.alloc(3));
+    TRY_R(h->counts.alloc(DFPT_COUNTS_SIZE)); TRY_R(h->stats.alloc(6)); TRY_R(h->pass_index.alloc(1)); TRY_R(h->mean.alloc(3));
     TRY_R(h->film_sum.alloc(n)); TRY_R(h->film_comp.alloc(n)); TRY_R(h->film_n.alloc(n)); TRY_R(h->bgra.alloc(n * 4));
     TRY_R(h->primitive_offsets.alloc(n));
     TRY_R(h->hit_prim.alloc(n)); TRY_R(h->hit_type.alloc(n)); TRY_R(h->hit_off.alloc(n)); TRY_R(h->hit_dist.alloc(n)); TRY_R(h->hit_normal.alloc(3 * n));
@@ -1261,7 +1261,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     TRY_R(cudaMemsetAsync(h->film_n.p, 0, n * sizeof(int), st));
     TRY_R(cudaMemsetAsync(h->primitive_offsets.p, 0xFF, n * sizeof(int), st));  // Arrays.fill(-1) (GRK:421)
     TRY_R(cudaMemsetAsync(h->hit_normal.p, 0, 3 * n * sizeof(float), st));
-    TRY_R(cudaMemsetAsync(h->stats.p, 0, 4 * sizeof(unsigned long long), st));
+    TRY_R(cudaMemsetAsync(h->stats.p, 0, 6 * sizeof(unsigned long long), st));
     TRY_R(cudaMemsetAsync(h->pass_index.p, 0, sizeof(int), st));
     TRY_R(cudaMemsetAsync(h->pixel_flags.p, 0, n * sizeof(int), st));
     DevPass& B = h->pass;
@@ -1475,7 +1475,7 @@ int dfpt_clear(dfpt_handle* h) {
 int dfpt_render(dfpt_handle* h, int32_t passes) {
     if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
     if (passes < 0) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "passes < 0");
-    if (h->counting) CUDA_TRY(cudaMemsetAsync(h->stats.p, 0, 4 * sizeof(unsigned long long), h->stream));
+    if (h->counting) CUDA_TRY(cudaMemsetAsync(h->stats.p, 0, 6 * sizeof(unsigned long long), h->stream));
     if (passes == 0) return DFPT_OK;
     h->events_used = 0;
     {
@@ -1719,12 +1719,12 @@ int dfpt_l2_reset(void) {
     return DFPT_OK;
 }
 
-int dfpt_read_counters(dfpt_handle* h, uint64_t* c4) {
-    if (!h || !c4) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
-    unsigned long long v[4];
+int dfpt_read_counters(dfpt_handle* h, uint64_t* c6) {
+    if (!h || !c6) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
+    unsigned long long v[6];
     CUDA_TRY(cudaMemcpyAsync(v, h->stats.p, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
-    for (int i = 0; i < 4; ++i) c4[i] = v[i];
+    for (int i = 0; i < 6; ++i) c6[i] = v[i];
     return DFPT_OK;
 }
 

@@ -123,9 +123,9 @@ int batch_prepare(dfpt_batch* b) {
         if (!b->d_wave_entries.p) CUDA_TRY(b->d_wave_entries.alloc(1));
         if (!b->counts.p) CUDA_TRY(b->counts.alloc(DFPT_COUNTS_SIZE));
         if (!b->pass_index.p) CUDA_TRY(b->pass_index.alloc(1));
-        if (!b->stats.p) CUDA_TRY(b->stats.alloc(4));
+        if (!b->stats.p) CUDA_TRY(b->stats.alloc(6));
         CUDA_TRY(cudaMemsetAsync(b->pass_index.p, 0, sizeof(int), st));
-        CUDA_TRY(cudaMemsetAsync(b->stats.p, 0, 4 * sizeof(unsigned long long), st));
+        CUDA_TRY(cudaMemsetAsync(b->stats.p, 0, 6 * sizeof(unsigned long long), st));
         const size_t pixels = (size_t)b->film_begin.back();
         b->film_sum.release(); b->film_comp.release(); b->film_n.release(); b->bgra.release();
         CUDA_TRY(b->film_sum.alloc(pixels));

@@ -459,6 +459,8 @@ __device__ __forceinline__ void warp_add_stats(const DevParams& P, unsigned long
         if (sa) atomicAdd(stats + which, sa);
         if (sb) atomicAdd(stats + 2, sb);
         if (sc) atomicAdd(stats + 3, sc);
+        if (which == 0 && sb) atomicAdd(stats + 4, sb);  // closest-hit share
+        if (which == 0 && sc) atomicAdd(stats + 5, sc);
     }
 }
 

@@ -152,7 +152,7 @@ class RendererKernel:
         check(self._lib.dfpt_set_graphs(self._need(), 1 if enabled else 0))
 
     def counters(self) -> np.ndarray:
-        c = np.empty(4, np.uint64)
+        c = np.empty(6, np.uint64)
         check(self._lib.dfpt_read_counters(self._need(), ptr(c, C.c_uint64)))
         return c
 

@@ -193,8 +193,9 @@ int dfpt_read_hits(dfpt_handle* handle, int32_t* primitive_offset, int32_t* shap
                    int32_t* shape_offset, float* distance, float* normal3);
 
 /* Ray-segment counters of the last dfpt_render call: closest-hit segments, any-hit segments,
- * BVH nodes visited and triangles tested (summed over all segments). */
-int dfpt_read_counters(dfpt_handle* handle, uint64_t* counters4);
+ * BVH nodes visited and triangles tested (summed over all segments), then the nodes and the
+ * triangles of the closest-hit segments alone. */
+int dfpt_read_counters(dfpt_handle* handle, uint64_t* counters6);
 /* Enables (1) or disables (0, the default) the traversal counters; counting costs atomics. */
 int dfpt_set_counting(dfpt_handle* handle, int32_t enabled);
 

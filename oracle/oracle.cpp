@@ -123,7 +123,7 @@ template <typename R> struct Isect {
     R px, py, pz, nx, ny, nz, u, v, tx, ty, tz;  // point, shading normal, UV, tangent
 };
 
-struct Counters { uint64_t closest = 0, any = 0, nodes = 0, tris = 0; };
+struct Counters { uint64_t closest = 0, any = 0, nodes = 0, tris = 0, closest_nodes = 0, closest_tris = 0; };
 
 // Differentiable-rendering inputs (per primitive: albedo multiplier, added emission, Phong
 // exponent) and the record of one path, for the FP64 host adjoint.
@@ -388,6 +388,7 @@ template <typename R> struct Kernel {
                     const int at = abs_off + rel;
                     const int* B = d->bounding_volume_hierarchies;
                     cnt.nodes++;
+                    if (!testing) cnt.closest_nodes++;
                     const R mnX = S.p3(B[at + 2]), mnY = S.p3(B[at + 2] + 1), mnZ = S.p3(B[at + 2] + 2);
                     const R mxX = S.p3(B[at + 3]), mxY = S.p3(B[at + 3] + 1), mxZ = S.p3(B[at + 3] + 2);
                     const R t0X = (mnX - oXo) * iX, t0Y = (mnY - oYo) * iY, t0Z = (mnZ - oZo) * iZ;
@@ -406,6 +407,7 @@ template <typename R> struct Kernel {
                             R a[3], b[3], c[3];
                             tri_positions(toff, a, b, c);
                             cnt.tris++;
+                            if (!testing) cnt.closest_tris++;
                             current = isect_triangle(oXo, oYo, oZo, dXo, dYo, dZo, a[0], a[1], a[2], b[0], b[1], b[2], c[0], c[1], c[2], (R)0.001f, closest);
                             if (current < closest) { closest = current; cMatrix = mo; cPrim = po; cType = DFPT_SHAPE_TRIANGLE; cOff = toff; }
                             if (testing && cPrim != -1) return closest;
@@ -426,6 +428,7 @@ template <typename R> struct Kernel {
                 R a[3], b[3], c[3];
                 tri_positions(off, a, b, c);
                 cnt.tris++;
+                if (!testing) cnt.closest_tris++;
                 current = isect_triangle(oXo, oYo, oZo, dXo, dYo, dZo, a[0], a[1], a[2], b[0], b[1], b[2], c[0], c[1], c[2], (R)0.001f, closest);
             }
             if (current < closest) { closest = current; cMatrix = mo; cPrim = po; cType = type; cOff = off; }
@@ -1260,6 +1263,8 @@ void render_rows(const Scene& S, int pass_begin, int passes, int row_begin, int 
     total.any += k.cnt.any;
     total.nodes += k.cnt.nodes;
     total.tris += k.cnt.tris;
+    total.closest_nodes += k.cnt.closest_nodes;
+    total.closest_tris += k.cnt.closest_tris;
 }
 
 template <typename R>
@@ -1286,6 +1291,7 @@ int render(const Scene& S, int pass_begin, int passes, int threads, int row_begi
     if (o.counters) {
         for (auto& c : counters) {
             o.counters[0] += c.closest; o.counters[1] += c.any; o.counters[2] += c.nodes; o.counters[3] += c.tris;
+            o.counters[4] += c.closest_nodes; o.counters[5] += c.closest_tris;
         }
     }
     return 0;

@@ -61,7 +61,7 @@ def render(scene, sky, params, width, height, passes=1, precision=64, threads=0,
         "sum": np.zeros(n * 3, np.float64),
         "sumsq": np.zeros(n * 3, np.float64),
         "primitive_offsets": np.full(n, -1, np.int32),
-        "counters": np.zeros(4, np.uint64),
+        "counters": np.zeros(6, np.uint64),
     }
     if want_bgra:
         out["bgra"] = np.zeros(n * 4, np.uint8)
