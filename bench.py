@@ -41,6 +41,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "M path samples/s @1080p"
 UNIT = "M samples/s"
+# Measured DRAM bytes (read + write) per closest-hit segment of the traversal kernel on
+# mesh_scene: one ncu capture at 960x540 (profiles/k_trace_dram_mesh_scene_960x540.md).
+TRACE_DRAM_BYTES_PER_SEGMENT = 65.5
 
 
 def parse():
@@ -594,11 +597,14 @@ def main():
     peak_note = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
     closest_segments = cnt[0]
-    # Visits per closest-hit segment (the timed kernel's work): the CPU restatement's counts on its
-    # sample when it ran, else the GPU's own counters (the same algorithm visits the same nodes).
-    nodes_per_seg = cpu["closest_nodes_per_segment"] if cpu else cnt[4] / max(cnt[0], 1)
-    tris_per_seg = cpu["closest_tris_per_segment"] if cpu else cnt[5] / max(cnt[0], 1)
+    # Visits per closest-hit segment, the timed kernel's work: the GPU's own counters over a step.
+    # Without primitive culling they equal the reference algorithm's (the CPU restatement's counts
+    # on its sample are reported beside them); with culling the GPU skips primitives the reference
+    # tests, and the roofline counts only the work done.
+    nodes_per_seg = cnt[4] / max(cnt[0], 1)
+    tris_per_seg = cnt[5] / max(cnt[0], 1)
     bytes_per_seg = nodes_per_seg * 32 + tris_per_seg * 48 + 64
+    oracle_bytes_per_seg = (cpu["closest_nodes_per_segment"] * 32 + cpu["closest_tris_per_segment"] * 48 + 64) if cpu else None
     # Closest-hit segments of one step (counters over a step) x algorithmic bytes per segment,
     # over the closest-hit traversal time of a step (events inside the profiled loop).
     avg_trace_ms = trace_ms / max(trace_n, 1)
@@ -606,13 +612,12 @@ def main():
     launches_per_step = max(trace_n / args.steps, 1)
     bytes_per_launch = closest_segments / launches_per_step * bytes_per_seg
     achieved = closest_segments * bytes_per_seg / (trace_ms_per_step / 1e3) / 1e9
+    # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum per closest-hit
+    # segment of the mesh_scene traversal at 960x540 (profiles/k_trace_dram_mesh_scene_960x540.md),
+    # scaled by this run's segments per launch (the traffic grows with the rays of a launch).
     traffic = None
-    tf = ROOT / "profiles" / "trace_traffic.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get("bytes_per_launch_full")
-        except ValueError:
-            traffic = None
+    if args.workload == "mesh_scene" and TRACE_DRAM_BYTES_PER_SEGMENT:
+        traffic = TRACE_DRAM_BYTES_PER_SEGMENT * closest_segments / launches_per_step
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -635,7 +640,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": peak_note,
                      "kernel": "k_trace<closest>", "avg_launch_ms": avg_trace_ms,
-                     "bytes_per_segment": bytes_per_seg, "segments_per_launch": closest_segments / launches_per_step,
+                     "bytes_per_segment": bytes_per_seg, "oracle_bytes_per_segment": oracle_bytes_per_seg,
+                     "nodes_per_segment": nodes_per_seg, "triangles_per_segment": tris_per_seg,
+                     "segments_per_launch": closest_segments / launches_per_step,
                      "segments_per_step": closest_segments},
         "kernels_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in kind_ms.items() if v[1]},
         "ms_per_step_profiled": sum(prof_ms) / len(prof_ms),

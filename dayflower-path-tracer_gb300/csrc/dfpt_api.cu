@@ -114,12 +114,15 @@ int float_bits_int(float f) {
     return i;
 }
 
-int add_tri_record(const HostScene& s, Derived& d, int off, bool last) {
+// Triangle record: {a, triangle offset}, {b - a, last in its leaf}, {c - a, node index of its leaf}
+// (the compact pair walk resumes the threaded order from a leaf it took off its stack; 0 for
+// triangle primitives).
+int add_tri_record(const HostScene& s, Derived& d, int off, bool last, int leaf_node = 0) {
     const float* P = s.point3fs.data();
     const int a = s.triangles[off], b = s.triangles[off + 1], c = s.triangles[off + 2];
     d.tris.push_back(make_float4(P[a], P[a + 1], P[a + 2], int_bits(off)));
     d.tris.push_back(make_float4(P[b] - P[a], P[b + 1] - P[a + 1], P[b + 2] - P[a + 2], int_bits(last ? 1 : 0)));
-    d.tris.push_back(make_float4(P[c] - P[a], P[c + 1] - P[a + 1], P[c + 2] - P[a + 2], 0.0f));
+    d.tris.push_back(make_float4(P[c] - P[a], P[c + 1] - P[a + 1], P[c + 2] - P[a + 2], int_bits(leaf_node)));
     return (int)(d.tris.size() / 3) - 1;
 }
 
@@ -172,7 +175,7 @@ int convert_bvh(const HostScene& s, Derived& d, int root, int& first_node) {
                     const int toff = s.bvh[at + 5 + k];
                     int r = check_triangle(s, toff);
                     if (r) return r;
-                    const int rec = add_tri_record(s, d, toff, k == cnt - 1);
+                    const int rec = add_tri_record(s, d, toff, k == cnt - 1, first_node + (int)i);
                     if (k == 0) leaf = rec;
                 }
             }
@@ -1124,10 +1127,11 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
         // scene keeps the threaded walk alone.
         const size_t nn = d.nodes.size() / 2;
         std::vector<float4> pairs(4 * nn, make_float4(0, 0, 0, 0));
-        bool full_binary = true;
+        bool full_binary = true, empty_leaf = false;
         auto next_of = [&](size_t n) { return float_bits_int(d.nodes[2 * n].w); };
         auto leaf_of = [&](size_t n) { return float_bits_int(d.nodes[2 * n + 1].w); };
         for (size_t n = 0; n < nn && full_binary; ++n) {
+            if (leaf_of(n) == -2) empty_leaf = true;
             if (leaf_of(n) != -1) continue;
             const size_t l = n + 1;
             const int r = l < nn ? next_of(l) : -1;
@@ -1138,7 +1142,8 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
             pairs[4 * n + 2] = make_float4(ro.z, rh.x, rh.y, rh.z);
             pairs[4 * n + 3] = make_float4(lh.w, rh.w, int_bits(r), 0.0f);
         }
-        st.scene.use_pairs = full_binary ? 1 : 0;
+        st.scene.use_pairs = full_binary ? (empty_leaf ? 1 : 2) : 0;
+        st.scene.pair_stack = 8;
         CUDA_TRY(upload(st.pairs, pairs, s));
         CUDA_TRY(cudaStreamSynchronize(s));
     }
@@ -1426,6 +1431,15 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
     h->wide_graph_valid = false;
         return apply_l2_policy(h);
     }
+    if (std::strcmp(key, "pair_stack") == 0) {
+        // Stack entries of the compact pair walk (trace configuration 16); fewer entries take its
+        // overflow path more often, with the same hits and visits.
+        if (value < 1 || value > 8) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "pair_stack %d outside [1, 8]", value);
+        h->sc.scene.pair_stack = value;
+        h->graph_valid = false;
+        h->wide_graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "primitive_culling") == 0) {
         if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
         scene_set_culling(h->sc, value);
@@ -1441,6 +1455,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "trace_config") == 0) { *value = h->ctx.trace_config; return DFPT_OK; }
     if (std::strcmp(key, "trace_configs") == 0) { *value = h->fast.trace_configs; return DFPT_OK; }
     if (std::strcmp(key, "primitive_culling") == 0) { *value = h->sc.scene.use_culling; return DFPT_OK; }
+    if (std::strcmp(key, "pair_stack") == 0) { *value = h->sc.scene.pair_stack; return DFPT_OK; }
     if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }

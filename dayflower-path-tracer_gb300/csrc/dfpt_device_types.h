@@ -27,11 +27,13 @@ struct DevScene {
     // Derived records.
     const int4* prim_info;  // {shape type, shape offset, surface offset, record index}
     const float4* nodes;    // 2 per BVH node: {min.xyz, next}, {max.xyz, first triangle or -1}
-    const float4* tris;     // 3 per triangle: {a.xyz, triangle offset}, {b-a, last-in-leaf}, {c-a, 0}
+    const float4* tris;     // 3 per triangle: {a.xyz, triangle offset}, {b-a, last-in-leaf}, {c-a, leaf node index}
     const float4* pairs;    // 4 per BVH node, filled for inner nodes N: the boxes of children L = N + 1 and
                             // R = next(L): {L.min.xyz, L.max.x}, {L.max.yz, R.min.xy}, {R.min.z, R.max.xyz},
                             // {L first triangle, R first triangle, R index, 0} (-1 inner, -2 empty leaf)
-    int use_pairs;          // every mesh BVH is a full binary tree, so pair records describe the walk
+    int use_pairs;          // 1: every mesh BVH is a full binary tree, so pair records describe the walk;
+                            // 2: the same, and no leaf is empty (the compact pair walk's condition)
+    int pair_stack;         // entries of the compact pair walk's stack in use (1..8; 8 unless a test lowers it)
     const float4* sphere4;  // {position.xyz, radius} per sphere record
     const float4* plane_a;  // point A per plane record
     const float4* plane_n;  // surface normal per plane record

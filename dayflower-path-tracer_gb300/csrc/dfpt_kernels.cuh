@@ -633,12 +633,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S0, const DevPar
             const bool valid = i < n;
             float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
             if (valid) {
-                o = qo[i];
-                d = qd[i];
+                // Streaming accesses: each ray and hit is touched once here, and the BVH records
+                // keep the L1.
+                o = __ldcs(qo + i);
+                d = __ldcs(qd + i);
             }
             const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
             const Hit h = trace_v<ANY, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            if (valid) B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
+            if (valid) __stcs(B.q_hit + i, make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset));
             warp_add_stats(P, B.stats, ANY ? 1 : 0, valid ? 1u : 0u, st.nodes, st.tris);
         }
     }
@@ -1579,7 +1581,7 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
     X(0, 0, 256, 4) X(1, 1, 256, 4) X(2, 1, 256, 3) X(3, 0, 128, 8) X(4, 2, 256, 4) X(5, 2, 128, 8) X(6, 2, 256, 3) \
     X(7, 3, 256, 4) X(8, 3, 128, 8) X(9, 3, 256, 3) X(10, 3, 256, 2) \
     X(11, 0, 256, 6) X(12, 1, 256, 6) X(13, 0, 256, 8) X(14, 1, 256, 8) \
-    X(15, 4, 256, 4)
+    X(15, 4, 256, 4) X(16, 5, 256, 4)
 
 // The scene argument of the batch stages: the context's scene in a one-scene set, else none (the
 // kernels read each item's scene from the batch).
@@ -1779,7 +1781,9 @@ KernelSet kernel_set() {
     k.init_tables = launch_init_tables;
     k.occupancy = occupancy;
     k.trace_grid = trace_grid;
-    k.trace_configs = 16;
+#define X(id, v, b, m) +1
+    k.trace_configs = 0 TRACE_CONFIGS(X);
+#undef X
 #ifdef DFPT_EXTENDED_KERNELS
     k.b_camera = launch_b_camera;
     k.b_trace_closest = launch_b_closest;
