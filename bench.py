@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the inverse-rendering leg")
     ap.add_argument("--adjoint-iters", type=int, default=10)
     ap.add_argument("--trace-config", type=int, default=-1, help="fixed traversal configuration (skips the autotuner)")
+    ap.add_argument("--set-tuning", action="append", default=[], metavar="KEY=VALUE",
+                    help="a dfpt_set_tuning key applied after the traversal configuration is chosen (repeatable)")
     ap.add_argument("--wide", type=int, default=0, help="fixed passes per wave (skips that tuner)")
     ap.add_argument("--shadow-defer", type=int, default=-1, help="with --wide: 1 one shadow launch per wave, 0 per bounce")
     return ap.parse_args()
@@ -483,6 +485,9 @@ def main():
         tuning = {"best": args.trace_config, "ms_per_pass": {}}
     else:
         tuning = tune_trace(k, passes=S, warmup=1)
+    for kv in args.set_tuning:
+        key, val = kv.split("=", 1)
+        k.set_tuning(key, int(val))
     for _ in range(args.warmup):
         k.execute(S)
     k.synchronize()
@@ -633,7 +638,8 @@ def main():
                    "l2_persist": tuning.get("l2_persist", 0),
                    "l2_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("l2_ms_per_pass", {}).items()},
                    "culling_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("culling_ms_per_pass", {}).items()},
-                   "trace_config_ms": {str(kk): round(v, 3) for kk, v in tuning["ms_per_pass"].items()}},
+                   "trace_config_ms": {str(kk): round(v, 3) for kk, v in tuning["ms_per_pass"].items()},
+                   "set_tuning": args.set_tuning},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4,
                 "loop": "dfpt_set_camera(pinned host) + dfpt_render(S passes) + dfpt_read_bgra8(pinned host) per step"},
         "gpu_launches": int(launches),

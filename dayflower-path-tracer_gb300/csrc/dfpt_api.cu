@@ -1431,6 +1431,19 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
     h->wide_graph_valid = false;
         return apply_l2_policy(h);
     }
+    if (std::strcmp(key, "trace_carveout") == 0) {
+        // Shared-memory carveout preference of the current configuration's closest-hit traversal
+        // kernels (percent of the maximum; -1 the driver's choice). A process-wide attribute of
+        // those kernels: it applies to every handle that uses them.
+        if (value < -1 || value > 100) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "trace_carveout %d outside [-1, 100]", value);
+        for (const KernelSet* ks : {&h->fast, &h->strict, &h->wide})
+            if (ks->trace_carveout) ks->trace_carveout(h->ctx.trace_config, value);
+        CUDA_TRY(cudaGetLastError());
+        h->ctx.grid_trace = kset(h).trace_grid(h->ctx.trace_config, h->sms);
+        h->graph_valid = false;
+        h->wide_graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "pair_stack") == 0) {
         // Stack entries of the compact pair walk (trace configuration 16); fewer entries take its
         // overflow path more often, with the same hits and visits.

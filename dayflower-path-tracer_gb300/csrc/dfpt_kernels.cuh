@@ -1593,6 +1593,14 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
 
 template <int V, int BLOCK, int MINB>
 struct TraceCfg {
+    static void carveout(int percent) {
+#ifndef DFPT_ONE_SCENE
+        cudaFuncSetAttribute(k_trace<false, false, V, BLOCK, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+#endif
+#ifdef DFPT_EXTENDED_KERNELS
+        cudaFuncSetAttribute(k_trace<true, false, (V == 2 ? 1 : V), BLOCK, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+#endif
+    }
 #ifndef DFPT_ONE_SCENE
     static void closest(const LaunchCtx& c, int bounce) {
         k_trace<false, false, V, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, bounce, c.pass->sorted_queues ? 0 : (bounce & 1));
@@ -1657,6 +1665,14 @@ static void launch_final(const LaunchCtx& c, int bounce) {
     }
 }
 #endif
+static void trace_carveout(int config, int percent) {
+    switch (config) {
+#define X(id, v, b, m) case id: TraceCfg<v, b, m>::carveout(percent); break;
+        TRACE_CONFIGS(X)
+#undef X
+        default: break;
+    }
+}
 static int trace_grid(int config, int sms) {
     switch (config) {
 #define X(id, v, b, m) case id: return TraceCfg<v, b, m>::grid(sms);
@@ -1781,6 +1797,7 @@ KernelSet kernel_set() {
     k.init_tables = launch_init_tables;
     k.occupancy = occupancy;
     k.trace_grid = trace_grid;
+    k.trace_carveout = trace_carveout;
 #define X(id, v, b, m) +1
     k.trace_configs = 0 TRACE_CONFIGS(X);
 #undef X

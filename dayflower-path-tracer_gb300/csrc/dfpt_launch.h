@@ -30,6 +30,9 @@ struct KernelSet {
     void (*init_tables)(cudaStream_t, const int* perm256, const float* grad36);
     void (*occupancy)(int sms, int& grid, int& grid_trace, int& grid_simple);
     int (*trace_grid)(int config, int sms);
+    // Shared-memory carveout preference (percent of the maximum, -1 the driver's choice) of the
+    // closest-hit traversal kernels of one configuration.
+    void (*trace_carveout)(int config, int percent);
     int trace_configs;
     // Batch stages (the fast kernel set only; null elsewhere). The int is the bounce where it applies.
     void (*b_camera)(const LaunchCtx&, int) = nullptr;
