@@ -67,8 +67,9 @@ def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=N
                verbose: bool = False) -> dict:
     """Picks the batch's wave capacity (queue depth) and traversal configuration (block size x
     resident blocks x walk variant) by timing the same window of the batch's own samples with
-    each candidate. The traversal is stackless (threaded BVH with skip pointers), so there is no
-    stack depth to choose. Leaves the films cleared and the best candidate set."""
+    each candidate. The walks' stack depth is fixed (the threaded walks keep none; the pair walks
+    keep 8 entries and fall back to the threaded records when those run out), so it is not a
+    candidate. Leaves the films cleared and the best candidate set."""
     total = batch.total_samples
     if configs is None:
         # Walk variant 2 (warp-synchronous) maps to the per-lane walk in a batch; skip duplicates.
