@@ -1056,7 +1056,7 @@ void SceneStore::release() {
     for (auto* b : fb) b->release();
     DevBuf<int>* ib[] = {&planes, &triangles, &primitives};
     for (auto* b : ib) b->release();
-    DevBuf<float4>* f4[] = {&trav, &pairs, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
+    DevBuf<float4>* f4[] = {&trav, &pairs, &shade_tris, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
     for (auto* b : f4) b->release();
     prim_info.release();
     cull_prims.release();
@@ -1147,6 +1147,46 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
         CUDA_TRY(upload(st.pairs, pairs, s));
         CUDA_TRY(cudaStreamSynchronize(s));
     }
+    {
+        // Shading records: the triangle's vertex values in one 144-byte record, indexed by triangle
+        // offset / 12, when every triangle the traversal can report sits at a multiple of 12.
+        bool aligned = true;
+        for (size_t k = 0; k < d.tris.size(); k += 3)
+            if (float_bits_int(d.tris[k].w) % 12 != 0) aligned = false;
+        const size_t nt = h.triangles.size() / 12;
+        st.shade_tris.release();
+        if (aligned && nt > 0) {
+            std::vector<float4> rec(9 * nt, make_float4(0, 0, 0, 0));
+            auto ok3 = [&](int i, size_t n) { return i >= 0 && (size_t)i + 3 <= n; };
+            for (size_t t = 0; t < nt; ++t) {
+                const int* T = h.triangles.data() + 12 * t;
+                bool valid = true;
+                for (int k = 0; k < 3; ++k) valid = valid && ok3(T[k], h.point3fs.size()) && ok3(T[3 + k], h.vector3fs.size()) &&
+                                                    ok3(T[9 + k], h.vector3fs.size()) && T[6 + k] >= 0 &&
+                                                    (size_t)T[6 + k] + 2 <= h.point2fs.size();
+                if (!valid) continue;  // never reported by the traversal (it reports validated triangles only)
+                const float* P = h.point3fs.data();
+                const float* V = h.vector3fs.data();
+                const float* U = h.point2fs.data();
+                const float* a = P + T[0]; const float* b = P + T[1]; const float* c = P + T[2];
+                const float* na = V + T[3]; const float* nb = V + T[4]; const float* nc = V + T[5];
+                const float* ua = U + T[6]; const float* ub = U + T[7]; const float* uc = U + T[8];
+                const float* ga = V + T[9]; const float* gb = V + T[10]; const float* gc = V + T[11];
+                float4* R = rec.data() + 9 * t;
+                R[0] = make_float4(a[0], a[1], a[2], b[0]);
+                R[1] = make_float4(b[1], b[2], c[0], c[1]);
+                R[2] = make_float4(c[2], ua[0], ua[1], ub[0]);
+                R[3] = make_float4(ub[1], uc[0], uc[1], na[0]);
+                R[4] = make_float4(na[1], na[2], nb[0], nb[1]);
+                R[5] = make_float4(nb[2], nc[0], nc[1], nc[2]);
+                R[6] = make_float4(ga[0], ga[1], ga[2], gb[0]);
+                R[7] = make_float4(gb[1], gb[2], gc[0], gc[1]);
+                R[8] = make_float4(gc[2], 0.0f, 0.0f, 0.0f);
+            }
+            CUDA_TRY(upload(st.shade_tris, rec, s));
+            CUDA_TRY(cudaStreamSynchronize(s));
+        }
+    }
     CUDA_TRY(upload(st.sphere4, d.sphere4, s));
     CUDA_TRY(upload(st.plane_a, d.plane_a, s));
     CUDA_TRY(upload(st.plane_n, d.plane_n, s));
@@ -1160,6 +1200,7 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     S.o2w = st.o2w.p; S.w2o = st.w2o.p; S.camera = st.camera.p;
     S.prim_info = st.prim_info.p; S.nodes = st.trav.p; S.tris = st.trav.p + st.trav_nodes; S.sphere4 = st.sphere4.p;
     S.pairs = st.pairs.p;
+    S.shade_tris = st.shade_tris.p;
     S.plane_a = st.plane_a.p; S.plane_n = st.plane_n.p;
     st.derived = Derived();
     return DFPT_OK;

@@ -34,6 +34,11 @@ struct DevScene {
     int use_pairs;          // 1: every mesh BVH is a full binary tree, so pair records describe the walk;
                             // 2: the same, and no leaf is empty (the compact pair walk's condition)
     int pair_stack;         // entries of the compact pair walk's stack in use (1..8; 8 unless a test lowers it)
+    const float4* shade_tris;  // per triangle (triangle offset / 12), the values surface() reads, copied from
+                               // point3fs / point2fs / vector3fs: {a.xyz, b.x}, {b.yz, c.xy}, {c.z, uva.xy, uvb.x},
+                               // {uvb.y, uvc.xy, na.x}, {na.yz, nb.xy}, {nb.z, nc.xyz}, {tga.xyz, tgb.x},
+                               // {tgb.yz, tgc.xy}, {tgc.z, 0, 0, 0}; null when some triangle offset is not a
+                               // multiple of 12 (surface() then follows the reference's indices)
     const float4* sphere4;  // {position.xyz, radius} per sphere record
     const float4* plane_a;  // point A per plane record
     const float4* plane_n;  // surface normal per plane record

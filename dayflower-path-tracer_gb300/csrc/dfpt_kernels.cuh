@@ -101,8 +101,25 @@ __device__ Surf surface(const DevScene& S, const DevParams& P, float ox, float o
         s.nx = nx * r; s.ny = ny * r; s.nz = nz * r;
         s.u = s.px; s.v = s.pz;
     } else {  // Triangle
+        // The vertex values come from the triangle's shading record (one contiguous 144-byte
+        // record, the same floats) when the scene has them, else through the reference's indices.
         const int* T = S.triangles + off;
-        const float3 a = p3(S, __ldg(T + 0)), b = p3(S, __ldg(T + 1)), c = p3(S, __ldg(T + 2));
+        const float4* R = S.shade_tris ? S.shade_tris + 9 * (size_t)(off / 12) : nullptr;
+        float3 a, b, c;
+        float uax, uay, ubx, uby, ucx, ucy;
+        if (R) {
+            const float4 r0 = __ldg(R), r1 = __ldg(R + 1), r2 = __ldg(R + 2), r3 = __ldg(R + 3);
+            a = make_float3(r0.x, r0.y, r0.z);
+            b = make_float3(r0.w, r1.x, r1.y);
+            c = make_float3(r1.z, r1.w, r2.x);
+            uax = r2.y; uay = r2.z; ubx = r2.w; uby = r3.x; ucx = r3.y; ucy = r3.z;
+        } else {
+            a = p3(S, __ldg(T + 0)); b = p3(S, __ldg(T + 1)); c = p3(S, __ldg(T + 2));
+            const int ta = __ldg(T + 6), tb = __ldg(T + 7), tc = __ldg(T + 8);
+            uax = __ldg(S.point2fs + ta); uay = __ldg(S.point2fs + ta + 1);
+            ubx = __ldg(S.point2fs + tb); uby = __ldg(S.point2fs + tb + 1);
+            ucx = __ldg(S.point2fs + tc); ucy = __ldg(S.point2fs + tc + 1);
+        }
         s.px = oxo + dxo * t; s.py = oyo + dyo * t; s.pz = ozo + dzo * t;
         const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
         const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
@@ -114,17 +131,28 @@ __device__ Surf surface(const DevScene& S, const DevParams& P, float ox, float o
         const float bu = (v1x * v0x + v1y * v0y + v1z * v0z) * dr;
         const float bv = (dxo * v2x + dyo * v2y + dzo * v2z) * dr;
         const float bw = 1.0f - bu - bv;
-        const int ta = __ldg(T + 6), tb = __ldg(T + 7), tc = __ldg(T + 8);
-        s.u = bw * __ldg(S.point2fs + ta) + bu * __ldg(S.point2fs + tb) + bv * __ldg(S.point2fs + tc);
-        s.v = bw * __ldg(S.point2fs + ta + 1) + bu * __ldg(S.point2fs + tb + 1) + bv * __ldg(S.point2fs + tc + 1);
+        s.u = bw * uax + bu * ubx + bv * ucx;
+        s.v = bw * uay + bu * uby + bv * ucy;
         float n0x = 0.0f, n0y = 0.0f, n0z = 0.0f, t0x = 0.0f, t0y = 0.0f, t0z = 0.0f;
         if (P.shader_type == DFPT_SHADER_FLAT) {
             n0x = aby * acz - abz * acy;
             n0y = abz * acx - abx * acz;
             n0z = abx * acy - aby * acx;
         } else if (P.shader_type == DFPT_SHADER_GOURAUD) {
-            const float3 na = v3(S, __ldg(T + 3)), nb = v3(S, __ldg(T + 4)), nc = v3(S, __ldg(T + 5));
-            const float3 tga = v3(S, __ldg(T + 9)), tgb = v3(S, __ldg(T + 10)), tgc = v3(S, __ldg(T + 11));
+            float3 na, nb, nc, tga, tgb, tgc;
+            if (R) {
+                const float4 r3 = __ldg(R + 3), r4 = __ldg(R + 4), r5 = __ldg(R + 5), r6 = __ldg(R + 6), r7 = __ldg(R + 7),
+                             r8 = __ldg(R + 8);
+                na = make_float3(r3.w, r4.x, r4.y);
+                nb = make_float3(r4.z, r4.w, r5.x);
+                nc = make_float3(r5.y, r5.z, r5.w);
+                tga = make_float3(r6.x, r6.y, r6.z);
+                tgb = make_float3(r6.w, r7.x, r7.y);
+                tgc = make_float3(r7.z, r7.w, r8.x);
+            } else {
+                na = v3(S, __ldg(T + 3)); nb = v3(S, __ldg(T + 4)); nc = v3(S, __ldg(T + 5));
+                tga = v3(S, __ldg(T + 9)); tgb = v3(S, __ldg(T + 10)); tgc = v3(S, __ldg(T + 11));
+            }
             n0x = na.x * bw + nb.x * bu + nc.x * bv;
             n0y = na.y * bw + nb.y * bu + nc.y * bv;
             n0z = na.z * bw + nb.z * bu + nc.z * bv;
@@ -991,12 +1019,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevPa
             const bool valid = i < n;
             float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
             if (valid) {
-                o = B.s_o[i];
-                d = B.s_d[i];
+                o = __ldcs(B.s_o + i);  // read once: streaming
+                d = __ldcs(B.s_d + i);
             }
             const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
             const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            if (valid && h.t >= INF - 0.0001f) unoccluded(i, o, B.s_c[i]);
+            if (valid && h.t >= INF - 0.0001f) unoccluded(i, o, __ldcs(B.s_c + i));
             warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
         }
     }

@@ -73,6 +73,7 @@ struct SceneStore {
     DevBuf<int4> prim_info;
     DevBuf<float4> trav;  // BVH nodes then triangles, one allocation (one L2 persistence window)
     DevBuf<float4> pairs;  // per node: the children's boxes (pair records, see DevScene::pairs)
+    DevBuf<float4> shade_tris;  // per triangle: the vertex values shading reads (see DevScene::shade_tris)
     size_t trav_nodes = 0;  // float4 records of nodes at the start of trav
     DevBuf<float4> sphere4, plane_a, plane_n;
     DevBuf<float4> cull_nodes, prim_box;
