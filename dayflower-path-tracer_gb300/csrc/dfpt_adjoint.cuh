@@ -261,8 +261,8 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
             h.prim = hr.y;
             h.shape_type = hr.z;
             h.shape_offset = hr.w;
-            float4 T = B.throughput[path];
-            float4 Lu = B.radiance[path];  // radiance gathered so far along the replay
+            float4 T = B.throughput[PSI(path)];
+            float4 Lu = B.radiance[PSI(path)];  // radiance gathered so far along the replay
             const float4 Lt = B.diff_L[sample * npix + pixel];
             float4 w = B.diff_dldi[pixel];
             w.x *= inv_spp; w.y *= inv_spp; w.z *= inv_spp;
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
                 sky_color_tan(P, d4.x, d4.y, d4.z, sr, sg, sb);
                 Lu.x += T.x * sr.v * INV_PI; Lu.y += T.y * sg.v * INV_PI; Lu.z += T.z * sb.v * INV_PI;
                 for (int j = 0; j < 4; ++j) gsky[j] += (w.x * T.x * sr.d[j] + w.y * T.y * sg.d[j] + w.z * T.z * sb.d[j]) * INV_PI;
-                B.radiance[path] = Lu;
+                B.radiance[PSI(path)] = Lu;
             } else {
                 Rng rng = make_rng(P, pixel, pass, B.rng[path]);
                 const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
@@ -337,8 +337,8 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
                     no = make_float4(sct.o.x, sct.o.y, sct.o.z, __int_as_float(path));
                     nd = make_float4(sct.d.x, sct.d.y, sct.d.z, 0.0f);
                 }
-                B.throughput[path] = T;
-                B.radiance[path] = Lu;
+                B.throughput[PSI(path)] = T;
+                B.radiance[PSI(path)] = Lu;
                 B.rng[path] = rng.state;
             }
         }
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(256) k_final_adj(DevScene S, const DevParams* 
         const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
         if (valid && !(h.t < INF)) {
             const int path = __float_as_int(o.w);
-            const float4 T = B.throughput[path];
+            const float4 T = B.throughput[PSI(path)];
             int pixel = path;
             if constexpr (BATCH) pixel = Q.slot_key[path].y;
             float4 w = B.diff_dldi[pixel];

@@ -430,7 +430,7 @@ struct dfpt_handle {
     DevParams dev_params_host{};
     DevBuf<DevParams> dev_params;
     // Pass buffers.
-    DevBuf<float4> q_o0, q_o1, q_d0, q_d1, s_o, s_d, s_c, throughput, radiance, primary_o, primary_d, film_sum, film_comp;
+    DevBuf<float4> q_o0, q_o1, q_d0, q_d1, s_o, s_d, s_c, throughput, primary_o, primary_d, film_sum, film_comp;
     DevBuf<int4> q_hit;
     DevBuf<uint64_t> rng;
     DevBuf<int> pixel_flags, counts, pass_index, film_n, primitive_offsets, hit_prim, hit_type, hit_off;
@@ -465,7 +465,7 @@ struct dfpt_handle {
     int wide_samples = 8;
     int wide_capacity = 0;
     size_t wide_shadow = 0;
-    DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput, w_radiance;
+    DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput;  // w_throughput: throughput + radiance records (PSI)
     DevBuf<int4> w_q_hit, w_slot_key;
     DevBuf<uint64_t> w_rng;
     DevBuf<int> w_pixel_flags, w_counts, w_wave_entries;
@@ -507,7 +507,7 @@ void release(dfpt_handle* h) {
     if (h->wide_graph) cudaGraphExecDestroy(h->wide_graph);
     h->wide_graph = nullptr;
     {
-        DevBuf<float4>* w4[] = {&h->w_q_o0, &h->w_q_o1, &h->w_q_d0, &h->w_q_d1, &h->w_s_o, &h->w_s_d, &h->w_s_c, &h->w_throughput, &h->w_radiance};
+        DevBuf<float4>* w4[] = {&h->w_q_o0, &h->w_q_o1, &h->w_q_d0, &h->w_q_d1, &h->w_s_o, &h->w_s_d, &h->w_s_c, &h->w_throughput};
         for (auto* b : w4) b->release();
         h->w_q_hit.release(); h->w_slot_key.release(); h->w_rng.release(); h->w_pixel_flags.release(); h->w_counts.release();
         h->w_wave_entries.release(); h->w_scene.release(); h->w_sample_begin.release(); h->w_film_begin.release();
@@ -522,7 +522,7 @@ void release(dfpt_handle* h) {
     for (auto* b : fb) b->release();
     DevBuf<int>* ib[] = {&h->pixel_flags, &h->counts, &h->pass_index, &h->film_n, &h->primitive_offsets, &h->hit_prim, &h->hit_type, &h->hit_off};
     for (auto* b : ib) b->release();
-    DevBuf<float4>* f4[] = {&h->q_o0, &h->q_o1, &h->q_d0, &h->q_d1, &h->s_o, &h->s_d, &h->s_c, &h->throughput, &h->radiance, &h->primary_o, &h->primary_d, &h->film_sum, &h->film_comp};
+    DevBuf<float4>* f4[] = {&h->q_o0, &h->q_o1, &h->q_d0, &h->q_d1, &h->s_o, &h->s_d, &h->s_c, &h->throughput, &h->primary_o, &h->primary_d, &h->film_sum, &h->film_comp};
     for (auto* b : f4) b->release();
     h->rng.release();
     h->bgra.release();
@@ -778,13 +778,13 @@ int wide_prepare(dfpt_handle* h) {
     // One bounce of shadow rays (traced before the next bounce), or every bounce's when deferred.
     const size_t shadow = (size_t)cap * (size_t)(h->shadow_defer ? bounces_of(h) : 1);
     if (cap != h->wide_capacity || shadow != h->wide_shadow) {
-        DevBuf<float4>* w4[] = {&h->w_q_o0, &h->w_q_o1, &h->w_q_d0, &h->w_q_d1, &h->w_s_o, &h->w_s_d, &h->w_s_c, &h->w_throughput, &h->w_radiance};
+        DevBuf<float4>* w4[] = {&h->w_q_o0, &h->w_q_o1, &h->w_q_d0, &h->w_q_d1, &h->w_s_o, &h->w_s_d, &h->w_s_c, &h->w_throughput};
         for (auto* b : w4) b->release();
         h->w_q_hit.release(); h->w_slot_key.release(); h->w_rng.release(); h->w_pixel_flags.release();
         const size_t c = (size_t)cap;
         CUDA_TRY(h->w_q_o0.alloc(c)); CUDA_TRY(h->w_q_o1.alloc(c)); CUDA_TRY(h->w_q_d0.alloc(c)); CUDA_TRY(h->w_q_d1.alloc(c));
         CUDA_TRY(h->w_q_hit.alloc(c)); CUDA_TRY(h->w_slot_key.alloc(c));
-        CUDA_TRY(h->w_throughput.alloc(c)); CUDA_TRY(h->w_radiance.alloc(c)); CUDA_TRY(h->w_rng.alloc(c)); CUDA_TRY(h->w_pixel_flags.alloc(c));
+        CUDA_TRY(h->w_throughput.alloc(2 * c)); CUDA_TRY(h->w_rng.alloc(c)); CUDA_TRY(h->w_pixel_flags.alloc(c));
         CUDA_TRY(h->w_s_o.alloc(shadow)); CUDA_TRY(h->w_s_d.alloc(shadow)); CUDA_TRY(h->w_s_c.alloc(shadow));
         h->w_s2_o.release(); h->w_s2_d.release(); h->w_s2_c.release(); h->w_vis.release();
         h->wide_capacity = cap;
@@ -812,7 +812,7 @@ int wide_prepare(dfpt_handle* h) {
     B.n_pixels = h->wide_capacity;
     B.q_o[0] = h->w_q_o0.p; B.q_o[1] = h->w_q_o1.p; B.q_d[0] = h->w_q_d0.p; B.q_d[1] = h->w_q_d1.p;
     B.q_hit = h->w_q_hit.p; B.s_o = h->w_s_o.p; B.s_d = h->w_s_d.p; B.s_c = h->w_s_c.p;
-    B.throughput = h->w_throughput.p; B.radiance = h->w_radiance.p; B.rng = h->w_rng.p; B.pixel_flags = h->w_pixel_flags.p;
+    B.throughput = h->w_throughput.p; B.radiance = h->w_throughput.p + 1; B.rng = h->w_rng.p; B.pixel_flags = h->w_pixel_flags.p;
     B.counts = h->w_counts.p; B.stats = h->stats.p; B.pass_index = h->pass_index.p;
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
     B.sorted_queues = (h->ray_sort && h->wide.b_sort) ? 1 : 0;
@@ -1294,7 +1294,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     const size_t n = (size_t)h->n_pixels;
     TRY_R(h->q_o0.alloc(n)); TRY_R(h->q_o1.alloc(n)); TRY_R(h->q_d0.alloc(n)); TRY_R(h->q_d1.alloc(n));
     TRY_R(h->q_hit.alloc(n));
-    TRY_R(h->throughput.alloc(n)); TRY_R(h->radiance.alloc(n)); TRY_R(h->rng.alloc(n)); TRY_R(h->pixel_flags.alloc(n));
+    TRY_R(h->throughput.alloc(2 * n)); TRY_R(h->rng.alloc(n)); TRY_R(h->pixel_flags.alloc(n));
     TRY_R(h->primary_o.alloc(n)); TRY_R(h->primary_d.alloc(n));
     TRY_R(h->counts.alloc(DFPT_COUNTS_SIZE)); TRY_R(h->stats.alloc(6)); TRY_R(h->pass_index.alloc(1)); TRY_R(h->mean.alloc(3));
     TRY_R(h->film_sum.alloc(n)); TRY_R(h->film_comp.alloc(n)); TRY_R(h->film_n.alloc(n)); TRY_R(h->bgra.alloc(n * 4));
@@ -1314,7 +1314,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     B.n_pixels = h->n_pixels;
     B.q_o[0] = h->q_o0.p; B.q_o[1] = h->q_o1.p; B.q_d[0] = h->q_d0.p; B.q_d[1] = h->q_d1.p;
     B.q_hit = h->q_hit.p; B.s_o = h->s_o.p; B.s_d = h->s_d.p; B.s_c = h->s_c.p;
-    B.throughput = h->throughput.p; B.radiance = h->radiance.p; B.rng = h->rng.p; B.pixel_flags = h->pixel_flags.p;
+    B.throughput = h->throughput.p; B.radiance = h->throughput.p + 1; B.rng = h->rng.p; B.pixel_flags = h->pixel_flags.p;
     B.primary_o = h->primary_o.p; B.primary_d = h->primary_d.p; B.counts = h->counts.p; B.stats = h->stats.p;
     B.pass_index = h->pass_index.p; B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p;
     B.bgra = h->bgra.p; B.primitive_offsets = h->primitive_offsets.p;

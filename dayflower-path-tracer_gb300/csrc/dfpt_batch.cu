@@ -46,7 +46,7 @@ struct dfpt_batch {
     long long capacity_request = 1ll << 23;
     int capacity = 0;         // slots allocated
     size_t shadow_slots = 0;  // deferred shadow queue entries allocated
-    DevBuf<float4> q_o0, q_o1, q_d0, q_d1, s_o, s_d, s_c, throughput, radiance, film_sum, film_comp;
+    DevBuf<float4> q_o0, q_o1, q_d0, q_d1, s_o, s_d, s_c, throughput, film_sum, film_comp;  // throughput: throughput + radiance records (PSI)
     DevBuf<int4> q_hit, slot_key;
     DevBuf<uint64_t> rng;
     DevBuf<int> pixel_flags, counts, pass_index, film_n;
@@ -73,7 +73,7 @@ struct dfpt_batch {
 namespace {
 
 void batch_release_buffers(dfpt_batch* b) {
-    DevBuf<float4>* f4[] = {&b->q_o0, &b->q_o1, &b->q_d0, &b->q_d1, &b->s_o, &b->s_d, &b->s_c, &b->throughput, &b->radiance};
+    DevBuf<float4>* f4[] = {&b->q_o0, &b->q_o1, &b->q_d0, &b->q_d1, &b->s_o, &b->s_d, &b->s_c, &b->throughput};
     for (auto* x : f4) x->release();
     b->q_hit.release();
     b->slot_key.release();
@@ -147,7 +147,7 @@ int batch_prepare(dfpt_batch* b) {
         const size_t c = (size_t)cap;
         CUDA_TRY(b->q_o0.alloc(c)); CUDA_TRY(b->q_o1.alloc(c)); CUDA_TRY(b->q_d0.alloc(c)); CUDA_TRY(b->q_d1.alloc(c));
         CUDA_TRY(b->q_hit.alloc(c)); CUDA_TRY(b->slot_key.alloc(c));
-        CUDA_TRY(b->throughput.alloc(c)); CUDA_TRY(b->radiance.alloc(c)); CUDA_TRY(b->rng.alloc(c)); CUDA_TRY(b->pixel_flags.alloc(c));
+        CUDA_TRY(b->throughput.alloc(2 * c)); CUDA_TRY(b->rng.alloc(c)); CUDA_TRY(b->pixel_flags.alloc(c));
         // Each path leaves at most one sun shadow ray per bounce; a bounce's are traced at once.
         CUDA_TRY(b->s_o.alloc(shadow)); CUDA_TRY(b->s_d.alloc(shadow)); CUDA_TRY(b->s_c.alloc(shadow));
         b->capacity = cap;
@@ -159,7 +159,7 @@ int batch_prepare(dfpt_batch* b) {
     B.n_pixels = b->capacity;
     B.q_o[0] = b->q_o0.p; B.q_o[1] = b->q_o1.p; B.q_d[0] = b->q_d0.p; B.q_d[1] = b->q_d1.p;
     B.q_hit = b->q_hit.p; B.s_o = b->s_o.p; B.s_d = b->s_d.p; B.s_c = b->s_c.p;
-    B.throughput = b->throughput.p; B.radiance = b->radiance.p; B.rng = b->rng.p; B.pixel_flags = b->pixel_flags.p;
+    B.throughput = b->throughput.p; B.radiance = b->throughput.p + 1; B.rng = b->rng.p; B.pixel_flags = b->pixel_flags.p;
     B.counts = b->counts.p; B.stats = b->stats.p; B.pass_index = b->pass_index.p;
     B.film_sum = b->film_sum.p; B.film_comp = b->film_comp.p; B.film_n = b->film_n.p; B.bgra = b->bgra.p;
     B.sorted_queues = (b->ray_sort && b->ks.b_sort) ? 1 : 0;

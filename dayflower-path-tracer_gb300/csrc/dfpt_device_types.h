@@ -113,6 +113,9 @@ enum {
 #define DFPT_DIFF_GLOBAL 4    // turbidity, sun direction x, y, z
 
 // Wavefront buffers of one handle. Queue entries are SoA float4 records.
+// Index of a path's record in DevPass::throughput / DevPass::radiance (2 float4 per path).
+#define PSI(i) (2 * (size_t)(i))
+
 struct DevPass {
     int n_pixels;
     float4* q_o[2];       // {origin.xyz, path id}
@@ -121,8 +124,8 @@ struct DevPass {
     float4* s_o;          // shadow rays {origin.xyz, path id}
     float4* s_d;          // {direction.xyz, 0}
     float4* s_c;          // pending sun contribution {rgb, 0}
-    float4* throughput;   // per path
-    float4* radiance;     // per path
+    float4* throughput;   // per path, index PSI(path): one 32-byte record holds a path's throughput
+    float4* radiance;     // and radiance (radiance = throughput + 1), read and written together
     uint64_t* rng;        // per pixel: LCG state or draw counter
     int* pixel_flags;     // bit 0: film set to black this pass
     float4* primary_o;    // primary rays (wireframe overlay)

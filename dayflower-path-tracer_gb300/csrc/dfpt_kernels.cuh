@@ -615,8 +615,8 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
             B.pixel_flags[i] = live ? 0 : 1;
             if (!lean_start<BATCH>(P)) {
                 B.rng[i] = rng.state;
-                B.throughput[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-                B.radiance[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                B.throughput[PSI(i)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+                B.radiance[PSI(i)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             }
             if (P.diff) B.vis[i] = 0;
             if (!BATCH && P.wireframes == 1) {
@@ -872,9 +872,25 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
             const DevParams& P = params_of<BATCH>(Pp, Q, sid);
             uint32_t rng_pixel = (uint32_t)path, rng_pass = pass;
             if constexpr (BATCH) {
+#ifdef DFPT_ONE_SCENE
+                // One scene: the slot's pixel and pass follow from its index as k_camera derived
+                // them (slot i of the wave is sample base + i), without the random slot-key load.
+                const long long local = Q.wave_base[0] + path - Q.sample_begin[0];
+                const long long np = (long long)P.width * P.height;
+                if (local < 0x7FFFFFFFll) {
+                    const unsigned q = (unsigned)local / (unsigned)np;
+                    rng_pixel = (unsigned)local - q * (unsigned)np;
+                    rng_pass = (uint32_t)(q + Q.wave_base[2]);
+                } else {
+                    const long long j = local / np;
+                    rng_pixel = (uint32_t)(local - j * np);
+                    rng_pass = (uint32_t)(j + Q.wave_base[2]);
+                }
+#else
                 const int4 key = Q.slot_key[path];
                 rng_pixel = (uint32_t)key.y;
                 rng_pass = (uint32_t)key.z;
+#endif
             }
             const int4 hr = B.q_hit[i];
             Hit h;
@@ -883,8 +899,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
             h.shape_type = hr.z;
             h.shape_offset = hr.w;
             const bool fresh = bounce == 0 && lean_start<BATCH>(P);
-            float4 T = fresh ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : B.throughput[path];
-            float4 L = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : B.radiance[path];
+            float4 T = fresh ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : B.throughput[PSI(path)];
+            float4 L = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : B.radiance[PSI(path)];
             if (!BATCH && bounce == 0) B.primitive_offsets[path] = h.prim >= 0 ? h.prim * 3 : -1;
             // A handle's waves of passes: the selection buffer holds the first hits of the call's
             // last pass (wave record entry 4; batches of scenes have no selection buffer).
@@ -895,7 +911,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
                 L.x += T.x * sky.x * INV_PI;
                 L.y += T.y * sky.y * INV_PI;
                 L.z += T.z * sky.z * INV_PI;
-                B.radiance[path] = L;
+                B.radiance[PSI(path)] = L;
                 if (!BATCH && bounce == 0 && P.record_hits) {
                     B.hit_prim_offset[path] = -1; B.hit_shape_type[path] = -1; B.hit_shape_offset[path] = -1;
                     B.hit_distance[path] = INF;
@@ -954,8 +970,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
                     no = make_float4(sct.o.x, sct.o.y, sct.o.z, __int_as_float(path));
                     nd = make_float4(sct.d.x, sct.d.y, sct.d.z, sid_bits);
                 }
-                B.throughput[path] = T;
-                B.radiance[path] = L;
+                B.throughput[PSI(path)] = T;
+                B.radiance[PSI(path)] = L;
                 B.rng[path] = rng.state;
             }
         }
@@ -994,7 +1010,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevPa
     // sum's order, and so its last bit, may vary).
     auto unoccluded = [&](int i, const float4& o, const float4& c) {
         const int path = __float_as_int(o.w);
-        float* L = reinterpret_cast<float*>(B.radiance + path);
+        float* L = reinterpret_cast<float*>(B.radiance + PSI(path));
         atomicAdd(L, c.x);
         atomicAdd(L + 1, c.y);
         atomicAdd(L + 2, c.z);
@@ -1041,13 +1057,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S0, const DevPar
         const int sid = BATCH ? __float_as_int(d.w) : 0;
         const DevParams& P = params_of<BATCH>(Pp, Q, sid);
         const int path = __float_as_int(o.w);
-        const float4 T = B.throughput[path];
+        const float4 T = B.throughput[PSI(path)];
         const float3 sky = sky_color(P, d.x, d.y, d.z);
-        float4 L = B.radiance[path];
+        float4 L = B.radiance[PSI(path)];
         L.x += T.x * sky.x * INV_PI;
         L.y += T.y * sky.y * INV_PI;
         L.z += T.z * sky.z * INV_PI;
-        B.radiance[path] = L;
+        B.radiance[PSI(path)] = L;
     };
     if constexpr (V == 3) {
         TraceStats st{0, 0};
@@ -1241,7 +1257,7 @@ __global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __r
                     }
                 }
             }
-            B.radiance[i] = make_float4(cr_, cg_, cb_, 0.0f);
+            B.radiance[PSI(i)] = make_float4(cr_, cg_, cb_, 0.0f);
             B.rng[i] = rng.state;
         }
         warp_add_stats(P, B.stats, 0, segs, st.nodes, st.tris);
@@ -1368,11 +1384,11 @@ __global__ void __launch_bounds__(256) k_film(const DevParams* __restrict__ Pp, 
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 sum = B.film_sum[i], comp = B.film_comp[i];
         int cnt = B.film_n[i];
-        film_add(B.radiance[i], B.pixel_flags[i], clear, sum, comp, cnt);
+        film_add(B.radiance[PSI(i)], B.pixel_flags[i], clear, sum, comp, cnt);
         if (P.diff) {
             const int k = pass - P.diff_pass0;
             if (k >= 0 && k < P.diff_spp) {
-                B.diff_L[(size_t)k * n + i] = B.radiance[i];
+                B.diff_L[(size_t)k * n + i] = B.radiance[PSI(i)];
                 B.diff_vis[(size_t)k * n + i] = (B.pixel_flags[i] & 1) ? 0 : B.vis[i];
             }
         }
@@ -1438,12 +1454,12 @@ __global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
         const long long pass0 = Q.wave_base[2];
         for (long long loc = first; loc < b; loc += np) {
             const int slot = (int)(slot0 + loc);
-            film_add(B.radiance[slot], B.pixel_flags[slot], loc / np == clear_sample, sum, comp, cnt);
+            film_add(B.radiance[PSI(slot)], B.pixel_flags[slot], loc / np == clear_sample, sum, comp, cnt);
             if (P.diff) {
                 // The differentiable forward's per-sample records (as k_film keeps them per pass).
                 const long long k = pass0 + loc / np - P.diff_pass0;
                 if (k >= 0 && k < P.diff_spp) {
-                    B.diff_L[k * np + pixel] = B.radiance[slot];
+                    B.diff_L[k * np + pixel] = B.radiance[PSI(slot)];
                     B.diff_vis[k * np + pixel] = (B.pixel_flags[slot] & 1) ? 0 : B.vis[slot];
                 }
             }
