@@ -51,6 +51,18 @@ __device__ __forceinline__ float jmax(float a, float b) {
     asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
     return r;
 }
+// Three-operand forms (sm_100 and later): the minimum / maximum of a set, NaN when any operand is
+// NaN, -0 below +0, so jmin3(a, b, c) == jmin(a, jmin(b, c)) for every input, in one instruction.
+__device__ __forceinline__ float jmin3(float a, float b, float c) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float jmax3(float a, float b, float c) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 // Aparapi's rsqrt is 1 / sqrt: both correctly rounded here (no fast-math).
 __device__ __forceinline__ float rsqrt_j(float x) { return 1.0f / sqrtf(x); }
 __device__ __forceinline__ float saturate_j(float v, float a, float b) {
@@ -382,8 +394,8 @@ __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim,
         }
         const float t0x = slab(n0.x, sr.ix, sr.px), t0y = slab(n0.y, sr.iy, sr.py), t0z = slab(n0.z, sr.iz, sr.pz);
         const float t1x = slab(n1.x, sr.ix, sr.px), t1y = slab(n1.y, sr.iy, sr.py), t1z = slab(n1.z, sr.iz, sr.pz);
-        const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
-        const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+        const float tmax = jmin3(jmax(t0x, t1x), jmax(t0y, t1y), jmax(t0z, t1z));
+        const float tmin = jmax3(jmin(t0x, t1x), jmin(t0y, t1y), jmin(t0z, t1z));
         const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
         if (tb >= 0.0f && leaf != -1) {
             // Leaf: its triangles in order (-2 marks an empty leaf).
@@ -427,8 +439,8 @@ __device__ __forceinline__ void slab_interval(float ax, float ay, float az, floa
                                               float& tmin, float& tmax) {
     const float t0x = slab(ax, sr.ix, sr.px), t0y = slab(ay, sr.iy, sr.py), t0z = slab(az, sr.iz, sr.pz);
     const float t1x = slab(bx, sr.ix, sr.px), t1y = slab(by, sr.iy, sr.py), t1z = slab(bz, sr.iz, sr.pz);
-    tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
-    tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+    tmax = jmin3(jmax(t0x, t1x), jmax(t0y, t1y), jmax(t0z, t1z));
+    tmin = jmax3(jmin(t0x, t1x), jmin(t0y, t1y), jmin(t0z, t1z));
 }
 
 // The threaded walk over pair records (DevScene::pairs), with a short stack in shared memory. An
@@ -685,8 +697,8 @@ __device__ __forceinline__ bool mesh_walk_warp(const DevScene& S, int root, int 
             const int leaf = __float_as_int(n1.w);
             const float t0x = slab(n0.x, sr.ix, sr.px), t0y = slab(n0.y, sr.iy, sr.py), t0z = slab(n0.z, sr.iz, sr.pz);
             const float t1x = slab(n1.x, sr.ix, sr.px), t1y = slab(n1.y, sr.iy, sr.py), t1z = slab(n1.z, sr.iz, sr.pz);
-            const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
-            const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+            const float tmax = jmin3(jmax(t0x, t1x), jmax(t0y, t1y), jmax(t0z, t1z));
+            const float tmin = jmax3(jmin(t0x, t1x), jmin(t0y, t1y), jmin(t0z, t1z));
             const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
             bool stop = false;
             if (tb >= 0.0f && leaf != -1) {
@@ -1020,8 +1032,8 @@ __device__ __forceinline__ void trace_refill(int n, int* fetch, SceneOf scene, L
         const int leaf = __float_as_int(n1.w);
         const float t0x = slab(n0.x, sr.ix, sr.px), t0y = slab(n0.y, sr.iy, sr.py), t0z = slab(n0.z, sr.iz, sr.pz);
         const float t1x = slab(n1.x, sr.ix, sr.px), t1y = slab(n1.y, sr.iy, sr.py), t1z = slab(n1.z, sr.iz, sr.pz);
-        const float tmax = jmin(jmax(t0x, t1x), jmin(jmax(t0y, t1y), jmax(t0z, t1z)));
-        const float tmin = jmax(jmin(t0x, t1x), jmax(jmin(t0y, t1y), jmin(t0z, t1z)));
+        const float tmax = jmin3(jmax(t0x, t1x), jmax(t0y, t1y), jmax(t0z, t1z));
+        const float tmin = jmax3(jmin(t0x, t1x), jmin(t0y, t1y), jmin(t0z, t1z));
         const float tb = tmin > tmax ? -1.0f : tmin > 0.001f && tmin < h.t ? tmin : tmax > 0.001f && tmax < h.t ? tmax : -1.0f;
         bool stop = false;
         if (tb >= 0.0f && leaf != -1) {
