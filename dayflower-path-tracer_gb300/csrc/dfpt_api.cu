@@ -480,6 +480,7 @@ struct dfpt_handle {
     long long wide_range[5] = {0, 0, 0, -1, -1};  // wave base, range end, pass of sample 0, clear sample, selection pass
     int pass_index_host = 0;  // source of pass-index copies (pageable: consumed on return)
     bool ray_sort = true;     // bin rays between bounces in wide passes
+    bool shadow_sort = true;  // with ray_sort, also bin the sun shadow rays before their launch
     bool shadow_defer = false;  // wide passes: one shadow launch per wave (queue of slots x depth)
     DevBuf<int> w_sort_bins;
     DevBuf<float4> w_s2_o, w_s2_d, w_s2_c;  // the binned copy of the shadow queue
@@ -819,7 +820,7 @@ int wide_prepare(dfpt_handle* h) {
     B.sort_bins = h->w_sort_bins.p;
     B.primitive_offsets = h->primitive_offsets.p;  // selection buffer: first hits of the call's last pass
     B.sort_count = h->w_sort_bins.p + DFPT_SORT_BINS;
-    B.sort_count_shadow = h->w_sort_bins.p + 2 * DFPT_SORT_BINS;
+    B.sort_count_shadow = h->shadow_sort ? h->w_sort_bins.p + 2 * DFPT_SORT_BINS : nullptr;  // null: shadow rays unbinned
     if (h->diff_on) {
         // The differentiable forward / replay: visibility bits per slot, the per-sample records.
         if (!h->w_vis.p) CUDA_TRY(h->w_vis.alloc((size_t)h->wide_capacity));
@@ -875,7 +876,7 @@ int issue_wide_wave(dfpt_handle* h) {
     // with shadow_defer, all bounces' at once after the last bounce (queue of slots x depth).
     auto shadows = [&]() {
         if (h->sky.is_sun_active != 1) return;
-        if (h->wpass.sorted_queues) {
+        if (h->wpass.sorted_queues && h->wpass.sort_count_shadow) {
             mark(h, KIND_SORT); k += K.b_sort_shadow(c, h->wpass_shadow);
             mark(h, KIND_SHADOW); K.b_shadow(h->wctx_shadow, 0); ++k;
         } else {
@@ -1456,6 +1457,11 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->wide_graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "shadow_sort") == 0) {
+        h->shadow_sort = value != 0;
+        h->wide_graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "shadow_defer") == 0) {
         h->shadow_defer = value != 0;
         h->wide_graph_valid = false;
@@ -1514,6 +1520,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
+    if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 

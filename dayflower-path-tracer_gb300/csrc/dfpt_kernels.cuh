@@ -805,8 +805,14 @@ __device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx
 // changes: every ray keeps its path id and its own result.
 __device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d);
 __device__ __forceinline__ int wave_first_scene(const DevBatch& Q) { return (int)Q.wave_tab[0]; }
+__device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits);
 __device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
     const int sid = __float_as_int(d.w);
+    if (Q.n_scenes == 1) {
+        // One scene in the wave: the scene bits go to the grid (11 bits: 16 x 16 x 8 cells).
+        const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
+        return (oct << 11) | cell_bits(Q.scenes[sid], o, 11);
+    }
     return (((sid - first) & 3) << 12) | ray_bin(Q.scenes[sid], o, d);
 }
 __device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d) {
@@ -846,8 +852,36 @@ __device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
     return cell;
 }
 
+// Origin cell over the scene bounds with `bits` bits in all (bits / 3 per axis, the remainder to
+// the axes of largest extent), axis bits interleaved from the least significant up.
+__device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits) {
+    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
+    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
+    const float p[3] = {o.x, o.y, o.z};
+    const float ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    int nb[3] = {bits / 3, bits / 3, bits / 3};
+    int extra = bits - 3 * (bits / 3);
+    // The smallest axis gets no extra bit; with 2 extra, the other two get one each.
+    const int small = ext[0] <= ext[1] && ext[0] <= ext[2] ? 0 : ext[1] <= ext[2] ? 1 : 2;
+    for (int a = 0; a < 3 && extra > 0; ++a)
+        if (a != small || extra == 3) { ++nb[a]; --extra; }
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        const float n = (float)(1 << nb[a]);
+        const float u = (p[a] - lo[a]) * (n * __frcp_rn(ext[a]));  // any monotone mapping bins alike
+        c[a] = u >= 0.0f ? (u < n - 1.0f ? (int)u : (1 << nb[a]) - 1) : 0;
+    }
+    int cell = 0, k = 0;
+    for (int b = 0; b < 5; ++b)
+        for (int a = 0; a < 3; ++a)
+            if (b < nb[a]) cell |= ((c[a] >> b) & 1) << k++;
+    return cell;
+}
+
 __device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
     const int sid = __float_as_int(d.w);
+    // One scene in the wave: the scene bits go to the grid (14 bits: 32 x 32 x 16 cells).
+    if (Q.n_scenes == 1) return cell_bits(Q.scenes[sid], o, 14);
     return (((sid - first) & 3) << 12) | shadow_bin(Q.scenes[sid], o);
 }
 
@@ -985,7 +1019,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* 
             if (B.sorted_queues) {
                 const int first = wave_first_scene(Q);
                 bin_count(B.sort_count, emit_next ? ray_bin_in_wave(Q, first, no, nd) : -1);
-                bin_count(B.sort_count_shadow, emit_shadow ? shadow_bin_in_wave(Q, first, so, sd) : -1);
+                if (B.sort_count_shadow) bin_count(B.sort_count_shadow, emit_shadow ? shadow_bin_in_wave(Q, first, so, sd) : -1);
             }
         }
         const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
