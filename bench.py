@@ -1,10 +1,11 @@
 """Benchmark: M path samples/s of the GB300 renderer core on the 1080p triangle-mesh workload.
 
-One step = one dfpt_render call of --spp-per-step passes (default 16) over the whole 1920x1080
+One step = one dfpt_render call of --spp-per-step passes (default 64) over the whole 1920x1080
 image; a pass is one sample per pixel, the unit of the reference's Kernel.execute
-(DayflowerApplication.java:853), so the default 16 timed steps render the 256 spp of the
+(DayflowerApplication.java:853), so the default 4 timed steps render the 256 spp of the
 triangle-mesh configuration. Inside a call, the passes run `wide_samples` at a time through the
-wave kernels (same samples, same film and image as pass-by-pass rendering, tested). The workload
+wave kernels (same samples, same film and image as pass-by-pass rendering, tested); the autotuner
+picks up to 64 passes per wave (133 M path slots). The workload
 is mesh_scene: an fBm-displaced geodesic icosphere (200,000 triangles, 4 Lambertian/Phong regions)
 over a 512x512 fBm heightfield (522,242 triangles), BVHs built by the restated reference builder,
 depth 8, ACES; seeded synthetic data (the reference publishes no scenes).
@@ -15,8 +16,8 @@ depth 8, ACES; seeded synthetic data (the reference publishes no scenes).
           (dfpt_set_camera from host memory, dfpt_render, dfpt_read_bgra8 into host memory);
   roofline : the dominant kernel (closest-hit traversal), algorithmic bytes per closest-hit
           segment = nodes*32 + triangles*48 + 64 with the mean visit counts of closest-hit
-          segments measured by the CPU restatement on the cpu_baseline sample, against
-          MEASURED_PEAKS.json's HBM copy rate;
+          segments from the GPU's own counters over a step (the CPU restatement's counts on its
+          sample reported beside them), against MEASURED_PEAKS.json's HBM copy rate;
   cpu_baseline : the oracle's strict-FP32 restatement of the reference kernel on all host cores,
           over a bounded band of rows (the reference's Java thread-pool path needs a JVM).
 --impl reference times that CPU restatement alone on the same workload and metric.
@@ -49,8 +50,8 @@ TRACE_DRAM_BYTES_PER_SEGMENT = 65.5
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=16)
-    ap.add_argument("--spp-per-step", type=int, default=16, help="passes (1 spp each) per step: one dfpt_render call")
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--spp-per-step", type=int, default=64, help="passes (1 spp each) per step: one dfpt_render call")
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="dfpt", choices=["dfpt", "reference"])
     ap.add_argument("--workload", default="mesh_scene", choices=["mesh_scene", "sphere_scene", "instances_scene"])
@@ -577,6 +578,9 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = world * n_pix * S * args.steps / e2e_s / 1e6
+    # The main handle's waves (up to 64 passes of 1080p with every bounce's shadow rays queued)
+    # hold most of the device memory: release it before the other legs create their handles.
+    k.dispose()
 
     batched = None
     if not args.no_batch:
@@ -663,7 +667,6 @@ def main():
         line["adjoint"] = adjoint
     line["rays_per_s"] = (cnt[0] + cnt[1]) * world / (total_s / args.steps)  # segments of one step / step time
     print(json.dumps(line), flush=True)
-    k.dispose()
     if dist is not None:
         dist.destroy_process_group()
 

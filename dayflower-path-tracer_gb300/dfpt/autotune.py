@@ -115,11 +115,12 @@ def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=N
             "ray_sort_m_samples_per_s": {str(k): round(v, 2) for k, v in sort.items()}}
 
 
-def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16), verbose: bool = False) -> dict:
+def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbose: bool = False) -> dict:
     """Picks how many passes run per wave in dfpt_render (1 = one pass at a time) by timing
-    `passes` passes per candidate on the handle's own scene; every choice gives the same film."""
+    `passes` passes per candidate (those up to `passes`) on the handle's own scene; every choice
+    gives the same film."""
     results = {}
-    for k in candidates:
+    for k in [c for c in candidates if c <= max(1, passes)]:
         kernel.set_tuning("wide_samples", k)
         kernel.execute(passes)
         kernel.synchronize()
