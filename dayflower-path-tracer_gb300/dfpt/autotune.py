@@ -63,7 +63,7 @@ def tune_trace(kernel, passes: int = 4, warmup: int = 1, verbose: bool = False) 
     return out
 
 
-def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=None, window: int | None = None,
+def tune_batch(batch, capacities=(1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26), configs=None, window: int | None = None,
                verbose: bool = False) -> dict:
     """Picks the batch's wave capacity (queue depth) and traversal configuration (block size x
     resident blocks x walk variant) by timing the same window of the batch's own samples with
@@ -72,8 +72,10 @@ def tune_batch(batch, capacities=(1 << 21, 1 << 22, 1 << 23, 1 << 24), configs=N
     candidate. Leaves the films cleared and the best candidate set."""
     total = batch.total_samples
     if configs is None:
-        # Walk variant 2 (warp-synchronous) maps to the per-lane walk in a batch; skip duplicates.
-        configs = [c for c in range(batch.get_tuning("trace_configs")) if c not in (4, 5, 6)]
+        # The per-lane walks at 4 and 3 blocks per SM, the lane-refill walk and the pair walks: the
+        # warp-synchronous walk (4-6) maps to the per-lane walk in a batch, and the 6-8 block
+        # configurations (11-14) spill and lose on every workload measured.
+        configs = [c for c in (0, 1, 2, 3, 9, 15, 16) if c < batch.get_tuning("trace_configs")]
     results = {}
     # One window of the batch's sample sequence for every candidate, so the rates compare.
     span = int(min(total, window if window is not None else 2 * max(capacities)))
