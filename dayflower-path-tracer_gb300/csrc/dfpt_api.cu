@@ -799,8 +799,8 @@ int wide_prepare(dfpt_handle* h) {
         CUDA_TRY(h->w_wave_base.alloc(5));
         CUDA_TRY(h->w_wave_tab.alloc(8));
         // Offsets, then the ray and the shadow-ray counts (zero at rest).
-        CUDA_TRY(h->w_sort_bins.alloc(3 * DFPT_SORT_BINS));
-        CUDA_TRY(cudaMemsetAsync(h->w_sort_bins.p, 0, 3 * DFPT_SORT_BINS * sizeof(int), h->stream));
+        CUDA_TRY(h->w_sort_bins.alloc(3 * DFPT_SORT_BINS + DFPT_SORT_CHUNKS));
+        CUDA_TRY(cudaMemsetAsync(h->w_sort_bins.p, 0, (3 * DFPT_SORT_BINS + DFPT_SORT_CHUNKS) * sizeof(int), h->stream));
         const std::vector<long long> sb = {0, 1ll << 62}, fb = {0, (long long)n};
         CUDA_TRY(upload(h->w_sample_begin, sb, h->stream));
         CUDA_TRY(upload(h->w_film_begin, fb, h->stream));
@@ -821,6 +821,7 @@ int wide_prepare(dfpt_handle* h) {
     B.primitive_offsets = h->primitive_offsets.p;  // selection buffer: first hits of the call's last pass
     B.sort_count = h->w_sort_bins.p + DFPT_SORT_BINS;
     B.sort_count_shadow = h->shadow_sort ? h->w_sort_bins.p + 2 * DFPT_SORT_BINS : nullptr;  // null: shadow rays unbinned
+    B.sort_partials = h->w_sort_bins.p + 3 * DFPT_SORT_BINS;
     if (h->diff_on) {
         // The differentiable forward / replay: visibility bits per slot, the per-sample records.
         if (!h->w_vis.p) CUDA_TRY(h->w_vis.alloc((size_t)h->wide_capacity));

@@ -166,8 +166,8 @@ int batch_prepare(dfpt_batch* b) {
     if (B.sorted_queues) {
         if (!b->sort_bins.p) {
             // Offsets, then the ray and the shadow-ray counts (zero at rest).
-            CUDA_TRY(b->sort_bins.alloc(3 * DFPT_SORT_BINS));
-            CUDA_TRY(cudaMemsetAsync(b->sort_bins.p, 0, 3 * DFPT_SORT_BINS * sizeof(int), b->stream));
+            CUDA_TRY(b->sort_bins.alloc(3 * DFPT_SORT_BINS + DFPT_SORT_CHUNKS));
+            CUDA_TRY(cudaMemsetAsync(b->sort_bins.p, 0, (3 * DFPT_SORT_BINS + DFPT_SORT_CHUNKS) * sizeof(int), b->stream));
         }
         if (!b->s2_o.p) {
             CUDA_TRY(b->s2_o.alloc(b->shadow_slots));
@@ -178,6 +178,7 @@ int batch_prepare(dfpt_batch* b) {
     B.sort_bins = b->sort_bins.p;
     B.sort_count = b->sort_bins.p ? b->sort_bins.p + DFPT_SORT_BINS : nullptr;
     B.sort_count_shadow = b->sort_bins.p ? b->sort_bins.p + 2 * DFPT_SORT_BINS : nullptr;
+    B.sort_partials = b->sort_bins.p ? b->sort_bins.p + 3 * DFPT_SORT_BINS : nullptr;
     b->pass_shadow = B;
     if (B.sorted_queues) {
         b->pass_shadow.s_o = b->s2_o.p;

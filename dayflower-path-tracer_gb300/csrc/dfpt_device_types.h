@@ -158,8 +158,14 @@ struct DevPass {
     int* sort_bins;            // DFPT_SORT_BINS exclusive offsets (scan output, scatter cursors)
     int* sort_count;           // DFPT_SORT_BINS ray counts of the next bounce; zero at rest (the scan clears them)
     int* sort_count_shadow;    // the same for the sun shadow rays
+    int* sort_partials;        // DFPT_SORT_CHUNKS chunk sums of the scan
 };
-#define DFPT_SORT_BINS 16384  // 2 bits of scene (within a wave) x 3 bits of octant x 9 bits of cell
+// Bins: waves of several scenes use 2 bits of scene (within a wave) x 3 bits of octant x 9 bits of
+// cell (bounce rays) or 12 bits of cell (shadow rays); waves of one scene spend 18 bits on the
+// octant and a 32^3 origin grid (bounce rays) or a 64^3 grid (shadow rays). The scan runs over
+// DFPT_SORT_CHUNKS chunks of 1024 bins.
+#define DFPT_SORT_BINS 262144
+#define DFPT_SORT_CHUNKS (DFPT_SORT_BINS / 1024)
 
 // Many scenes rendered by one set of launches. Every scene's samples form one global sequence
 // (scene-major, then sample, then pixel); a wave takes `capacity` consecutive samples of it, one

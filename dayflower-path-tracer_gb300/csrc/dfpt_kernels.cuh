@@ -809,9 +809,9 @@ __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits);
 __device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
     const int sid = __float_as_int(d.w);
     if (Q.n_scenes == 1) {
-        // One scene in the wave: the scene bits go to the grid (11 bits: 16 x 16 x 8 cells).
+        // One scene in the wave: no scene bits; the octant over a 32 x 32 x 32 origin grid (18 bits).
         const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
-        return (oct << 11) | cell_bits(Q.scenes[sid], o, 11);
+        return (oct << 15) | cell_bits(Q.scenes[sid], o, 15);
     }
     return (((sid - first) & 3) << 12) | ray_bin(Q.scenes[sid], o, d);
 }
@@ -852,8 +852,8 @@ __device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
     return cell;
 }
 
-// Origin cell over the scene bounds with `bits` bits in all (bits / 3 per axis, the remainder to
-// the axes of largest extent), axis bits interleaved from the least significant up.
+// Origin cell over the scene bounds with `bits` bits in all (at most 18: bits / 3 per axis, the
+// remainder to the axes of largest extent), axis bits interleaved from the least significant up.
 __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits) {
     const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
     const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
@@ -872,7 +872,7 @@ __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits) 
         c[a] = u >= 0.0f ? (u < n - 1.0f ? (int)u : (1 << nb[a]) - 1) : 0;
     }
     int cell = 0, k = 0;
-    for (int b = 0; b < 5; ++b)
+    for (int b = 0; b < 6; ++b)
         for (int a = 0; a < 3; ++a)
             if (b < nb[a]) cell |= ((c[a] >> b) & 1) << k++;
     return cell;
@@ -880,8 +880,8 @@ __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits) 
 
 __device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
     const int sid = __float_as_int(d.w);
-    // One scene in the wave: the scene bits go to the grid (14 bits: 32 x 32 x 16 cells).
-    if (Q.n_scenes == 1) return cell_bits(Q.scenes[sid], o, 14);
+    // One scene in the wave: a 64 x 64 x 64 origin grid (18 bits).
+    if (Q.n_scenes == 1) return cell_bits(Q.scenes[sid], o, 18);
     return (((sid - first) & 3) << 12) | shadow_bin(Q.scenes[sid], o);
 }
 
@@ -1563,24 +1563,56 @@ __global__ void __launch_bounds__(256) k_sort_shadow_scatter(DevBatch Q, DevPass
     }
 }
 
-// Exclusive scan of the bin counts into B.sort_bins (one block of 1024 threads, DFPT_SORT_BINS /
-// 1024 bins each); the counts are cleared for the next count.
-__global__ void __launch_bounds__(1024) k_sort_scan(DevPass B, int* counts) {
-    constexpr int PER = DFPT_SORT_BINS / 1024;
-    __shared__ int part[1024];
-    const int t = threadIdx.x;
-    int v[PER], sum = 0;
-    for (int j = 0; j < PER; ++j) { v[j] = counts[PER * t + j]; sum += v[j]; counts[PER * t + j] = 0; }
-    part[t] = sum;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int x = t >= off ? part[t - off] : 0;
-        __syncthreads();
-        part[t] += x;
-        __syncthreads();
+// Exclusive scan of the bin counts into B.sort_bins, clearing the counts for the next count, in
+// three launches over DFPT_SORT_CHUNKS chunks of 1024 bins: the chunk sums, their scan (one block),
+// then each chunk's scan from its offset. Every access is coalesced (4 bins per thread).
+__device__ __forceinline__ int block_exclusive_scan_256(int v, int& total) {
+    __shared__ int warp_sum[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
     }
-    int run = part[t] - sum;
-    for (int j = 0; j < PER; ++j) { B.sort_bins[PER * t + j] = run; run += v[j]; }
+    if (lane == 31) warp_sum[w] = x;
+    __syncthreads();
+    int before = 0;
+    total = 0;
+    for (int k = 0; k < 8; ++k) {
+        const int s = warp_sum[k];
+        if (k < w) before += s;
+        total += s;
+    }
+    __syncthreads();  // warp_sum is reused by the next call
+    return before + x - v;
+}
+__global__ void __launch_bounds__(256) k_sort_chunk_sums(DevPass B, const int* __restrict__ counts) {
+    const int4 c = reinterpret_cast<const int4*>(counts + (size_t)blockIdx.x * 1024)[threadIdx.x];
+    int total;
+    block_exclusive_scan_256(c.x + c.y + c.z + c.w, total);
+    if (threadIdx.x == 0) B.sort_partials[blockIdx.x] = total;
+}
+__global__ void __launch_bounds__(256) k_sort_chunk_offsets(DevPass B) {
+    constexpr int PER = DFPT_SORT_CHUNKS / 256;
+    int v[PER], sum = 0;
+    for (int j = 0; j < PER; ++j) { v[j] = B.sort_partials[PER * threadIdx.x + j]; sum += v[j]; }
+    int total;
+    int run = block_exclusive_scan_256(sum, total);
+    for (int j = 0; j < PER; ++j) { B.sort_partials[PER * threadIdx.x + j] = run; run += v[j]; }
+}
+__global__ void __launch_bounds__(256) k_sort_chunk_scan(DevPass B, int* counts) {
+    int4* cp = reinterpret_cast<int4*>(counts + (size_t)blockIdx.x * 1024) + threadIdx.x;
+    const int4 c = *cp;
+    *cp = make_int4(0, 0, 0, 0);
+    int total;
+    const int before = block_exclusive_scan_256(c.x + c.y + c.z + c.w, total) + B.sort_partials[blockIdx.x];
+    reinterpret_cast<int4*>(B.sort_bins + (size_t)blockIdx.x * 1024)[threadIdx.x] =
+        make_int4(before, before + c.x, before + c.x + c.y, before + c.x + c.y + c.z);
+}
+static void launch_sort_scan(const LaunchCtx& c, int* counts) {
+    k_sort_chunk_sums<<<DFPT_SORT_CHUNKS, 256, 0, c.stream>>>(*c.pass, counts);
+    k_sort_chunk_offsets<<<1, 256, 0, c.stream>>>(*c.pass);
+    k_sort_chunk_scan<<<DFPT_SORT_CHUNKS, 256, 0, c.stream>>>(*c.pass, counts);
 }
 
 __global__ void __launch_bounds__(256) k_sort_scatter(DevBatch Q, DevPass B, int bounce) {
@@ -1795,16 +1827,16 @@ static void launch_b_shadow_reset(const LaunchCtx& c, int) { k_shadow_reset<<<1,
 // Returns the kernels launched.
 static int launch_b_sort(const LaunchCtx& c, int bounce, bool counted) {
     if (!counted) k_sort_hist<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
-    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass, c.pass->sort_count);
+    launch_sort_scan(c, c.pass->sort_count);
     k_sort_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, bounce);
-    return counted ? 2 : 3;
+    return counted ? 4 : 5;
 }
 // Bins the shadow queue into `to` (a pass record whose s_* point at the second set); k_shade
 // counted the bins.
 static int launch_b_sort_shadow(const LaunchCtx& c, const DevPass& to) {
-    k_sort_scan<<<1, 1024, 0, c.stream>>>(*c.pass, c.pass->sort_count_shadow);
+    launch_sort_scan(c, c.pass->sort_count_shadow);
     k_sort_shadow_scatter<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass, to.s_o, to.s_d, to.s_c);
-    return 2;
+    return 4;
 }
 
 // Path-replay adjoint. Per-primitive partials live in shared memory when they fit in 44 KB.
