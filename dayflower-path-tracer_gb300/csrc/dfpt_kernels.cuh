@@ -809,9 +809,9 @@ __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits);
 __device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
     const int sid = __float_as_int(d.w);
     if (Q.n_scenes == 1) {
-        // One scene in the wave: no scene bits; the octant over a 32 x 32 x 32 origin grid (18 bits).
+        // One scene in the wave: no scene bits; the octant over the origin grid.
         const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
-        return (oct << 15) | cell_bits(Q.scenes[sid], o, 15);
+        return (oct << DFPT_RAY_CELL_BITS) | cell_bits(Q.scenes[sid], o, DFPT_RAY_CELL_BITS);
     }
     return (((sid - first) & 3) << 12) | ray_bin(Q.scenes[sid], o, d);
 }
@@ -852,7 +852,7 @@ __device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
     return cell;
 }
 
-// Origin cell over the scene bounds with `bits` bits in all (at most 18: bits / 3 per axis, the
+// Origin cell over the scene bounds with `bits` bits in all (at most 24: bits / 3 per axis, the
 // remainder to the axes of largest extent), axis bits interleaved from the least significant up.
 __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits) {
     const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
@@ -872,7 +872,7 @@ __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits) 
         c[a] = u >= 0.0f ? (u < n - 1.0f ? (int)u : (1 << nb[a]) - 1) : 0;
     }
     int cell = 0, k = 0;
-    for (int b = 0; b < 6; ++b)
+    for (int b = 0; b < 8; ++b)
         for (int a = 0; a < 3; ++a)
             if (b < nb[a]) cell |= ((c[a] >> b) & 1) << k++;
     return cell;
@@ -880,8 +880,8 @@ __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits) 
 
 __device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
     const int sid = __float_as_int(d.w);
-    // One scene in the wave: a 64 x 64 x 64 origin grid (18 bits).
-    if (Q.n_scenes == 1) return cell_bits(Q.scenes[sid], o, 18);
+    // One scene in the wave: the origin grid alone.
+    if (Q.n_scenes == 1) return cell_bits(Q.scenes[sid], o, DFPT_SHADOW_CELL_BITS);
     return (((sid - first) & 3) << 12) | shadow_bin(Q.scenes[sid], o);
 }
 
