@@ -160,11 +160,11 @@ struct DevPass {
     int* sort_count_shadow;    // the same for the sun shadow rays
     int* sort_partials;        // DFPT_SORT_CHUNKS chunk sums of the scan
 };
-// Bins: waves of several scenes use 2 bits of scene (within a wave) x 3 bits of octant x 9 bits of
-// cell (bounce rays) or 12 bits of cell (shadow rays); waves of one scene use the octant over an
+// Bins: waves of several scenes use 3 bits of scene (within a wave) x 3 bits of octant x 15 bits of
+// cell (bounce rays) or x 18 bits of cell (shadow rays); waves of one scene use the octant over an
 // origin grid of DFPT_RAY_CELL_BITS bits (bounce rays) or a grid of DFPT_SHADOW_CELL_BITS bits
-// (shadow rays), multiples of 3 (an equal split over the axes). The scan runs over
-// DFPT_SORT_CHUNKS chunks of 1024 bins.
+// (shadow rays), multiples of 3 (an equal split over the axes). Every key stays below 2^21. The
+// scan runs over DFPT_SORT_CHUNKS chunks of 1024 bins.
 #ifndef DFPT_RAY_CELL_BITS
 #define DFPT_RAY_CELL_BITS 18
 #endif
@@ -172,7 +172,7 @@ struct DevPass {
 #define DFPT_SHADOW_CELL_BITS 21
 #endif
 #define DFPT_SORT_BITS (DFPT_RAY_CELL_BITS + 3 > DFPT_SHADOW_CELL_BITS ? DFPT_RAY_CELL_BITS + 3 : DFPT_SHADOW_CELL_BITS)
-#define DFPT_SORT_BINS (1 << (DFPT_SORT_BITS < 14 ? 14 : DFPT_SORT_BITS))
+#define DFPT_SORT_BINS (1 << (DFPT_SORT_BITS < 21 ? 21 : DFPT_SORT_BITS))
 #define DFPT_SORT_CHUNKS (DFPT_SORT_BINS / 1024)
 
 // Many scenes rendered by one set of launches. Every scene's samples form one global sequence

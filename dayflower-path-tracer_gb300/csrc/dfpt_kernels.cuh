@@ -799,11 +799,11 @@ __device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx
 }
 
 // Ray binning between bounces: the bin of a ray is its direction octant (3 bits) and its origin's
-// cell in an 8 x 8 x 8 grid over its scene's bounds, in Morton order (9 bits), under 2 bits of its
-// scene's place in the wave (a wave holds consecutive scenes). Rays of a bin start near each other
-// and head the same way, so a warp of them walks much the same nodes. Only the processing order
-// changes: every ray keeps its path id and its own result.
-__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d);
+// cell in a grid over its scene's bounds (axis bits interleaved), under 3 bits of its scene's
+// place in the wave when the wave holds several (consecutive) scenes; shadow rays, all headed for
+// the sun, are binned by origin cell alone. Rays of a bin start near each other and head the same
+// way, so a warp of them walks much the same nodes. Only the processing order changes: every ray
+// keeps its path id and its own result. Keys stay below DFPT_SORT_BINS = 2^21.
 __device__ __forceinline__ int wave_first_scene(const DevBatch& Q) { return (int)Q.wave_tab[0]; }
 __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits);
 __device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
@@ -813,21 +813,9 @@ __device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, flo
         const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
         return (oct << DFPT_RAY_CELL_BITS) | cell_bits(Q.scenes[sid], o, DFPT_RAY_CELL_BITS);
     }
-    return (((sid - first) & 3) << 12) | ray_bin(Q.scenes[sid], o, d);
-}
-__device__ __forceinline__ int ray_bin(const DevScene& S, float4 o, float4 d) {
-    int cell = 0;
-    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
-    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
-    const float p[3] = {o.x, o.y, o.z};
-    int c[3];
-    for (int a = 0; a < 3; ++a) {
-        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 8.0f;
-        c[a] = u >= 0.0f ? (u < 7.0f ? (int)u : 7) : 0;  // NaN and below: 0
-    }
-    for (int b = 0; b < 3; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
+    // Several scenes: 3 bits of the scene's place in the wave over the octant and a 32^3 grid.
     const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
-    return (oct << 9) | cell;
+    return (((sid - first) & 7) << 18) | (oct << 15) | cell_bits(Q.scenes[sid], o, 15);
 }
 
 // Bin counts with one atomic per distinct bin of a warp.
@@ -836,21 +824,6 @@ __device__ __forceinline__ void bin_count(int* bins, int key) {
     if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(bins + key, __popc(same));
 }
 
-// Shadow rays all head for the sun: their bin is the origin's cell in a 16 x 16 x 16 grid over the
-// scene bounds (Morton order, 12 bits).
-__device__ __forceinline__ int shadow_bin(const DevScene& S, float4 o) {
-    const float lo[3] = {S.bounds_lo.x, S.bounds_lo.y, S.bounds_lo.z};
-    const float hi[3] = {S.bounds_hi.x, S.bounds_hi.y, S.bounds_hi.z};
-    const float p[3] = {o.x, o.y, o.z};
-    int c[3];
-    for (int a = 0; a < 3; ++a) {
-        const float u = (p[a] - lo[a]) / (hi[a] - lo[a]) * 16.0f;
-        c[a] = u >= 0.0f ? (u < 15.0f ? (int)u : 15) : 0;
-    }
-    int cell = 0;
-    for (int b = 0; b < 4; ++b) cell |= (((c[0] >> b) & 1) << (3 * b)) | (((c[1] >> b) & 1) << (3 * b + 1)) | (((c[2] >> b) & 1) << (3 * b + 2));
-    return cell;
-}
 
 // Origin cell over the scene bounds with `bits` bits in all (at most 24: bits / 3 per axis, the
 // remainder to the axes of largest extent), axis bits interleaved from the least significant up.
@@ -882,7 +855,8 @@ __device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, 
     const int sid = __float_as_int(d.w);
     // One scene in the wave: the origin grid alone.
     if (Q.n_scenes == 1) return cell_bits(Q.scenes[sid], o, DFPT_SHADOW_CELL_BITS);
-    return (((sid - first) & 3) << 12) | shadow_bin(Q.scenes[sid], o);
+    // Several scenes: 3 bits of the scene's place in the wave over a 64^3 grid.
+    return (((sid - first) & 7) << 18) | cell_bits(Q.scenes[sid], o, 18);
 }
 
 // One bounce of shading: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
