@@ -650,6 +650,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": peak_note,
                      "kernel": "k_trace<closest>", "avg_launch_ms": avg_trace_ms,
+                     "note": "algorithmic bytes (node and triangle records per closest-hit segment); the records "
+                             "stay L2-resident, DRAM carries the rays (traffic), so achieved can exceed the HBM copy rate",
                      "bytes_per_segment": bytes_per_seg, "oracle_bytes_per_segment": oracle_bytes_per_seg,
                      "nodes_per_segment": nodes_per_seg, "triangles_per_segment": tris_per_seg,
                      "segments_per_launch": closest_segments / launches_per_step,

@@ -166,12 +166,18 @@ struct DevPass {
 // (shadow rays), multiples of 3 (an equal split over the axes). Every key stays below 2^21. The
 // scan runs over DFPT_SORT_CHUNKS chunks of 1024 bins.
 #ifndef DFPT_RAY_CELL_BITS
-#define DFPT_RAY_CELL_BITS 18
+#define DFPT_RAY_CELL_BITS 15
 #endif
 #ifndef DFPT_SHADOW_CELL_BITS
 #define DFPT_SHADOW_CELL_BITS 21
 #endif
-#define DFPT_SORT_BITS (DFPT_RAY_CELL_BITS + 3 > DFPT_SHADOW_CELL_BITS ? DFPT_RAY_CELL_BITS + 3 : DFPT_SHADOW_CELL_BITS)
+#ifndef DFPT_RAY_DIR_RES
+#define DFPT_RAY_DIR_RES 4  // 0: direction octant (3 bits); n: cube-map bins, 6 x n x n directions
+#endif
+#define DFPT_RAY_DIR_COUNT (DFPT_RAY_DIR_RES ? 6 * DFPT_RAY_DIR_RES * DFPT_RAY_DIR_RES : 8)
+#define DFPT_RAY_DIR_BITS (DFPT_RAY_DIR_COUNT <= 8 ? 3 : DFPT_RAY_DIR_COUNT <= 16 ? 4 : DFPT_RAY_DIR_COUNT <= 32 ? 5 : \
+                           DFPT_RAY_DIR_COUNT <= 64 ? 6 : DFPT_RAY_DIR_COUNT <= 128 ? 7 : DFPT_RAY_DIR_COUNT <= 256 ? 8 : 9)
+#define DFPT_SORT_BITS (DFPT_RAY_CELL_BITS + DFPT_RAY_DIR_BITS > DFPT_SHADOW_CELL_BITS ? DFPT_RAY_CELL_BITS + DFPT_RAY_DIR_BITS : DFPT_SHADOW_CELL_BITS)
 #define DFPT_SORT_BINS (1 << (DFPT_SORT_BITS < 21 ? 21 : DFPT_SORT_BITS))
 #define DFPT_SORT_CHUNKS (DFPT_SORT_BINS / 1024)
 
