@@ -174,11 +174,14 @@ struct DevPass {
 #ifndef DFPT_RAY_DIR_RES
 #define DFPT_RAY_DIR_RES 4  // 0: direction octant (3 bits); n: cube-map bins, 6 x n x n directions
 #endif
+#ifndef DFPT_BATCH_DIR_BINS
+#define DFPT_BATCH_DIR_BINS 1  // waves of several scenes: 1 cube-map 6 x 4 x 4 direction bins, 0 the octant
+#endif
 #define DFPT_RAY_DIR_COUNT (DFPT_RAY_DIR_RES ? 6 * DFPT_RAY_DIR_RES * DFPT_RAY_DIR_RES : 8)
 #define DFPT_RAY_DIR_BITS (DFPT_RAY_DIR_COUNT <= 8 ? 3 : DFPT_RAY_DIR_COUNT <= 16 ? 4 : DFPT_RAY_DIR_COUNT <= 32 ? 5 : \
                            DFPT_RAY_DIR_COUNT <= 64 ? 6 : DFPT_RAY_DIR_COUNT <= 128 ? 7 : DFPT_RAY_DIR_COUNT <= 256 ? 8 : 9)
 #define DFPT_SORT_BITS (DFPT_RAY_CELL_BITS + DFPT_RAY_DIR_BITS > DFPT_SHADOW_CELL_BITS ? DFPT_RAY_CELL_BITS + DFPT_RAY_DIR_BITS : DFPT_SHADOW_CELL_BITS)
-#define DFPT_SORT_BINS (1 << (DFPT_SORT_BITS < 21 ? 21 : DFPT_SORT_BITS))
+#define DFPT_SORT_BINS (1 << (DFPT_SORT_BITS < 22 ? 22 : DFPT_SORT_BITS))  // several scenes: up to 22 bits
 #define DFPT_SORT_CHUNKS (DFPT_SORT_BINS / 1024)
 
 // Many scenes rendered by one set of launches. Every scene's samples form one global sequence

@@ -806,30 +806,39 @@ __device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx
 // keeps its path id and its own result. Keys stay below DFPT_SORT_BINS = 2^21.
 __device__ __forceinline__ int wave_first_scene(const DevBatch& Q) { return (int)Q.wave_tab[0]; }
 __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits);
+// Cube-map direction bin: the major axis and its sign, the two minor components over the face in
+// N steps each (6 N^2 values).
+template <int N>
+__device__ __forceinline__ int cube_dir_bin(float4 d) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    const int major = ax >= ay && ax >= az ? 0 : ay >= az ? 1 : 2;
+    const float m = major == 0 ? d.x : major == 1 ? d.y : d.z;
+    const float u = major == 0 ? d.y : d.x, v = major == 2 ? d.y : d.z;
+    const float r = (0.5f * N) / fmaxf(fabsf(m), 1e-30f);
+    const int iu = min(N - 1, max(0, (int)(u * r + 0.5f * N))), iv = min(N - 1, max(0, (int)(v * r + 0.5f * N)));
+    return ((major * 2 + (m < 0.0f ? 1 : 0)) * N + iu) * N + iv;
+}
 __device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, float4 o, float4 d) {
     const int sid = __float_as_int(d.w);
     if (Q.n_scenes == 1) {
 #if DFPT_RAY_DIR_RES
-        // One scene in the wave: a cube-map direction bin (major axis and sign, the two minor
-        // components over the face in DFPT_RAY_DIR_RES steps each) over the origin grid.
-        constexpr int N = DFPT_RAY_DIR_RES;
-        const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-        const int major = ax >= ay && ax >= az ? 0 : ay >= az ? 1 : 2;
-        const float m = major == 0 ? d.x : major == 1 ? d.y : d.z;
-        const float u = major == 0 ? d.y : d.x, v = major == 2 ? d.y : d.z;
-        const float r = (0.5f * N) / fmaxf(fabsf(m), 1e-30f);
-        const int iu = min(N - 1, max(0, (int)(u * r + 0.5f * N))), iv = min(N - 1, max(0, (int)(v * r + 0.5f * N)));
-        const int dir = ((major * 2 + (m < 0.0f ? 1 : 0)) * N + iu) * N + iv;
-        return (dir << DFPT_RAY_CELL_BITS) | cell_bits(Q.scenes[sid], o, DFPT_RAY_CELL_BITS);
+        // One scene in the wave: a cube-map direction bin over the origin grid.
+        return (cube_dir_bin<DFPT_RAY_DIR_RES>(d) << DFPT_RAY_CELL_BITS) | cell_bits(Q.scenes[sid], o, DFPT_RAY_CELL_BITS);
 #else
         // One scene in the wave: no scene bits; the octant over the origin grid.
         const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
         return (oct << DFPT_RAY_CELL_BITS) | cell_bits(Q.scenes[sid], o, DFPT_RAY_CELL_BITS);
 #endif
     }
+#if DFPT_BATCH_DIR_BINS
+    // Several scenes: 3 bits of the scene's place in the wave over a 6 x 4 x 4 direction bin
+    // (7 bits) and a 16^3 grid.
+    return (((sid - first) & 7) << 19) | (cube_dir_bin<4>(d) << 12) | cell_bits(Q.scenes[sid], o, 12);
+#else
     // Several scenes: 3 bits of the scene's place in the wave over the octant and a 32^3 grid.
     const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
     return (((sid - first) & 7) << 18) | (oct << 15) | cell_bits(Q.scenes[sid], o, 15);
+#endif
 }
 
 // Bin counts with one atomic per distinct bin of a warp.
