@@ -209,7 +209,13 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
 /* Launch tuning (no reference counterpart; results never depend on it). Keys:
  *   "trace_config"      traversal kernel configuration (walk variant x block size x resident
  *                       blocks per SM, 0..N-1, N readable as "trace_configs"); every configuration
- *                       visits the same nodes in the same order;
+ *                       visits the same nodes in the same order (16: the compact pair walk for
+ *                       closest hits, the autotuner's usual pick);
+ *   "pair_stack"        stack entries of the compact pair walk (1..8, default 8); fewer entries
+ *                       take its overflow path more often (same hits; a rejected node may then be
+ *                       counted twice by the visit counters);
+ *   "trace_carveout"    shared-memory carveout preference of the current configuration's
+ *                       closest-hit kernels (percent, -1 the driver's choice; process-wide);
  *   "primitive_culling" 0 the reference's full primitive loop, 1 a padded world-box test per
  *                       primitive, 2 candidates from a BVH over those boxes, tested in primitive
  *                       order (scenes with fewer than 8 bounded primitives always use 0);
@@ -217,8 +223,10 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       access-policy window on the handle's stream; 0 turns it off;
  *   "wide_samples"      passes per wave when dfpt_render renders several passes (1..64, default
  *                       8; 1 renders pass by pass); the film is the same either way;
- *   "ray_sort"          1 (default) bins rays by origin cell and direction octant between the
- *                       bounces of wide passes (processing order only);
+ *   "ray_sort"          1 (default) bins rays by direction and origin cell between the bounces of
+ *                       wide passes (processing order only);
+ *   "shadow_sort"       with ray_sort, 1 (default) also bins the sun shadow rays by origin cell
+ *                       before their launch;
  *   "shadow_defer"      0 (default) traces each bounce's sun shadow rays after its shading in wide
  *                       passes; 1 traces all bounces' at once after the last (faster, but the
  *                       shadow queue holds depth x as many rays). */
