@@ -885,7 +885,10 @@ __device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, 
 // One bounce of shading: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
 // roulette, material sampling and the next ray (GRK:3185-3686).
 template <bool BATCH>
-__global__ void __launch_bounds__(256, 3) k_shade(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
+#ifndef DFPT_SHADE_MINB
+#define DFPT_SHADE_MINB 3  // resident blocks of 256 per SM the shading kernel is compiled for
+#endif
+__global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     const int n = B.counts[bounce];
     const int qi = B.sorted_queues ? 0 : (bounce & 1);
     const uint32_t pass = BATCH ? 0u : (uint32_t)*B.pass_index;
