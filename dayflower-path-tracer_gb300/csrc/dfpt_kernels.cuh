@@ -552,6 +552,30 @@ template <bool BATCH>
 __device__ __forceinline__ bool lean_start(const DevParams& P) {
     return BATCH && P.rng_kind == DFPT_RNG_COUNTER && !P.diff;
 }
+#ifdef DFPT_ONE_SCENE
+// A handle's waves (one scene, sample order pass-major from a first sample at a pass boundary).
+// When the capacity is a whole number of passes every wave holds whole passes, and its slots run
+// pixel-major: the wave's samples of one pixel are adjacent, so a warp's primary rays leave one or
+// two pixels. wave_passes returns the passes of the current wave, or 0 when the slots stay in
+// sample order. `rel` is a sample's place in the wave in sample order.
+__device__ __forceinline__ unsigned wave_passes(const DevBatch& Q, long long np) {
+    if (Q.capacity % np != 0) return 0u;
+    const long long base = Q.wave_base[0];
+    const long long end = base + Q.capacity < Q.wave_base[1] ? base + Q.capacity : Q.wave_base[1];
+    return (unsigned)((end - base) / np);
+}
+__device__ __forceinline__ unsigned slot_of_rel(unsigned rel, unsigned np, unsigned passes) {
+    if (passes == 0u) return rel;
+    const unsigned j = rel / np;
+    return (rel - j * np) * passes + j;
+}
+__device__ __forceinline__ unsigned rel_of_slot(unsigned slot, unsigned np, unsigned passes) {
+    if (passes == 0u) return slot;
+    const unsigned x = slot / passes;
+    return (slot - x * passes) * np + x;
+}
+#endif
+
 __device__ __forceinline__ uint32_t camera_draws(const DevScene& S, const DevParams& P) {
     const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
                     (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
@@ -568,6 +592,9 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
         end = Q.wave_base[1];
         pass0 = Q.wave_base[2];
     }
+#ifdef DFPT_ONE_SCENE
+    const unsigned wave_p = wave_passes(Q, (long long)Q.params[0].width * Q.params[0].height);
+#endif
     // A thin lens keeps every pixel, so with one scene the queue is the slots in order (no atomics):
     // the valid slots are a prefix.
     const bool dense = (!BATCH || Q.n_scenes == 1) && __ldg(scene_of<BATCH>(S0, Q, 0).camera + 18) != 2.0f;
@@ -582,7 +609,14 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
         uint32_t sample = pass;
         if constexpr (BATCH) {
             if (valid) {
+#ifdef DFPT_ONE_SCENE
+                // Slots past the wave's samples stay invalid (rel_of_slot maps only those below).
+                const unsigned np0 = (unsigned)((long long)Q.params[0].width * Q.params[0].height);
+                const long long g = wave_p == 0u ? base + i
+                                    : (unsigned)i < wave_p * np0 ? base + rel_of_slot((unsigned)i, np0, wave_p) : end;
+#else
                 const long long g = base + i;
+#endif
                 if (g >= end) {
                     valid = false;
                 } else {
@@ -909,8 +943,8 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
 #ifdef DFPT_ONE_SCENE
                 // One scene: the slot's pixel and pass follow from its index as k_camera derived
                 // them (slot i of the wave is sample base + i), without the random slot-key load.
-                const long long local = Q.wave_base[0] + path - Q.sample_begin[0];
                 const long long np = (long long)P.width * P.height;
+                const long long local = Q.wave_base[0] + rel_of_slot((unsigned)path, (unsigned)np, wave_passes(Q, np)) - Q.sample_begin[0];
                 if (local < 0x7FFFFFFFll) {
                     const unsigned q = (unsigned)local / (unsigned)np;
                     rng_pixel = (unsigned)local - q * (unsigned)np;
@@ -1486,8 +1520,15 @@ __global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
         int cnt = B.film_n[f];
         const DevParams& P = Q.params[s];
         const long long pass0 = Q.wave_base[2];
+#ifdef DFPT_ONE_SCENE
+        const unsigned wave_p = wave_passes(Q, np);
+#endif
         for (long long loc = first; loc < b; loc += np) {
+#ifdef DFPT_ONE_SCENE
+            const int slot = (int)slot_of_rel((unsigned)(slot0 + loc), (unsigned)np, wave_p);
+#else
             const int slot = (int)(slot0 + loc);
+#endif
             film_add(B.radiance[PSI(slot)], B.pixel_flags[slot], loc / np == clear_sample, sum, comp, cnt);
             if (P.diff) {
                 // The differentiable forward's per-sample records (as k_film keeps them per pass).
