@@ -1336,6 +1336,10 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     h->ctx.pass = &h->pass;
     h->ctx.stream = h->stream;
     h->fast.occupancy(h->sms, h->ctx.grid, h->ctx.grid_trace, h->ctx.grid_simple);
+    // The compact pair walk: the autotuner's pick on every workload measured (the same hits as
+    // every other configuration).
+    h->ctx.trace_config = DFPT_DEFAULT_TRACE_CONFIG < h->fast.trace_configs ? DFPT_DEFAULT_TRACE_CONFIG : 0;
+    h->ctx.grid_trace = h->fast.trace_grid(h->ctx.trace_config, h->sms);
     r = push_params(h);
     if (!r) r = reset_rng(h);
     if (!r) r = apply_l2_policy(h);

@@ -55,7 +55,7 @@ struct dfpt_batch {
     DevPass pass{};
     DevBatch Q{};
     LaunchCtx ctx{};
-    int trace_config = 2;
+    int trace_config = DFPT_DEFAULT_TRACE_CONFIG;
     bool use_graph = true;
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;

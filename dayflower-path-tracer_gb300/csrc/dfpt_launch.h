@@ -5,6 +5,9 @@
 
 #include "dfpt_device_types.h"
 
+// Traversal configuration a handle or batch starts with (the compact pair walk).
+#define DFPT_DEFAULT_TRACE_CONFIG 16
+
 struct LaunchCtx {
     const DevScene* scene;
     const DevParams* params;  // device pointer
