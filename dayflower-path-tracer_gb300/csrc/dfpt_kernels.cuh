@@ -633,7 +633,12 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
                         pixel = (int)(local - j * np);
                     }
                     sample = (uint32_t)(j + pass0);
+#ifdef DFPT_ONE_SCENE
+                    // One scene: shading derives the key from the slot; the adjoint replay reads it.
+                    if (Q.params[0].diff) Q.slot_key[i] = make_int4(sid, pixel, (int)sample, 0);
+#else
                     Q.slot_key[i] = make_int4(sid, pixel, (int)sample, 0);
+#endif
                 }
             }
         }
