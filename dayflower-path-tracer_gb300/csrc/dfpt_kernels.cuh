@@ -552,6 +552,34 @@ template <bool BATCH>
 __device__ __forceinline__ bool lean_start(const DevParams& P) {
     return BATCH && P.rng_kind == DFPT_RNG_COUNTER && !P.diff;
 }
+#ifndef DFPT_ONE_SCENE
+// Waves of several scenes: within each scene's segment [a, b) of the wave (scene-local sample
+// indices, sample order: pass j, pixel x at j * np + x) the slots run pixel-major, a pixel's
+// samples adjacent in pass order. Pixel x holds K + (x >= a % np) + (x < b % np) of the segment's
+// samples (K = b / np - a / np - 1) and starts at pos(x), the sum of the counts of the pixels
+// before it; seg_local_of_pos inverts pos over its three linear pieces.
+__device__ __forceinline__ long long seg_pos(long long x, long long K, long long ra, long long rb) {
+    return x * K + (x > ra ? x - ra : 0) + (x < rb ? x : rb);
+}
+__device__ __forceinline__ long long seg_pos_of_local(long long loc, long long a, long long b, long long np) {
+    const long long ja = a / np, ra = a - ja * np, jb = b / np, rb = b - jb * np, K = jb - ja - 1;
+    const long long j = loc / np, x = loc - j * np;
+    return seg_pos(x, K, ra, rb) + (j - (ja + (x >= ra ? 0 : 1)));
+}
+__device__ __forceinline__ long long seg_local_of_pos(long long p, long long a, long long b, long long np) {
+    const long long ja = a / np, ra = a - ja * np, jb = b / np, rb = b - jb * np, K = jb - ja - 1;
+    const long long lo = ra < rb ? ra : rb, hi = ra < rb ? rb : ra;
+    const long long s0 = K + 1, s1 = ra < rb ? K + 2 : K;
+    const long long p_lo = lo * s0, p_hi = p_lo + (hi - lo) * s1;
+    long long x;
+    if (p < p_lo) x = p / s0;                     // p_lo > 0 implies s0 > 0
+    else if (p < p_hi) x = lo + (p - p_lo) / s1;  // p_hi > p_lo implies s1 > 0
+    else x = hi + (p - p_hi) / s0;                // reached only when s0 > 0
+    const long long j = ja + (x >= ra ? 0 : 1) + (p - seg_pos(x, K, ra, rb));
+    return j * np + x;
+}
+#endif
+
 #ifdef DFPT_ONE_SCENE
 // A handle's waves (one scene, sample order pass-major from a first sample at a pass boundary).
 // When the capacity is a whole number of passes every wave holds whole passes, and its slots run
@@ -621,8 +649,16 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
                     valid = false;
                 } else {
                     sid = batch_scene_of(Q, g);
-                    const long long local = g - Q.sample_begin[sid];
                     const long long np = (long long)Q.params[sid].width * Q.params[sid].height;
+#ifdef DFPT_ONE_SCENE
+                    const long long local = g - Q.sample_begin[sid];
+#else
+                    // The slot's place in its scene's segment of the wave, pixel-major.
+                    const long long b0 = Q.sample_begin[sid], b1 = Q.sample_begin[sid + 1];
+                    const long long wend = base + Q.capacity < end ? base + Q.capacity : end;
+                    const long long sa = (base > b0 ? base : b0) - b0, sb = (wend < b1 ? wend : b1) - b0;
+                    const long long local = seg_local_of_pos(g - (b0 + sa), sa, sb, np);
+#endif
                     long long j;
                     if (local < 0x7FFFFFFFll) {  // 32-bit division where it fits (np < 2^28)
                         const unsigned q = (unsigned)local / (unsigned)np;
@@ -1532,7 +1568,7 @@ __global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
 #ifdef DFPT_ONE_SCENE
             const int slot = (int)slot_of_rel((unsigned)(slot0 + loc), (unsigned)np, wave_p);
 #else
-            const int slot = (int)(slot0 + loc);
+            const int slot = (int)(slot0 + a + seg_pos_of_local(loc, a, b, np));
 #endif
             film_add(B.radiance[PSI(slot)], B.pixel_flags[slot], loc / np == clear_sample, sum, comp, cnt);
             if (P.diff) {
