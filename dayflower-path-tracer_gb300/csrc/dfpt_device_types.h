@@ -160,11 +160,12 @@ struct DevPass {
     int* sort_count_shadow;    // the same for the sun shadow rays
     int* sort_partials;        // DFPT_SORT_CHUNKS chunk sums of the scan
 };
-// Bins: waves of several scenes use 3 bits of scene (within a wave) x 3 bits of octant x 15 bits of
-// cell (bounce rays) or x 18 bits of cell (shadow rays); waves of one scene use the octant over an
-// origin grid of DFPT_RAY_CELL_BITS bits (bounce rays) or a grid of DFPT_SHADOW_CELL_BITS bits
-// (shadow rays), multiples of 3 (an equal split over the axes). Every key stays below 2^21. The
-// scan runs over DFPT_SORT_CHUNKS chunks of 1024 bins.
+// Bins: waves of several scenes use 3 bits of scene (within a wave) x a 6 x 4 x 4 cube-map
+// direction bin (7 bits) x 12 bits of origin cell (bounce rays), or 3 bits of scene x 18 bits of
+// cell (shadow rays); waves of one scene use a direction bin (DFPT_RAY_DIR_RES) over an origin grid
+// of DFPT_RAY_CELL_BITS bits (bounce rays) or a grid of DFPT_SHADOW_CELL_BITS bits (shadow rays),
+// multiples of 3 (an equal split over the axes). Every key stays below DFPT_SORT_BINS (2^22 with
+// these settings). The scan runs over DFPT_SORT_CHUNKS chunks of 1024 bins.
 #ifndef DFPT_RAY_CELL_BITS
 #define DFPT_RAY_CELL_BITS 15
 #endif

@@ -873,12 +873,12 @@ __device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx
     return out;
 }
 
-// Ray binning between bounces: the bin of a ray is its direction octant (3 bits) and its origin's
-// cell in a grid over its scene's bounds (axis bits interleaved), under 3 bits of its scene's
+// Ray binning between bounces: the bin of a ray is its direction bin (cube-map or octant) and its
+// origin's cell in a grid over its scene's bounds (axis bits interleaved), under 3 bits of its scene's
 // place in the wave when the wave holds several (consecutive) scenes; shadow rays, all headed for
 // the sun, are binned by origin cell alone. Rays of a bin start near each other and head the same
 // way, so a warp of them walks much the same nodes. Only the processing order changes: every ray
-// keeps its path id and its own result. Keys stay below DFPT_SORT_BINS = 2^21.
+// keeps its path id and its own result. Keys stay below DFPT_SORT_BINS.
 __device__ __forceinline__ int wave_first_scene(const DevBatch& Q) { return (int)Q.wave_tab[0]; }
 __device__ __forceinline__ int cell_bits(const DevScene& S, float4 o, int bits);
 // Cube-map direction bin: the major axis and its sign, the two minor components over the face in
