@@ -9,12 +9,16 @@ Method names follow AbstractRendererKernel / AbstractImageKernel / GPURendererKe
   update_camera/update_primitives/update_sun_and_sky                         (GPURendererKernel.java:455-569)
   toggle_sky/toggle_sun/toggle_primitive_material/toggle_primitive_selection  (GPURendererKernel.java:314-397)
   set_renderer_type, set_tone_mapper_type, ... and the matching getters     (AbstractRendererKernel.java:383-580)
+  toggle_renderer_type/_normal_mapping/_wireframes, toggle_shader_type       (AbstractRendererKernel.java:591-690)
+  is_renderer_type_*, has_changed/set_changed                                (AbstractRendererKernel.java:238-297, 383)
+  set_global_*/get_global_* (noise parameters)                               (AbstractKernel.java:205-295)
 Errors: a size mismatch in update() raises ValueError, the IllegalArgumentException of
 AbstractImageKernel.java:146-148; device failures raise DfptError.
 """
 from __future__ import annotations
 
 import ctypes as C
+import struct
 
 import numpy as np
 
@@ -61,6 +65,7 @@ class RendererKernel:
         self.resolution_y = 0
         self._selected_primitive_offset = -1
         self._selected_primitive_index = -1
+        self._has_changed = False
 
     # -- lifecycle -------------------------------------------------------------------------
     def update(self, resolution_x: int, resolution_y: int, image_data_byte=None, local_size: int = 0) -> None:
@@ -234,13 +239,90 @@ class RendererKernel:
         return self._selected_primitive_index
 
     # -- settings (AbstractRendererKernel setters) ------------------------------------------
-    def _set(self, name, value, allowed=None):
+    @staticmethod
+    def _differs(old, new) -> bool:
+        """!=, with Float.compare's semantics for floats (NaN equals NaN, -0.0 differs from 0.0)."""
+        if isinstance(old, float) or isinstance(new, float):
+            def bits(v):
+                return struct.unpack("<I", struct.pack("<f", float("nan") if v != v else v))[0]
+            return bits(float(old)) != bits(float(new))
+        return old != new
+
+    def _set(self, name, value, allowed=None, mark=True):
         if allowed is not None and value not in allowed:
             return  # the reference ignores unknown values
-        if getattr(self.params, name) != value:
+        if self._differs(getattr(self.params, name), value):
             setattr(self.params, name, value)
+            if mark:
+                self._has_changed = True  # the setters and toggles of AbstractRendererKernel mark a change
             if self._h:
                 self._push_params()
+
+    def has_changed(self) -> bool:
+        """AbstractRendererKernel.hasChanged (AbstractRendererKernel.java:238-240)."""
+        return self._has_changed
+
+    def set_changed(self, has_changed: bool) -> None:
+        """AbstractRendererKernel.setChanged (AbstractRendererKernel.java:383-385)."""
+        self._has_changed = bool(has_changed)
+
+    # Renderer-type predicates (AbstractRendererKernel.java:247-297).
+    def is_renderer_type_ambient_occlusion(self) -> bool:
+        return self.params.renderer_type == RENDERER_TYPE_AMBIENT_OCCLUSION
+
+    def is_renderer_type_path_tracer(self) -> bool:
+        return self.params.renderer_type == RENDERER_TYPE_PATH_TRACER
+
+    def is_renderer_type_ray_caster(self) -> bool:
+        return self.params.renderer_type == RENDERER_TYPE_RAY_CASTER
+
+    def is_renderer_type_ray_marcher(self) -> bool:
+        return self.params.renderer_type == RENDERER_TYPE_RAY_MARCHER
+
+    def is_renderer_type_ray_tracer(self) -> bool:
+        return self.params.renderer_type == RENDERER_TYPE_RAY_TRACER
+
+    def is_renderer_type_surface_normals(self) -> bool:
+        return self.params.renderer_type == RENDERER_TYPE_SURFACE_NORMALS
+
+    # Toggles (AbstractRendererKernel.java:591-690): unknown current values stay as they are.
+    _RENDERER_TYPE_CYCLE = {RENDERER_TYPE_AMBIENT_OCCLUSION: RENDERER_TYPE_PATH_TRACER,
+                            RENDERER_TYPE_PATH_TRACER: RENDERER_TYPE_RAY_CASTER,
+                            RENDERER_TYPE_RAY_CASTER: RENDERER_TYPE_RAY_MARCHER,
+                            RENDERER_TYPE_RAY_MARCHER: RENDERER_TYPE_RAY_TRACER,
+                            RENDERER_TYPE_RAY_TRACER: RENDERER_TYPE_SURFACE_NORMALS,
+                            RENDERER_TYPE_SURFACE_NORMALS: RENDERER_TYPE_AMBIENT_OCCLUSION}
+
+    def toggle_renderer_type(self) -> None:
+        nxt = self._RENDERER_TYPE_CYCLE.get(self.params.renderer_type)
+        if nxt is not None:
+            self._set("renderer_type", nxt)
+
+    def toggle_renderer_normal_mapping(self) -> None:
+        v = self.params.normal_mapping
+        if v in (BOOLEAN_FALSE, BOOLEAN_TRUE):
+            self._set("normal_mapping", BOOLEAN_TRUE if v == BOOLEAN_FALSE else BOOLEAN_FALSE)
+
+    def toggle_renderer_wireframes(self) -> None:
+        v = self.params.wireframes
+        if v in (BOOLEAN_FALSE, BOOLEAN_TRUE):
+            self._set("wireframes", BOOLEAN_TRUE if v == BOOLEAN_FALSE else BOOLEAN_FALSE)
+
+    def toggle_shader_type(self) -> None:
+        v = self.params.shader_type
+        if v in (SHADER_TYPE_FLAT, SHADER_TYPE_GOURAUD):
+            self._set("shader_type", SHADER_TYPE_GOURAUD if v == SHADER_TYPE_FLAT else SHADER_TYPE_FLAT)
+
+    # Scene accessors (AbstractRendererKernel getCompiledScene / getSky / getCamera): the compiled
+    # scene's arrays, the sky record and the camera's 19 floats.
+    def get_compiled_scene(self) -> CompiledScene:
+        return self.compiled
+
+    def get_sky(self) -> SkyState:
+        return self.sky
+
+    def get_camera(self) -> np.ndarray:
+        return self.compiled.camera
 
     def set_renderer_type(self, v: int) -> None:
         self._set("renderer_type", v, (1, 2, 3, 4, 5, 6))
@@ -270,19 +352,19 @@ class RendererKernel:
         self._set("ao_maximum_distance", float(v))
 
     def set_global_amplitude(self, v: float) -> None:
-        self._set("global_amplitude", float(v))
+        self._set("global_amplitude", float(v), mark=False)  # AbstractKernel's setters mark nothing
 
     def set_global_frequency(self, v: float) -> None:
-        self._set("global_frequency", float(v))
+        self._set("global_frequency", float(v), mark=False)  # AbstractKernel's setters mark nothing
 
     def set_global_gain(self, v: float) -> None:
-        self._set("global_gain", float(v))
+        self._set("global_gain", float(v), mark=False)  # AbstractKernel's setters mark nothing
 
     def set_global_lacunarity(self, v: float) -> None:
-        self._set("global_lacunarity", float(v))
+        self._set("global_lacunarity", float(v), mark=False)  # AbstractKernel's setters mark nothing
 
     def set_global_octaves(self, v: int) -> None:
-        self._set("global_octaves", int(v))
+        self._set("global_octaves", int(v), mark=False)
 
     def set_seed(self, seed: int, rng_kind: int = RNG_COUNTER) -> None:
         self.params.seed = int(seed) & ((1 << 64) - 1)
@@ -307,3 +389,27 @@ class RendererKernel:
 
     def get_renderer_pt_ray_depth_russian_roulette(self) -> int:
         return self.params.pt_ray_depth_russian_roulette
+
+    def get_renderer_ao_maximum_distance(self) -> float:
+        return self.params.ao_maximum_distance
+
+    def get_renderer_normal_mapping(self) -> int:
+        return self.params.normal_mapping
+
+    def get_renderer_wireframes(self) -> int:
+        return self.params.wireframes
+
+    def get_global_amplitude(self) -> float:
+        return self.params.global_amplitude
+
+    def get_global_frequency(self) -> float:
+        return self.params.global_frequency
+
+    def get_global_gain(self) -> float:
+        return self.params.global_gain
+
+    def get_global_lacunarity(self) -> float:
+        return self.params.global_lacunarity
+
+    def get_global_octaves(self) -> int:
+        return self.params.global_octaves
