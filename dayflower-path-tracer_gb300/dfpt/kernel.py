@@ -203,12 +203,18 @@ class RendererKernel:
         check(self._lib.dfpt_set_sky(self._need(), C.byref(self.sky.raw)))
 
     def toggle_sky(self) -> None:
+        """GPURendererKernel.toggleSky: flips the sky and marks a change; pushed when a handle exists."""
         self.sky.raw.is_sky_active = 0 if self.sky.raw.is_sky_active == 1 else 1
-        self.update_sun_and_sky()
+        self._has_changed = True
+        if self._h:
+            self.update_sun_and_sky()
 
     def toggle_sun(self) -> None:
+        """GPURendererKernel.toggleSun: flips the sun and marks a change; pushed when a handle exists."""
         self.sky.raw.is_sun_active = 0 if self.sky.raw.is_sun_active == 1 else 1
-        self.update_sun_and_sky()
+        self._has_changed = True
+        if self._h:
+            self.update_sun_and_sky()
 
     def toggle_primitive_material(self) -> None:
         off = self._selected_primitive_offset
@@ -219,7 +225,9 @@ class RendererKernel:
         order = [CLEAR_COAT, GLASS, LAMBERTIAN, PHONG, REFLECTION]
         if 0 <= old - 1 < len(order):
             self.compiled.surfaces[so] = order[(old - 1 + 1) % len(order)]
-            check(self._lib.dfpt_set_surfaces(self._need(), ptr(self.compiled.surfaces, C.c_float), self.compiled.surfaces.size))
+            self._has_changed = True
+            if self._h:
+                check(self._lib.dfpt_set_surfaces(self._h, ptr(self.compiled.surfaces, C.c_float), self.compiled.surfaces.size))
 
     def toggle_primitive_selection(self, x: int, y: int) -> None:
         offs = self.primitive_offsets()

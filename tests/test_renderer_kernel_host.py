@@ -90,3 +90,28 @@ def test_scene_accessors(rk):
     assert rk.get_compiled_scene() is rk.compiled
     assert rk.get_sky() is rk.sky
     assert rk.get_camera().shape == (19,)
+
+
+def test_sky_and_sun_toggles_mark_changes(rk):
+    sky0, sun0 = rk.get_sky().raw.is_sky_active, rk.get_sky().raw.is_sun_active
+    rk.toggle_sky()
+    assert rk.has_changed() and rk.get_sky().raw.is_sky_active == 1 - sky0
+    rk.set_changed(False)
+    rk.toggle_sun()
+    assert rk.has_changed() and rk.get_sky().raw.is_sun_active == 1 - sun0
+
+
+def test_primitive_material_toggle_cycles_the_selected_surface(rk):
+    from dfpt.scene import CLEAR_COAT, GLASS, LAMBERTIAN, PHONG, REFLECTION
+
+    rk.toggle_primitive_material()  # nothing selected: no change (GPURendererKernel.togglePrimitiveMaterial)
+    assert not rk.has_changed()
+    off = 3  # the second primitive's offset in the primitives array
+    rk._selected_primitive_offset = off
+    so = int(rk.compiled.primitives[off + 2])
+    order = [CLEAR_COAT, GLASS, LAMBERTIAN, PHONG, REFLECTION]
+    first = int(rk.compiled.surfaces[so])
+    for k in range(1, 6):
+        rk.toggle_primitive_material()
+        assert int(rk.compiled.surfaces[so]) == order[(first - 1 + k) % 5]
+    assert rk.has_changed()
