@@ -43,7 +43,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "M path samples/s @1080p"
 UNIT = "M samples/s"
 # Measured DRAM bytes (read + write) per closest-hit segment of the traversal kernel on
-# mesh_scene: one ncu capture at 960x540 (profiles/k_trace_dram_mesh_scene_960x540.md).
+# mesh_scene: one ncu capture of the traversal kernel at 960x540.
 TRACE_DRAM_BYTES_PER_SEGMENT = 65.5
 
 
@@ -622,7 +622,7 @@ def main():
     bytes_per_launch = closest_segments / launches_per_step * bytes_per_seg
     achieved = closest_segments * bytes_per_seg / (trace_ms_per_step / 1e3) / 1e9
     # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum per closest-hit
-    # segment of the mesh_scene traversal at 960x540 (profiles/k_trace_dram_mesh_scene_960x540.md),
+    # segment of the mesh_scene traversal at 960x540 (one ncu capture),
     # scaled by this run's segments per launch (the traffic grows with the rays of a launch).
     traffic = None
     if args.workload == "mesh_scene" and TRACE_DRAM_BYTES_PER_SEGMENT:

@@ -532,6 +532,9 @@ void release(dfpt_handle* h) {
     h->dev_params.release();
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
+    // Lines the window marked persisting go back to normal with the records they cached.
+    if (h->l2_window.num_bytes > 0) (void)cudaCtxResetPersistingL2Cache();
+    h->l2_window = cudaAccessPolicyWindow{};
 }
 
 }  // namespace
@@ -865,6 +868,8 @@ int wide_prepare(dfpt_handle* h) {
 }
 
 // One wave; returns the number of kernels launched.
+cudaError_t graph_l2_window(dfpt_handle* h, cudaGraph_t g);
+
 int issue_wide_wave(dfpt_handle* h) {
     const KernelSet& K = h->wide;
     const LaunchCtx& c = h->wctx;
@@ -921,6 +926,7 @@ int render_wide(dfpt_handle* h, int passes) {
             CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
             const int k = issue_wide_wave(h);
             cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+            if (e == cudaSuccess) e = graph_l2_window(h, g);
             if (e == cudaSuccess) e = cudaGraphInstantiate(&h->wide_graph, g, 0);
             if (g) cudaGraphDestroy(g);
             if (e != cudaSuccess) {
@@ -973,9 +979,12 @@ int ensure_shadow_capacity(dfpt_handle* h) {
 }
 
 // L2 residency: the traversal records (BVH nodes + triangles, one allocation) get an access-policy
-// window - hits persisting, misses streaming - on the handle's stream and on every kernel node of
-// the pass graph, so the ray queues and path state streaming through L2 each bounce do not evict
-// the scene. The persisting carve-out is a limit of this process's CUDA context (it ends with it).
+// window - hits persisting, misses streaming - on every kernel node of the pass and wave graphs,
+// and on the handle's stream when the handle created that stream, so the ray queues and path
+// state streaming through L2 each bounce do not evict the scene. A stream the caller passed to
+// dfpt_set_stream is never given the window: it outlives the handle, and a window left on it
+// would keep marking a freed range (or another handle's) as persisting. The persisting carve-out
+// is a limit of this process's CUDA context (it ends with it).
 int apply_l2_policy(dfpt_handle* h) {
     cudaAccessPolicyWindow w{};
     if (h->l2_persist && h->sc.trav.p) {
@@ -997,10 +1006,30 @@ int apply_l2_policy(dfpt_handle* h) {
         }
     }
     h->l2_window = w;
-    cudaStreamAttrValue v{};
-    v.accessPolicyWindow = w;
-    CUDA_TRY(cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &v));
+    if (h->own_stream) {
+        cudaStreamAttrValue v{};
+        v.accessPolicyWindow = w;
+        CUDA_TRY(cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &v));
+    }
     return DFPT_OK;
+}
+
+// The handle's L2 window on every kernel node of a captured graph (capture does not carry it).
+cudaError_t graph_l2_window(dfpt_handle* h, cudaGraph_t g) {
+    if (h->l2_window.num_bytes == 0) return cudaSuccess;
+    size_t count = 0;
+    cudaError_t e = cudaGraphGetNodes(g, nullptr, &count);
+    std::vector<cudaGraphNode_t> nodes(count);
+    if (e == cudaSuccess && count) e = cudaGraphGetNodes(g, nodes.data(), &count);
+    cudaKernelNodeAttrValue kv{};
+    kv.accessPolicyWindow = h->l2_window;
+    for (size_t i = 0; e == cudaSuccess && i < count; ++i) {
+        cudaGraphNodeType type;
+        e = cudaGraphNodeGetType(nodes[i], &type);
+        if (e == cudaSuccess && type == cudaGraphNodeTypeKernel)
+            e = cudaGraphKernelNodeSetAttribute(nodes[i], cudaKernelNodeAttributeAccessPolicyWindow, &kv);
+    }
+    return e;
 }
 
 int build_graph(dfpt_handle* h) {
@@ -1016,25 +1045,11 @@ int build_graph(dfpt_handle* h) {
         (void)cudaGetLastError();
         return dfpt_fail(DFPT_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
     }
-    if (h->l2_window.num_bytes > 0) {
-        // The window on every kernel node (capture does not have to carry stream attributes).
-        size_t count = 0;
-        e = cudaGraphGetNodes(g, nullptr, &count);
-        std::vector<cudaGraphNode_t> nodes(count);
-        if (e == cudaSuccess && count) e = cudaGraphGetNodes(g, nodes.data(), &count);
-        cudaKernelNodeAttrValue kv{};
-        kv.accessPolicyWindow = h->l2_window;
-        for (size_t i = 0; e == cudaSuccess && i < count; ++i) {
-            cudaGraphNodeType type;
-            e = cudaGraphNodeGetType(nodes[i], &type);
-            if (e == cudaSuccess && type == cudaGraphNodeTypeKernel)
-                e = cudaGraphKernelNodeSetAttribute(nodes[i], cudaKernelNodeAttributeAccessPolicyWindow, &kv);
-        }
-        if (e != cudaSuccess) {
-            (void)cudaGetLastError();
-            cudaGraphDestroy(g);
-            return dfpt_fail(DFPT_ERR_CUDA, "graph L2 window: %s", cudaGetErrorString(e));
-        }
+    e = graph_l2_window(h, g);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaGraphDestroy(g);
+        return dfpt_fail(DFPT_ERR_CUDA, "graph L2 window: %s", cudaGetErrorString(e));
     }
     e = cudaGraphInstantiate(&h->graph_exec, g, 0);
     cudaGraphDestroy(g);

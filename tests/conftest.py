@@ -4,6 +4,7 @@
 C-ABI's exported symbols and its validation paths); `-m gpu` tests call the CUDA core through
 the C-ABI and compare it with the oracle.
 """
+import os
 import sys
 from pathlib import Path
 
@@ -13,6 +14,17 @@ ROOT = Path(__file__).resolve().parent.parent
 for p in (str(ROOT / "dayflower-path-tracer_gb300"), str(ROOT)):
     if p not in sys.path:
         sys.path.insert(0, p)
+
+
+def reference_resources():
+    """The reference checkout's `resources/distribution/resources` directory (models, textures),
+    named by the DFPT_REFERENCE_RESOURCES environment variable; None when it is unset or absent.
+    Tests that read the reference's own resource files skip without it."""
+    v = os.environ.get("DFPT_REFERENCE_RESOURCES")
+    if not v:
+        return None
+    p = Path(v)
+    return p if p.is_dir() else None
 
 
 def pytest_configure(config):

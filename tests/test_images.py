@@ -13,9 +13,11 @@ import numpy as np
 import pytest
 
 from _imaging import encode_jpeg, png, smooth_image
+from conftest import reference_resources
 from dfpt import images
 
-TEX = Path("/root/reference/resources/distribution/resources/texture")
+_RES = reference_resources()
+TEX = _RES / "texture" if _RES else Path("missing-reference-resources")
 
 
 def _unpack(v):

@@ -9,9 +9,11 @@ import pytest
 
 from dfpt import scene as sc
 from dfpt import scenes
+from conftest import reference_resources
 
-RES = Path("/root/reference/resources/distribution/resources")
-pytestmark = pytest.mark.skipif(not (RES / "model").exists(), reason="reference resources not available")
+RES = reference_resources() or Path("missing-reference-resources")
+pytestmark = pytest.mark.skipif(not (RES / "model").exists(),
+                                reason="reference resources not available (set DFPT_REFERENCE_RESOURCES)")
 
 BUILT = ("Girl_Scene", "House_2_Scene", "Image_Scene", "Material_Showcase_Scene", "Monkey_Scene", "Terrain_Scene",
          "Wine_Glass_Scene")

@@ -5,6 +5,7 @@ from pathlib import Path
 
 import numpy as np
 import pytest
+from conftest import reference_resources
 
 F = np.float32
 
@@ -118,7 +119,7 @@ def test_java_float_parsing():
     assert _java_float("0.1") == F(0.1)
 
 
-ICO = Path("/root/reference/resources/distribution/resources/model/icosphere.obj")
+ICO = (reference_resources() or Path("missing-reference-resources")) / "model" / "icosphere.obj"
 
 
 @pytest.mark.skipif(not ICO.exists(), reason="the reference's model files are not mounted")
