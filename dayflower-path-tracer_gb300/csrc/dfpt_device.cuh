@@ -65,6 +65,23 @@ __device__ __forceinline__ float jmax3(float a, float b, float c) {
 }
 // Aparapi's rsqrt is 1 / sqrt: both correctly rounded here (no fast-math).
 __device__ __forceinline__ float rsqrt_j(float x) { return 1.0f / sqrtf(x); }
+// sin, cos, asin, atan2 and pow of float arguments. The reference's Java path evaluates them as
+// java.lang.Math in double and casts the result to float; the strict set does the same (CUDA's
+// double functions, one rounding to float), so its results equal the strict-FP32 oracle's. The fast
+// sets call the float functions.
+#if defined(DFPT_STRICT_MATH)
+__device__ __forceinline__ float sin_j(float x) { return (float)sin((double)x); }
+__device__ __forceinline__ float cos_j(float x) { return (float)cos((double)x); }
+__device__ __forceinline__ float asin_j(float x) { return (float)asin((double)x); }
+__device__ __forceinline__ float atan2_j(float y, float x) { return (float)atan2((double)y, (double)x); }
+__device__ __forceinline__ float pow_j(float a, float b) { return (float)pow((double)a, (double)b); }
+#else
+__device__ __forceinline__ float sin_j(float x) { return sinf(x); }
+__device__ __forceinline__ float cos_j(float x) { return cosf(x); }
+__device__ __forceinline__ float asin_j(float x) { return asinf(x); }
+__device__ __forceinline__ float atan2_j(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ float pow_j(float a, float b) { return powf(a, b); }
+#endif
 __device__ __forceinline__ float saturate_j(float v, float a, float b) {
     const float lo = jmin(a, b), hi = jmax(a, b);
     return v < lo ? lo : v > hi ? hi : v;
@@ -285,7 +302,7 @@ __device__ float isect_terrain(float ox, float oy, float oz, float dx, float dy,
         const float px = ox * scale_r + dx * tc;
         const float py = oy * scale_r + dy * tc;
         const float pz = oz * scale_r + dz * tc;
-        const float h = sinf(px) * sinf(pz);
+        const float h = sin_j(px) * sin_j(pz);
         if (py < h) {
             t = tc - t_delta + t_delta * (lh - ly) / (py - ly - h + lh);
             tc = 10.0f;

@@ -88,15 +88,15 @@ __device__ Surf surface(const DevScene& S, const DevParams& P, float ox, float o
         const float n0x = s.px - c.x, n0y = s.py - c.y, n0z = s.pz - c.z;
         const float r = rsqrt_j(n0x * n0x + n0y * n0y + n0z * n0z);
         s.nx = n0x * r; s.ny = n0y * r; s.nz = n0z * r;
-        s.u = 0.5f + atan2f(-s.nz, -s.nx) * INV_TWO_PI;
-        s.v = 0.5f - asinf(-s.ny) * INV_PI;
+        s.u = 0.5f + atan2_j(-s.nz, -s.nx) * INV_TWO_PI;
+        s.v = 0.5f - asin_j(-s.ny) * INV_PI;
     } else if (h.shape_type == DFPT_SHAPE_TERRAIN) {
         const float sr = 1.0f / 10.0f;
         s.px = oxo * sr + dxo * t; s.py = oyo * sr + dyo * t; s.pz = ozo * sr + dzo * t;
         const float e = 0.02f;
-        const float nx = (sinf(s.px - e) * sinf(s.pz)) - (sinf(s.px + e) * sinf(s.pz));
+        const float nx = (sin_j(s.px - e) * sin_j(s.pz)) - (sin_j(s.px + e) * sin_j(s.pz));
         const float ny = 2.0f * e;
-        const float nz = (sinf(s.px) * sinf(s.pz - e)) - (sinf(s.px) * sinf(s.pz + e));
+        const float nz = (sin_j(s.px) * sin_j(s.pz - e)) - (sin_j(s.px) * sin_j(s.pz + e));
         const float r = rsqrt_j(nx * nx + ny * ny + nz * nz);
         s.nx = nx * r; s.ny = ny * r; s.nz = nz * r;
         s.u = s.px; s.v = s.pz;
@@ -373,7 +373,7 @@ __device__ bool sun_sample(const DevParams& P, float px, float py, float pz, flo
     const float cos_t = u * (cos_max - 1.0f) + 1.0f;
     const float sin_t = sqrtf(jmax(0.0f, 1.0f - cos_t * cos_t));
     const float phi = TWO_PI * v;
-    const float x = cosf(phi) * sin_t, y = sinf(phi) * sin_t, z = cos_t;
+    const float x = cos_j(phi) * sin_t, y = sin_j(phi) * sin_t, z = cos_t;
     const float wx = P.sun_dir_world[0], wy = P.sun_dir_world[1], wz = P.sun_dir_world[2];
     const float ax = fabsf(wx), ay = fabsf(wy), az = fabsf(wz);
     const float vx = ax < ay && ax < az ? 0.0f : ay < az ? wz : wy;
@@ -396,7 +396,7 @@ __device__ bool sun_sample(const DevParams& P, float px, float py, float pz, flo
 __device__ __forceinline__ void cosine_dir(float wx, float wy, float wz, float u, float v, float& ox, float& oy, float& oz) {
     const float phi = TWO_PI * u;
     const float ct = sqrtf(v), st = sqrtf(1.0f - v);
-    const float x = cosf(phi) * st, y = sinf(phi) * st, z = ct;
+    const float x = cos_j(phi) * st, y = sin_j(phi) * st, z = ct;
     const bool isY = fabsf(wx) > 0.1f;
     const float ux = (isY ? 1.0f : 0.0f) * wz;
     const float uy = -((isY ? 0.0f : 1.0f) * wz);
@@ -453,7 +453,7 @@ __device__ bool primary_ray(const DevScene& S, const DevParams& P, int pixel, bo
         const float r1 = rng.next(), r2 = rng.next();
         const float angle = TWO_PI * r1;
         const float dist = aperture * sqrtf(r2);
-        const float ax = cosf(angle) * dist, ay = sinf(angle) * dist;
+        const float ax = cos_j(angle) * dist, ay = sin_j(angle) * dist;
         apx = ex + ux * ax + vx * ay;
         apy = ey + uy * ax + vy * ay;
         apz = ez + uz * ax + vz * ay;
@@ -610,6 +610,16 @@ __device__ __forceinline__ uint32_t camera_draws(const DevScene& S, const DevPar
     return (pt ? 2u : 0u) + (__ldg(S.camera) > 0.00001f ? 2u : 0u);
 }
 
+// A pixel the fisheye lens rejects has no primary ray: its hit record says "no hit".
+__device__ __forceinline__ void record_rejected(const DevParams& P, DevPass& B, int pixel) {
+    if (!P.record_hits) return;
+    B.hit_prim_offset[pixel] = -1;
+    B.hit_shape_type[pixel] = -1;
+    B.hit_shape_offset[pixel] = -1;
+    B.hit_distance[pixel] = 0.0f;
+    B.hit_normal[3 * pixel] = 0.0f; B.hit_normal[3 * pixel + 1] = 0.0f; B.hit_normal[3 * pixel + 2] = 0.0f;
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q) {
     const int n = BATCH ? Q.capacity : B.n_pixels;
@@ -688,6 +698,7 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
             Rng rng = make_rng(P, (uint32_t)pixel, sample, (!BATCH && P.rng_kind == DFPT_RNG_LCG) ? B.rng[i] : 0ull);
             live = primary_ray(S, P, pixel, pt, rng, o, d);
             B.pixel_flags[i] = live ? 0 : 1;
+            if (!BATCH && !live) record_rejected(P, B, pixel);
             if (!lean_start<BATCH>(P)) {
                 B.rng[i] = rng.state;
                 B.throughput[PSI(i)] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
@@ -811,10 +822,10 @@ __device__ __forceinline__ Scatter scatter(const Surf& s, int material, float wx
     } else if (material == DFPT_MATERIAL_PHONG) {
         const float u = rng.next(), v = rng.next();
         const float phi = TWO_PI * u;
-        const float ct = powf(1.0f - v, 1.0f / (exponent + 1.0f));
+        const float ct = pow_j(1.0f - v, 1.0f / (exponent + 1.0f));
         out.phong_ct = ct;
         const float st = sqrtf(jmax(0.0f, 1.0f - ct * ct));
-        const float x = cosf(phi) * st, y = sinf(phi) * st, z = ct;
+        const float x = cos_j(phi) * st, y = sin_j(phi) * st, z = ct;
         const float rwr = rsqrt_j(rx * rx + ry * ry + rz * rz);
         const float rnx = rx * rwr, rny = ry * rwr, rnz = rz * rwr;
         const bool isY = fabsf(rnx) > 0.1f;
@@ -1228,7 +1239,7 @@ __device__ int phong0(const DevScene& S, const DevParams& P, bool test, float px
             const float rx = 2.0f * ldn * nx - lnx, ry = 2.0f * ldn * ny - lny, rz = 2.0f * ldn * nz - lnz;
             const float rr = rsqrt_j(rx * rx + ry * ry + rz * rz);
             const float rdv = rx * rr * vx + ry * rr * vy + rz * rr * vz;
-            const float sh = powf(jmax(rdv, 0.0f), 250.0f);
+            const float sh = pow_j(jmax(rdv, 0.0f), 250.0f);
             r += 0.5f * sh * 1.0f; g += 0.5f * sh * 1.0f; b += 0.5f * sh * 1.0f;
         }
     }
@@ -1264,6 +1275,7 @@ __global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __r
             float4 o4, d4;
             const bool live = primary_ray(S, P, i, false, rng, o4, d4);
             B.pixel_flags[i] = live ? 0 : 1;
+            if (!live) record_rejected(P, B, i);
             if (P.wireframes == 1) { B.primary_o[i] = o4; B.primary_d[i] = d4; }
             float cr_ = 0.0f, cg_ = 0.0f, cb_ = 0.0f;
             if (live) {
@@ -1326,7 +1338,7 @@ __global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __r
                             const float v0x = w1y * u2z - w1z * u2y, v0y = w1z * u2x - w1x * u2z, v0z = w1x * u2y - w1y * u2x;
                             const float xi = rng.next(), xj = rng.next();
                             const float phi = TWO_PI * xi;
-                            const float cp = cosf(phi), sp = sinf(phi), sth = sqrtf(xj), cth = sqrtf(1.0f - xj);
+                            const float cp = cos_j(phi), sp = sin_j(phi), sth = sqrtf(xj), cth = sqrtf(1.0f - xj);
                             const float e0x = cp * sth, e0y = sp * sth, e0z = cth;
                             const float e1x = e0x * u2x + e0y * v0x + e0z * w1x;
                             const float e1y = e0x * u2y + e0y * v0y + e0z * w1y;

@@ -207,11 +207,13 @@ def heightfield(n: int, size: float, height: float, seed: int, octaves: int = 6)
 SUN_45 = (0.5, 0.70710677, 0.5)  # elevation 45 degrees (azimuth 45)
 
 
-def sphere_scene(seed: int = 0, width: int = 512, height: int = 512):
+def sphere_scene(seed: int = 0, width: int = 512, height: int = 512, checker_colors=((0.5, 0.5, 0.5), (0.5, 0.5, 0.5))):
+    """`checker_colors`: the ground's two checkerboard colours; the default is the reference's
+    CheckerboardTexture() (GRAY and GRAY, CheckerboardTexture.java:109-110), parity tests pass two."""
     rng = np.random.default_rng(seed)
     b = sc.SceneBuilder()
     black = b.constant(0, 0, 0)
-    checker = b.checkerboard((0.5, 0.5, 0.5), (0.5, 0.5, 0.5), 0.0, 5.0, 5.0)
+    checker = b.checkerboard(checker_colors[0], checker_colors[1], 0.0, 5.0, 5.0)
     ground = b.surface(sc.LAMBERTIAN, checker, black, black)
     b.primitive(b.plane((0, 0, 0), (0, 0, 1), (1, 0, 0)), ground)
     sphere = b.sphere((0, 0, 0), 1.0)

@@ -5,7 +5,8 @@ Tolerances (written per test):
   path tracer, same RNG stream- film mean absolute difference < 1% of the mean radiance (the two
                                 sides trace the same paths; FP32 transcendentals may diverge a few);
   path tracer vs FP64 oracle  - relative RMSE <= 1% of the converged radiance and per-pixel
-                                z-scores against the oracle's sample variance.
+                                z-scores against the oracle's sample variance (tests/_parity.py);
+                                the bench configuration is checked in test_gpu_bench_parity.py.
 """
 import numpy as np
 import pytest
@@ -95,33 +96,30 @@ def test_pathtrace_same_stream(scenes, oracle_mod, name):
     k.dispose()
 
 
-def test_pathtrace_converged_rmse_and_zscores(scenes, oracle_mod):
-    scene, sky, params, (w, h) = scenes["spheres"]
+@pytest.mark.parametrize("name", ["spheres", "meshes"])
+def test_pathtrace_converged_rmse_and_zscores(scenes, oracle_mod, name):
+    """Fast kernels, one pass at a time: the film at 256 spp against an independent FP64 oracle
+    render at 1024 spp (converged relative RMSE <= 1% and z-scores, tests/_parity.py), and with
+    the oracle's own seed against its first 256 passes (same stream: relative RMSE <= 1%)."""
+    from _parity import assert_converged, film_stats, oracle_pair, same_stream_rel_rmse
+
+    scene, sky, params, (w, h) = scenes[name]
     spp = 256
     k = _kernel(scene, sky, params, w, h, strict=False)
+    k.set_tuning("wide_samples", 1)
     k.set_seed(12345)
     k.execute(spp)
     film, _ = k.film()
-    # Passes 0..spp-1 drew with seed 12345; the oracle renders the same passes with the default seed.
-    ref = oracle_mod.render(scene, sky, _params(params), w, h, passes=spp, precision=64, pass_begin=spp)
     a = film.reshape(-1).astype(np.float64)
-    b = ref["film"]
-    rel_rmse = np.sqrt(np.mean((a - b) ** 2)) / b.mean()
-    assert rel_rmse <= 0.05, rel_rmse  # independent streams: noise-limited at 256 spp
-    # Same seed and pass indices (spp..2spp-1) on both sides: the estimate itself within 1%.
-    k.set_seed(_params(params).seed)
-    k.clear()
+    same, full = oracle_pair(oracle_mod, scene, sky, params, w, h, spp, 4 * spp, seed=777)
+    assert_converged(film_stats(a, spp, full, 4 * spp))
+    k.dispose()
+    k = _kernel(scene, sky, params, w, h, strict=False)
+    k.set_tuning("wide_samples", 1)
+    k.set_seed(777)
     k.execute(spp)
     film2, _ = k.film()
-    a2 = film2.reshape(-1).astype(np.float64)
-    assert np.sqrt(np.mean((a2 - b) ** 2)) / b.mean() <= 0.01
-    # Per-pixel z-scores of the independent-stream GPU mean against the oracle's sample variance.
-    var = np.maximum(ref["sumsq"] / spp - (ref["sum"] / spp) ** 2, 0.0)
-    se = np.sqrt(2.0 * var / spp) + 1e-12
-    z = (a - b) / se
-    ok = var > 1e-10
-    assert np.mean(np.abs(z[ok]) > 4.0) < 0.01
-    assert abs(np.mean(z[ok])) < 0.2
+    assert same_stream_rel_rmse(film2, same["film"]) <= 0.01
     k.dispose()
 
 
