@@ -287,6 +287,7 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
                 float er = cr(emission), eg = cg(emission), eb = cb(emission);
                 const int material = f2i(__ldg(S.surfaces + so_off + 0));
                 float exponent = 50.0f;
+                if (S.prim_ext) primitive_extension(S, h.prim, er, eg, eb, exponent);
                 diff_surface(P, h.prim, ar, ag, ab, er, eg, eb, exponent);
                 // Emission.
                 Lu.x += T.x * er; Lu.y += T.y * eg; Lu.z += T.z * eb;

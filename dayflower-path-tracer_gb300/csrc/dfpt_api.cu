@@ -1073,7 +1073,7 @@ void SceneStore::release() {
     for (auto* b : fb) b->release();
     DevBuf<int>* ib[] = {&planes, &triangles, &primitives};
     for (auto* b : ib) b->release();
-    DevBuf<float4>* f4[] = {&trav, &pairs, &shade_tris, &sphere4, &plane_a, &plane_n, &cull_nodes, &prim_box};
+    DevBuf<float4>* f4[] = {&trav, &pairs, &shade_tris, &sphere4, &plane_a, &plane_n, &prim_ext, &cull_nodes, &prim_box};
     for (auto* b : f4) b->release();
     prim_info.release();
     cull_prims.release();
@@ -1103,6 +1103,20 @@ int scene_load(const dfpt_scene_desc* sd, SceneStore& st) {
     s.w2o.assign(sd->primitives_world_to_object, sd->primitives_world_to_object + np * 16);
     if (s.o2w.empty()) { s.o2w.assign(16, 0.0f); s.w2o.assign(16, 0.0f); }
     s.camera.assign(sd->camera, sd->camera + 19);
+    s.prim_ext.clear();
+    if (sd->primitive_extensions_count != 0 || sd->primitive_extensions) {
+        if (!sd->primitive_extensions || sd->primitive_extensions_count != np * 4)
+            return dfpt_fail(DFPT_ERR_INVALID_SCENE, "primitive extensions need 4 floats per primitive (%lld given for %lld primitives)",
+                             (long long)sd->primitive_extensions_count, (long long)np);
+        for (int64_t i = 0; i < np; ++i) {
+            const float* x = sd->primitive_extensions + 4 * i;
+            if (!(x[0] >= 0.0f && x[0] <= 1.0e6f) || !std::isfinite(x[1]) || !std::isfinite(x[2]) || !std::isfinite(x[3]) ||
+                x[1] < 0.0f || x[2] < 0.0f || x[3] < 0.0f)
+                return dfpt_fail(DFPT_ERR_INVALID_SCENE, "primitive %lld: bad extension record {%g, %g, %g, %g}", (long long)i, x[0],
+                                 x[1], x[2], x[3]);
+            s.prim_ext.push_back(make_float4(x[0], x[1], x[2], x[3]));
+        }
+    }
     Derived& d = st.derived;
     int r = build_derived(s, d);
     if (r) return r;
@@ -1207,6 +1221,8 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     CUDA_TRY(upload(st.sphere4, d.sphere4, s));
     CUDA_TRY(upload(st.plane_a, d.plane_a, s));
     CUDA_TRY(upload(st.plane_n, d.plane_n, s));
+    st.prim_ext.release();
+    if (!h.prim_ext.empty()) CUDA_TRY(upload(st.prim_ext, h.prim_ext, s));
     int rc = culling_upload(st, d, s);
     if (rc) return rc;
     CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors below are freed
@@ -1219,6 +1235,7 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
     S.pairs = st.pairs.p;
     S.shade_tris = st.shade_tris.p;
     S.plane_a = st.plane_a.p; S.plane_n = st.plane_n.p;
+    S.prim_ext = h.prim_ext.empty() ? nullptr : st.prim_ext.p;
     st.derived = Derived();
     return DFPT_OK;
 }

@@ -39,6 +39,7 @@ struct DevScene {
                                // {uvb.y, uvc.xy, na.x}, {na.yz, nb.xy}, {nb.z, nc.xyz}, {tga.xyz, tgb.x},
                                // {tgb.yz, tgc.xy}, {tgc.z, 0, 0, 0}; null when some triangle offset is not a
                                // multiple of 12 (surface() then follows the reference's indices)
+    const float4* prim_ext; // per primitive {Phong exponent, emission scale r, g, b}; null when absent
     const float4* sphere4;  // {position.xyz, radius} per sphere record
     const float4* plane_a;  // point A per plane record
     const float4* plane_n;  // surface normal per plane record

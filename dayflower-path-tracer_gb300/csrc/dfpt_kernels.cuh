@@ -760,6 +760,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S0, const DevPar
     }
 }
 
+// A primitive's extension record (scenes that carry them): its Phong exponent, and a scale on its
+// emission texture's 8-bit colour (HDR emitters).
+__device__ __forceinline__ void primitive_extension(const DevScene& S, int prim, float& er, float& eg, float& eb, float& exponent) {
+    const float4 x = __ldg(S.prim_ext + prim);
+    exponent = x.x;
+    er *= x.y; eg *= x.z; eb *= x.w;
+}
+
 // Differentiable mode: the primitive's parameters applied to its texture colors.
 __device__ __forceinline__ void diff_surface(const DevParams& P, int prim, float& ar, float& ag, float& ab, float& er, float& eg,
                                              float& eb, float& exponent) {
@@ -1055,6 +1063,7 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
                 float er = cr(emission), eg = cg(emission), eb = cb(emission);
                 const int material = f2i(__ldg(S.surfaces + so_off + 0));
                 float exponent = 50.0f;  // the reference's fixed Phong exponent (GRK:3524)
+                if (S.prim_ext) primitive_extension(S, h.prim, er, eg, eb, exponent);
                 if (P.diff) diff_surface(P, h.prim, ar, ag, ab, er, eg, eb, exponent);
                 if ((material == DFPT_MATERIAL_CLEAR_COAT || material == DFPT_MATERIAL_LAMBERTIAN || material == DFPT_MATERIAL_PHONG) &&
                     P.sun_active == 1) {

@@ -1097,6 +1097,7 @@ int dfpt_compiled_describe(const dfpt_compiled* c, dfpt_scene_desc* d) {
     d->primitives_object_to_world = c->o2w.data(); d->primitives_object_to_world_count = (int64_t)c->o2w.size();
     d->primitives_world_to_object = c->w2o.data(); d->primitives_world_to_object_count = (int64_t)c->w2o.size();
     d->camera = c->camera.data(); d->camera_count = (int64_t)c->camera.size();
+    d->primitive_extensions = nullptr; d->primitive_extensions_count = 0;  // not among the compiled arrays
     return DFPT_OK;
 }
 

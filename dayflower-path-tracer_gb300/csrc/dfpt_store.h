@@ -51,6 +51,7 @@ cudaError_t upload(DevBuf<T>& b, const std::vector<T>& v, cudaStream_t s) {
 struct HostScene {
     std::vector<float> point2fs, point3fs, vector3fs, spheres, terrains, textures, surfaces, o2w, w2o, camera;
     std::vector<int> planes, triangles, bvh, primitives;
+    std::vector<float4> prim_ext;  // optional extension records, one per primitive (empty: none)
 };
 
 // Traversal records derived from the arrays at upload (16-byte aligned, see build_derived).
@@ -75,7 +76,7 @@ struct SceneStore {
     DevBuf<float4> pairs;  // per node: the children's boxes (pair records, see DevScene::pairs)
     DevBuf<float4> shade_tris;  // per triangle: the vertex values shading reads (see DevScene::shade_tris)
     size_t trav_nodes = 0;  // float4 records of nodes at the start of trav
-    DevBuf<float4> sphere4, plane_a, plane_n;
+    DevBuf<float4> sphere4, plane_a, plane_n, prim_ext;
     DevBuf<float4> cull_nodes, prim_box;
     DevBuf<int> cull_prims, always;
     std::vector<float> obj_box;      // object-space bound per primitive (culling rebuilds)

@@ -44,6 +44,7 @@ class SceneDesc(C.Structure):
         ("primitives_object_to_world", f32p), ("primitives_object_to_world_count", C.c_int64),
         ("primitives_world_to_object", f32p), ("primitives_world_to_object_count", C.c_int64),
         ("camera", f32p), ("camera_count", C.c_int64),
+        ("primitive_extensions", f32p), ("primitive_extensions_count", C.c_int64),
     ]
 
 

@@ -60,12 +60,16 @@ class CompiledScene:
     primitives_object_to_world: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     primitives_world_to_object: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     camera: np.ndarray = field(default_factory=lambda: np.zeros(19, np.float32))
+    # Optional per-primitive extension records {Phong exponent, emission scale r, g, b} (empty: none;
+    # see dfpt_scene_desc.primitive_extensions). Not part of the reference's arrays or .scene file.
+    primitive_extensions: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
 
     def __post_init__(self):
         for k in FLOAT_ARRAYS:
             setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.float32))
         for k in INT_ARRAYS:
             setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.int32))
+        self.primitive_extensions = np.ascontiguousarray(self.primitive_extensions, dtype=np.float32).reshape(-1)
 
     @property
     def primitive_count(self) -> int:
@@ -79,21 +83,26 @@ class CompiledScene:
             setattr(d, k if k != "bounding_volume_hierarchies" else "bounding_volume_hierarchies",
                     ptr(a, C.c_float if k in FLOAT_ARRAYS else C.c_int32))
             setattr(d, k + "_count", int(a.size))
+        if self.primitive_extensions.size:
+            d.primitive_extensions = ptr(self.primitive_extensions, C.c_float)
+            d.primitive_extensions_count = int(self.primitive_extensions.size)
         return d
 
     def arrays(self) -> dict:
         return {k: getattr(self, k) for k in FLOAT_ARRAYS + INT_ARRAYS}
 
     def copy(self) -> "CompiledScene":
-        return CompiledScene(self.name, **{k: v.copy() for k, v in self.arrays().items()})
+        return CompiledScene(self.name, **{k: v.copy() for k, v in self.arrays().items()},
+                             primitive_extensions=self.primitive_extensions.copy())
 
     def save_npz(self, path) -> None:
-        np.savez_compressed(path, name=np.array(self.name), **self.arrays())
+        np.savez_compressed(path, name=np.array(self.name), primitive_extensions=self.primitive_extensions, **self.arrays())
 
     @staticmethod
     def load_npz(path) -> "CompiledScene":
         z = np.load(path, allow_pickle=False)
-        return CompiledScene(str(z["name"]), **{k: z[k] for k in FLOAT_ARRAYS + INT_ARRAYS})
+        ext = z["primitive_extensions"] if "primitive_extensions" in z.files else np.zeros(0, np.float32)
+        return CompiledScene(str(z["name"]), **{k: z[k] for k in FLOAT_ARRAYS + INT_ARRAYS}, primitive_extensions=ext)
 
     # -- the reference's .scene file ---------------------------------------------------------
     def write(self, path) -> None:
@@ -189,6 +198,7 @@ class SceneBuilder:
         h = C.c_void_p()
         check(self._lib.dfpt_builder_create(C.byref(h)))
         self._h = h
+        self._ext = []  # per primitive: (Phong exponent, emission scale r, g, b)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -278,9 +288,18 @@ class SceneBuilder:
         return check(self._lib.dfpt_builder_add_mesh(self._h, ptr(v, C.c_float), nv, ptr(idx, C.c_int32), len(idx),
                                                     1 if as_mesh else 0))
 
-    def primitive(self, shape, surface, position=(0, 0, 0), rotation=(0, 0, 0, 1), scale=(1, 1, 1)) -> int:
+    def primitive(self, shape, surface, position=(0, 0, 0), rotation=(0, 0, 0, 1), scale=(1, 1, 1),
+                  phong_exponent=None, emission_scale=None) -> int:
+        """A primitive (Primitive: shape, surface, Transform). `phong_exponent` (the exponent a
+        PhongMaterial holds, which SceneCompiler drops) and `emission_scale` (a factor on the
+        emission texture's 8-bit colour, for HDR emitters) go into the scene's extension records;
+        without them the primitive renders as the reference's (exponent 50, scale 1)."""
         t = np.asarray(list(position) + list(rotation) + list(scale), dtype=np.float32)
-        return check(self._lib.dfpt_builder_add_primitive(self._h, shape, surface, ptr(t, C.c_float)))
+        idx = check(self._lib.dfpt_builder_add_primitive(self._h, shape, surface, ptr(t, C.c_float)))
+        es = (1.0, 1.0, 1.0) if emission_scale is None else tuple(float(v) for v in np.broadcast_to(emission_scale, (3,)))
+        rec = (50.0 if phong_exponent is None else float(phong_exponent),) + es
+        self._ext.append((rec, phong_exponent is not None or emission_scale is not None))
+        return idx
 
     def camera(self, eye, look_at, field_of_view_x=90.0, resolution=(800, 800), aperture_radius=0.0,
                focal_distance=30.0, fisheye=False) -> None:
@@ -305,6 +324,9 @@ class SceneBuilder:
                 p = getattr(d, k)
                 dtype = np.float32 if k in FLOAT_ARRAYS else np.int32
                 arrays[k] = np.ctypeslib.as_array(p, shape=(n,)).astype(dtype, copy=True) if n else np.zeros(0, dtype)
-            return CompiledScene(name, **arrays)
+            # The compiler keeps the primitives in the order they were added.
+            ext = np.asarray([r for r, _ in self._ext], np.float32).reshape(-1) if any(u for _, u in self._ext) \
+                else np.zeros(0, np.float32)
+            return CompiledScene(name, **arrays, primitive_extensions=ext)
         finally:
             self._lib.dfpt_compiled_destroy(out)

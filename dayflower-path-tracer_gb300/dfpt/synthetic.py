@@ -4,10 +4,12 @@ The reference publishes no benchmark scenes, so each workload is generated from 
   sphere_scene      - ground plane (checkerboard, Lambertian) + 3 unit spheres (Lambertian, Glass,
                       ClearCoat), Perez sky T=2, sun at 45 degrees; 512x512, depth 5, RR 3, Reinhard.
   mesh_scene        - an fBm-displaced geodesic icosphere (frequency 100: 200,000 triangles) in four
-                      Lambertian/Phong regions over a 512x512 fBm heightfield (522,242 triangles);
-                      1920x1080, depth 8, ACES.
+                      Lambertian/Phong regions (Phong exponent U(10,200) per region, extension
+                      records) over a 512x512 fBm heightfield (522,242 triangles); 1920x1080,
+                      depth 8, ACES.
   instances_scene   - 40 displaced icospheres of 50,000 triangles each (2M), scale U(0.5,3) in a
-                      100^3 box, Glass/Reflection/Lambertian, 500 emissive triangles.
+                      100^3 box, Glass/Reflection/Lambertian, 500 emissive triangle primitives with
+                      emission U(1,20) (extension records).
   spheres_on_plane  - 256 spheres on a plane under a Perez sky (the inverse-rendering scene).
   batch_workload    - 64 scenes (displaced icosphere on a plane) with log-uniform triangle counts in
                       [1k, 500k], resolutions {256^2, 512^2, 1024^2}, spp {16, 64, 256}.
@@ -236,13 +238,16 @@ def mesh_scene(seed: int = 1, width: int = 1920, height: int = 1080, frequency: 
     pos, idx, region, nrm, uv = displaced_icosphere(frequency, 0.1, seed, radius=3.0)
     pos = pos + np.array([0.0, 4.0, 0.0])
     tng = tangents_for(nrm)
-    # Four regions by base face id: Lambertian and Phong alternate.
+    # Four regions by base face id: Lambertian and Phong alternate; each Phong region has its own
+    # exponent U(10, 200) (an extension record: the reference's compiler drops the exponent).
     quadrant = region % 4
+    rng_x = np.random.default_rng(seed + 7919)
     for q in range(4):
         sel = idx[quadrant == q]
         mat = sc.LAMBERTIAN if q % 2 == 0 else sc.PHONG
         surf = b.surface(mat, b.constant(*rng.uniform(0.3, 0.9, 3)), black, black)
-        b.primitive(b.mesh(pos, sel, nrm, uv, tng), surf)
+        b.primitive(b.mesh(pos, sel, nrm, uv, tng), surf,
+                    phong_exponent=float(rng_x.uniform(10.0, 200.0)) if mat == sc.PHONG else None)
     hp, hi, hn, huv = heightfield(grid, 60.0, 2.0, seed)
     b.primitive(b.mesh(hp, hi, hn, huv, tangents_for(hn)), b.surface(sc.LAMBERTIAN, b.constant(0.55, 0.5, 0.45), black, black))
     b.camera((0, 6, 14), (0, 3.5, 0), 70.0, (width, height))
@@ -287,7 +292,8 @@ def instances_scene(seed: int = 2, width: int = 1920, height: int = 1080, freque
         mat = mats[k % 3]
         surf = b.surface(mat, b.constant(*rng.uniform(0.3, 0.95, 3)), black, black)
         b.primitive(b.mesh(pos * s + c, idx, nrm, uv, tangents_for(nrm)), surf)
-    # Emissive triangles (emission clamped to the reference's 8-bit range).
+    # Area lights: `lights` triangle primitives with a white emission texture scaled by U(1, 20) each
+    # (an extension record: the reference packs emission into 8 bits clamped to 1).
     lp = rng.uniform(0.0, 100.0, (lights, 3))
     tris = []
     for k in range(lights):
@@ -296,8 +302,13 @@ def instances_scene(seed: int = 2, width: int = 1920, height: int = 1080, freque
     tris = np.asarray(tris).reshape(-1, 3)
     tidx = np.arange(len(tris), dtype=np.int32).reshape(-1, 3)
     n = vertex_normals(tris, tidx)
+    tg = tangents_for(n)
     emit = b.surface(sc.LAMBERTIAN, b.constant(1, 1, 1), b.constant(1, 1, 1), black)
-    b.primitive(b.mesh(tris, tidx, n, np.zeros((len(tris), 2)), tangents_for(n)), emit)
+    scale = np.random.default_rng(seed + 104729).uniform(1.0, 20.0, lights)
+    zero_uv = np.zeros((3, 2))
+    for k in range(lights):
+        v = slice(3 * k, 3 * k + 3)
+        b.primitive(b.mesh(tris[v], [[0, 1, 2]], n[v], zero_uv, tg[v], as_mesh=False), emit, emission_scale=float(scale[k]))
     b.camera((50, 50, -60), (50, 50, 50), 70.0, (width, height))
     params = dict(renderer_type=2, pt_ray_depth_maximum=5, pt_ray_depth_russian_roulette=3, tone_mapper_type=1,
                   tone_mapper_exposure=1.0)

@@ -68,6 +68,15 @@ typedef struct dfpt_scene_desc {
     const float* primitives_object_to_world;  int64_t primitives_object_to_world_count;
     const float* primitives_world_to_object;  int64_t primitives_world_to_object_count;
     const float* camera;                      int64_t camera_count; /* 19 floats, Camera.java:87-222 */
+    /* Optional per-primitive extension records: 4 floats per primitive {Phong exponent, emission
+     * scale r, g, b}; NULL and 0 when absent (a zero-initialised descriptor has none). They have no
+     * counterpart in the compiled arrays: PhongMaterial's exponent is dropped by the compiler
+     * (PhongMaterial.java:39-58, SceneCompiler.java:760-768; the kernel uses 50, GRK:3524) and
+     * colours are packed to 8 bits clamped to [0, 1] (ConstantTexture.java:150-155). The path tracer
+     * (and its adjoint) uses a primitive's exponent for its Phong lobe and multiplies its emission
+     * texture's colour by the scale (HDR emitters). Absent: exponent 50, scale 1. Exponents must be
+     * finite and in [0, 1e6], scales finite and >= 0. */
+    const float* primitive_extensions;        int64_t primitive_extensions_count;
 } dfpt_scene_desc;
 
 /* Sun and sky state: the scalars and arrays GPURendererKernel copies from Sky

@@ -824,6 +824,13 @@ template <typename R> struct Kernel {
             const R tR = aR, tG = aG, tB = aB;
             R exponent = (R)50;
             const int prim = po / 3;
+            if (S.d->primitive_extensions) {
+                // Per-primitive extension record {Phong exponent, emission scale r, g, b} (the
+                // exponent PhongMaterial holds and SceneCompiler.java:760-768 drops; HDR emission).
+                const float* x = S.d->primitive_extensions + 4 * (size_t)prim;
+                exponent = (R)x[0];
+                eR *= (R)x[1]; eG *= (R)x[2]; eB *= (R)x[3];
+            }
             if (diff) {
                 aR *= (R)diff->albedo[3 * prim]; aG *= (R)diff->albedo[3 * prim + 1]; aB *= (R)diff->albedo[3 * prim + 2];
                 eR += (R)diff->emission[3 * prim]; eG += (R)diff->emission[3 * prim + 1]; eB += (R)diff->emission[3 * prim + 2];
@@ -1509,6 +1516,7 @@ int oracle_render(const dfpt_scene_desc* scene, const dfpt_sky* sky, const dfpt_
                   double* sum, double* sumsq, int* primitive_offsets, uint8_t* bgra, int* hit_prim, int* hit_type,
                   int* hit_off, double* hit_dist, double* hit_normal, uint64_t* rng_state, uint64_t* counters) {
     if (!scene || !sky || !params || !film || width <= 0 || height <= 0 || passes < 1) return -1;
+    if (scene->primitive_extensions && scene->primitive_extensions_count != scene->primitives_count / 3 * 4) return -2;
     if (row_begin < 0) row_begin = 0;
     if (row_end > height || row_end <= 0) row_end = height;
     Scene S{scene, sky, params, width, height};
@@ -1613,6 +1621,7 @@ int oracle_diff(const dfpt_scene_desc* scene, const dfpt_sky* sky, const dfpt_pa
                 const double* sun3, const double* dldi, double* image, double* grad) {
     if (!scene || !sky || !params || !albedo || !emission || !exponent || !sun3 || !dldi || !image || !grad) return -1;
     if (width <= 0 || height <= 0 || passes < 1 || params->rng_kind != DFPT_RNG_COUNTER) return -1;
+    if (scene->primitive_extensions && scene->primitive_extensions_count != scene->primitives_count / 3 * 4) return -2;
     Scene S{scene, sky, params, width, height};
     const DiffIn din{albedo, emission, exponent};
     const SunDual sd = sky_set_dual(turbidity, sun3);

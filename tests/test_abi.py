@@ -99,3 +99,18 @@ def test_noalloc_rejects_bad_sizes_without_device(lib):
     assert lib.dfpt_film_mean_noalloc(C.cast(rgb, C.c_void_p), 0, C.cast(out, C.c_void_p), None) == -1
     assert lib.dfpt_film_mean_noalloc(C.cast(rgb, C.c_void_p), (1 << 28) + 1, C.cast(out, C.c_void_p), None) == -1
     assert lib.dfpt_film_mean_noalloc(None, 10, C.cast(out, C.c_void_p), None) == -1
+
+
+@pytest.mark.parametrize("ext", [
+    np.zeros(5, np.float32),                                                 # not 4 per primitive
+    np.tile(np.asarray([-1.0, 1, 1, 1], np.float32), 4),                     # negative exponent
+    np.tile(np.asarray([50.0, np.nan, 1, 1], np.float32), 4),                # NaN emission scale
+    np.tile(np.asarray([50.0, 1, -2, 1], np.float32), 4),                    # negative emission scale
+])
+def test_bad_primitive_extensions_rejected(lib, ext):
+    scene, sky, _, _ = _scene()
+    s = scene.copy()
+    assert s.primitive_count == 4
+    s.primitive_extensions = ext
+    assert _create(lib, s, sky) == -4
+    assert b"extension" in lib.dfpt_last_error()
