@@ -14,19 +14,25 @@ depth 8, ACES; seeded synthetic data (the reference publishes no scenes).
           stream, L2 flushed between steps with a 256 MiB write);
   e2e   : the same metric through the C-ABI as the reference's render loop uses it
           (dfpt_set_camera from host memory, dfpt_render, dfpt_read_bgra8 into host memory);
+  frame_loop : the interactive loop of DayflowerApplication (one pass per dfpt_render call, the
+          image read back every frame), M samples/s on the host clock;
   roofline : the dominant kernel (closest-hit traversal), algorithmic bytes per closest-hit
           segment = nodes*32 + triangles*48 + 64 with the mean visit counts of closest-hit
           segments from the GPU's own counters over a step (the CPU restatement's counts on its
-          sample reported beside them), against MEASURED_PEAKS.json's HBM copy rate;
+          sample reported beside them), against the L2-resident read bandwidth measured in the
+          same run (the records live in L2); the HBM copy rate of MEASURED_PEAKS.json and the
+          DRAM traffic of one ncu capture are reported beside it;
   cpu_baseline : the oracle's strict-FP32 restatement of the reference kernel on all host cores,
           over a bounded band of rows (the reference's Java thread-pool path needs a JVM).
---impl reference times that CPU restatement alone on the same workload and metric.
+--impl reference times that CPU restatement alone on the same workload, config and metric; it
+reads the workload file that build() wrote (dfpt.workloads), so its process maps only the oracle.
 Multi-GPU: pixels are independent, so N ranks render N replicas (weak scaling, no collective on
 the data path); value sums the ranks' samples over the slowest rank's time.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import math
 import json
 import os
@@ -72,22 +78,34 @@ def parse():
 
 
 def build_workload(name, width, height):
-    from dfpt import synthetic
+    """(scene, sky, params struct, (w, h), meta, source) from the workload file `build()` wrote
+    (read with numpy alone: the process maps no GPU library for it), else generated here."""
+    from dfpt import workloads
 
-    if name == "mesh_scene":
-        return synthetic.mesh_scene(width=width, height=height)
-    if name == "sphere_scene":
-        return synthetic.sphere_scene(0, width, height)
-    return synthetic.instances_scene(width=width, height=height)
+    path = workloads.cache_path(name, width, height)
+    source = "workload file"
+    if not path.exists():
+        path = workloads.prepare(name, width, height)  # generator + libdfpt's scene compiler
+        source = "generated in this process"
+    scene, sky, params, size, meta = workloads.load(path)
+    return scene, sky, params, size, meta, source
 
 
-def params_struct(d):
-    from dfpt.kernel import default_params
+TONE_MAPPERS = {1: "ACES (modified filmic)", 2: "Reinhard", 3: "Reinhard modified 1", 4: "Reinhard modified 2"}
+EXTENSIONS = {
+    "mesh_scene": "Phong regions with exponents U(10,200) (extension records)",
+    "instances_scene": "500 area-light triangle primitives, emission U(1,20) (extension records)",
+    "sphere_scene": "none",
+}
 
-    p = default_params()
-    for k, v in d.items():
-        setattr(p, k, v)
-    return p
+
+def workload_config(name, w, h, scene, params, world=1):
+    """The workload as both arms name it (same keys and values on the GPU and CPU reference arms)."""
+    return {"workload": f"{name} {w}x{h}", "triangles": int(scene.triangles.size // 12),
+            "primitives": int(scene.primitive_count), "depth_max": int(params.pt_ray_depth_maximum),
+            "russian_roulette_from": int(params.pt_ray_depth_russian_roulette),
+            "tone_mapper": TONE_MAPPERS.get(int(params.tone_mapper_type), str(params.tone_mapper_type)),
+            "extensions": EXTENSIONS.get(name, "none"), "spp_per_pass": 1, "parallelism": f"replicas x{world}"}
 
 
 class ClockSampler:
@@ -137,11 +155,10 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def cpu_baseline(scene, sky, params, width, height, seconds, threads=0):
+def cpu_baseline(scene, sky, p, width, height, seconds, threads=0):
     """Times the oracle's strict-FP32 restatement on a band of rows sized to ~`seconds`."""
     from oracle import oracle
 
-    p = params_struct(params)
     threads = threads or os.cpu_count() or 1
     rows = max(1, threads // 2)
     t0 = time.perf_counter()
@@ -182,10 +199,9 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    scene, sky, params, (w, h) = build_workload(args.workload, args.width, args.height)
+    scene, sky, p, (w, h), meta, source = build_workload(args.workload, args.width, args.height)
     from oracle import oracle
 
-    p = params_struct(params)
     threads = os.cpu_count() or 1
     # Each step renders a band of rows sized so the whole run stays within a few minutes.
     band = max(1, threads // 2)
@@ -204,15 +220,20 @@ def run_reference(args):
         total += time.perf_counter() - t0
         samples += band * w
     value = samples / total / 1e6
+    with open("/proc/self/maps") as f:
+        maps = f.read()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": f"{args.workload} {w}x{h}", "passes_per_step": 1, "rows_per_step": band},
+        "config": workload_config(args.workload, w, h, scene, p, args.gpus),
+        "step": {"rows": band, "passes": 1, "samples": band * w},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{band} rows x {w} px per step, strict FP32 restatement of GPURendererKernel.run "
-                                   "(the reference's Java thread-pool path is unavailable: no JVM)"},
+                         "sample": f"{band} rows x {w} px x 1 pass per step, strict FP32 restatement of "
+                                   "GPURendererKernel.run on all host threads (the reference's Java thread-pool "
+                                   "path is unavailable: no JVM)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "workload_source": source, "gpu_library_mapped": "libdfpt" in maps,
     }
     print(json.dumps(line), flush=True)
 
@@ -426,6 +447,52 @@ def adjoint_leg(args, torch, barrier, dist, world):
     }
 
 
+def l2_read_peak(torch, stream):
+    """The L2-resident read roof: dfpt_probe_read_bandwidth over buffers of 24-64 MiB (smaller than
+    L2), the best of three runs per size, on the bench's stream."""
+    from dfpt import _lib as dlib
+
+    lib = dlib.load()
+    best, per_size = 0.0, {}
+    for mib in (24, 48, 64):
+        buf = torch.ones(mib * (1 << 20) // 4, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        g = C.c_double()
+        runs = []
+        for _ in range(3):
+            dlib.check(lib.dfpt_probe_read_bandwidth(C.c_void_p(buf.data_ptr()), buf.numel() * 4, 200,
+                                                     C.c_void_p(stream.cuda_stream), C.byref(g)))
+            runs.append(g.value)
+        per_size[str(mib)] = round(max(runs), 1)
+        best = max(best, max(runs))
+        del buf
+    return best, per_size
+
+
+def frame_loop(k, cam, host_img, frames, warmup, barrier):
+    """The reference's interactive render loop (DayflowerApplication.java:853-855): per frame
+    dfpt_set_camera from host memory, dfpt_render of ONE pass (1 spp) and dfpt_read_bgra8 into host
+    memory. Host clock around `frames` frames; M samples/s of the whole image."""
+    for _ in range(warmup):
+        k.update_camera(cam)
+        k.execute(1)
+        k.get(host_img)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        k.update_camera(cam)
+        k.execute(1)
+        k.get(host_img)
+    barrier()
+    return time.perf_counter() - t0
+
+
+# ncu figures of the closest-hit traversal kernel on mesh_scene (960x540, 4-pass waves, pixel-major
+# slots, configuration 16; one --set full capture): active lanes per issued instruction at bounces
+# 0 and 1, and the fraction of cycles with an instruction issued.
+TRACE_NCU = {"lanes_per_instruction": {"bounce0": 16.1, "bounce1": 9.1}, "issue_active": [0.64, 0.73]}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -451,13 +518,15 @@ def main():
 
     from dfpt.kernel import RendererKernel
     from dfpt import _lib as dlib
+    from dfpt import workloads
 
     def l2_reset():
         # Persisting L2 lines survive a plain flush: return them to normal too.
         dlib.check(dlib.load().dfpt_l2_reset())
 
     t_build = time.perf_counter()
-    scene, sky, params, (w, h) = build_workload(args.workload, args.width, args.height)
+    scene, sky, pstruct, (w, h), meta, source = build_workload(args.workload, args.width, args.height)
+    params = workloads.params_to_dict(pstruct)
     t_build = time.perf_counter() - t_build
     k = RendererKernel(scene, sky, params)
     k.update(w, h)
@@ -556,8 +625,6 @@ def main():
 
     # End to end through the C-ABI with host buffers (camera in, BGRA8 out), the render loop of
     # DayflowerApplication.java:832-877.
-    import ctypes as C
-
     cam = torch.from_numpy(np.ascontiguousarray(scene.camera.copy())).pin_memory().numpy()
     host_img = torch.empty(n_pix * 4, dtype=torch.uint8).pin_memory().numpy()  # pinned host buffers
     # Untimed warm-up steps: the counting step above changed the pass graphs, which are rebuilt here.
@@ -573,14 +640,19 @@ def main():
         k.get(host_img)
     barrier()
     e2e_s = time.perf_counter() - t0
+    # The interactive loop: one pass per call, as many frames as one step has passes.
+    fl_s = frame_loop(k, cam, host_img, S, max(3, args.warmup), barrier)
     if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
+        t = torch.tensor([e2e_s, fl_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s, fl_s = (float(v) for v in t.tolist())
     e2e_value = world * n_pix * S * args.steps / e2e_s / 1e6
+    fl_value = world * n_pix * S / fl_s / 1e6
     # The main handle's waves (up to 64 passes of 1080p with every bounce's shadow rays queued)
     # hold most of the device memory: release it before the other legs create their handles.
     k.dispose()
+    del flush
+    l2_peak, l2_sizes = l2_read_peak(torch, stream)
 
     batched = None
     if not args.no_batch:
@@ -596,14 +668,14 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline:
-        cpu = cpu_baseline(scene, sky, params, w, h, args.cpu_seconds)
+        cpu = cpu_baseline(scene, sky, pstruct, w, h, args.cpu_seconds)
 
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
         peaks = json.loads(pk.read_text())
     hbm = peaks.get("hbm_gbs")
-    peak_note = "measured" if hbm else "fallback"
+    hbm_note = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
     closest_segments = cnt[0]
     # Visits per closest-hit segment, the timed kernel's work: the GPU's own counters over a step.
@@ -619,46 +691,56 @@ def main():
     avg_trace_ms = trace_ms / max(trace_n, 1)
     trace_ms_per_step = trace_ms / args.steps
     launches_per_step = max(trace_n / args.steps, 1)
-    bytes_per_launch = closest_segments / launches_per_step * bytes_per_seg
     achieved = closest_segments * bytes_per_seg / (trace_ms_per_step / 1e3) / 1e9
     # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum per closest-hit
-    # segment of the mesh_scene traversal at 960x540 (one ncu capture),
-    # scaled by this run's segments per launch (the traffic grows with the rays of a launch).
+    # segment of the mesh_scene traversal at 960x540 (one ncu capture), scaled by this run's
+    # segments per launch (the traffic grows with the rays of a launch).
     traffic = None
     if args.workload == "mesh_scene" and TRACE_DRAM_BYTES_PER_SEGMENT:
         traffic = TRACE_DRAM_BYTES_PER_SEGMENT * closest_segments / launches_per_step
+    dram_gbs = traffic / (avg_trace_ms / 1e3) / 1e9 if traffic else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": f"{args.workload} {w}x{h}", "triangles": int(len(scene.triangles) // 12),
-                   "depth_max": params["pt_ray_depth_maximum"], "passes_per_step": S, "spp_total": S * args.steps,
-                   "wide_samples": wide["best"], "wide_ms_per_step": wide["ms_per_step"],
+        "config": workload_config(args.workload, w, h, scene, pstruct, world),
+        "step": {"passes": S, "spp_total": S * args.steps, "samples": n_pix * S,
+                 "l2": "flushed between steps (256 MiB write)"},
+        "tuning": {"wide_samples": wide["best"], "wide_ms_per_step": wide["ms_per_step"],
                    "ray_sort": wide.get("ray_sort"), "sort_ms_per_step": wide.get("sort_ms_per_step"),
                    "shadow_defer": wide.get("shadow_defer"), "defer_ms_per_step": wide.get("defer_ms_per_step"),
-                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                   "scene_build_s": round(t_build, 1), "trace_config": tuning["best"],
-                   "primitive_culling": tuning.get("primitive_culling", 0),
+                   "trace_config": tuning["best"], "primitive_culling": tuning.get("primitive_culling", 0),
                    "l2_persist": tuning.get("l2_persist", 0),
                    "l2_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("l2_ms_per_pass", {}).items()},
                    "culling_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("culling_ms_per_pass", {}).items()},
                    "trace_config_ms": {str(kk): round(v, 3) for kk, v in tuning["ms_per_pass"].items()},
                    "set_tuning": args.set_tuning},
+        "workload_source": source, "scene_build_s": round(t_build, 1),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4,
                 "loop": "dfpt_set_camera(pinned host) + dfpt_render(S passes) + dfpt_read_bgra8(pinned host) per step"},
+        "frame_loop": {"value": fl_value, "unit": UNIT, "frames": S, "ms_per_frame": fl_s / S * 1e3,
+                       "fraction_of_value": fl_value / value,
+                       "loop": "per frame: dfpt_set_camera(pinned host) + dfpt_render(1 pass) + dfpt_read_bgra8(pinned host), "
+                               "as DayflowerApplication's execute/get loop"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_source": peak_note,
+        "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak, "unit": "GB/s", "frac": achieved / l2_peak,
+                     "traffic": traffic,
+                     "peak_source": "measured in this run: L2-resident 16-byte ld.global.cg read stream "
+                                    "(dfpt_probe_read_bandwidth, best of 24/48/64 MiB buffers)",
+                     "peak_by_buffer_mib": l2_sizes,
                      "kernel": "k_trace<closest>", "avg_launch_ms": avg_trace_ms,
-                     "note": "algorithmic bytes (node and triangle records per closest-hit segment); the records "
-                             "stay L2-resident, DRAM carries the rays (traffic), so achieved can exceed the HBM copy rate",
+                     "note": "algorithmic bytes = node and triangle records per closest-hit segment; the records are "
+                             "L2-resident, so the roof is L2 read bandwidth; DRAM carries the rays (traffic)",
+                     "hbm": {"peak": hbm, "peak_source": hbm_note, "dram_gbs": dram_gbs,
+                             "dram_frac": dram_gbs / hbm if dram_gbs else None,
+                             "algorithmic_frac": achieved / hbm},
+                     "ncu": TRACE_NCU,
                      "bytes_per_segment": bytes_per_seg, "oracle_bytes_per_segment": oracle_bytes_per_seg,
                      "nodes_per_segment": nodes_per_seg, "triangles_per_segment": tris_per_seg,
                      "segments_per_launch": closest_segments / launches_per_step,
                      "segments_per_step": closest_segments},
         "kernels_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in kind_ms.items() if v[1]},
         "ms_per_step_profiled": sum(prof_ms) / len(prof_ms),
-
         "clocks": clocks,
     }
     if cpu:

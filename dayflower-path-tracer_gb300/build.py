@@ -42,6 +42,7 @@ def _units():
         ([nvcc, *ARCH, *NVCC_COMMON, "-fmad=false", "-c", str(CSRC / "dfpt_kernels_strict.cu")], BUILD_DIR / "dfpt_kernels_strict.o"),
         ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_api.cu")], BUILD_DIR / "dfpt_api.o"),
         ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_noalloc.cu")], BUILD_DIR / "dfpt_noalloc.o"),
+        ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_probe.cu")], BUILD_DIR / "dfpt_probe.o"),
         ([nvcc, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "dfpt_batch.cu")], BUILD_DIR / "dfpt_batch.o"),
         ([gxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}", "-c",
           str(CSRC / "dfpt_scene.cpp")], BUILD_DIR / "dfpt_scene.o"),

@@ -244,6 +244,13 @@ int dfpt_get_tuning(dfpt_handle* handle, const char* key, int32_t* value);
 /* Measurement hook (no reference counterpart): returns every persisting L2 line of this process
  * to normal, as a benchmark's L2 flush between timed steps must. */
 int dfpt_l2_reset(void);
+/* Measurement hook (no reference counterpart): the read bandwidth, in GB/s, of streaming the
+ * caller's device buffer (`bytes`: at least 1 MiB, a multiple of 16; 16-byte aligned) `repeats`
+ * times through L2 only (16-byte ld.global.cg loads), timed with CUDA events on `stream` (NULL: the
+ * legacy default stream) after one untimed pass that brings it into L2. With a buffer smaller than
+ * L2 this is the roof of kernels whose working set is L2-resident, as the closest-hit traversal's
+ * BVH and triangle records are. */
+int dfpt_probe_read_bandwidth(const void* device_buffer, int64_t bytes, int32_t repeats, void* stream, double* gbs);
 
 /* Number of kernels the handle launched since it was created (for launch accounting). */
 int dfpt_launch_count(dfpt_handle* handle, uint64_t* launches);

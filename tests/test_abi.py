@@ -114,3 +114,15 @@ def test_bad_primitive_extensions_rejected(lib, ext):
     s.primitive_extensions = ext
     assert _create(lib, s, sky) == -4
     assert b"extension" in lib.dfpt_last_error()
+
+
+def test_read_probe_rejects_bad_arguments_without_device(lib):
+    g = C.c_double()
+    buf = (C.c_uint8 * 64)()
+    base = C.cast(buf, C.c_void_p).value
+    aligned = (base + 15) // 16 * 16
+    assert lib.dfpt_probe_read_bandwidth(None, 1 << 20, 1, None, C.byref(g)) == -1
+    assert lib.dfpt_probe_read_bandwidth(C.c_void_p(aligned + 4), 1 << 20, 1, None, C.byref(g)) == -1  # not 16-byte aligned
+    assert lib.dfpt_probe_read_bandwidth(C.c_void_p(aligned), 4096, 1, None, C.byref(g)) == -1  # under 1 MiB
+    assert lib.dfpt_probe_read_bandwidth(C.c_void_p(aligned), (1 << 20) + 8, 1, None, C.byref(g)) == -1  # not a multiple of 16
+    assert lib.dfpt_probe_read_bandwidth(C.c_void_p(aligned), 1 << 20, 0, None, C.byref(g)) == -1
