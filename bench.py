@@ -396,50 +396,80 @@ def adjoint_leg(args, torch, barrier, dist, world):
         losses.append(loss)
     barrier()
     t_adj = float(np.median(iters))
-    # Finite-difference spot checks at the start point (same seed on both sides: fresh handles), on
-    # the loss linearised at the start image (weights 2 r0: the L2 gradient at r0, and a central
-    # difference without the loss's own second-order term). Once as configured (Russian roulette
-    # from depth 3: its albedo-dependent decisions make the common-random-number difference
-    # noisy) and once with roulette off (the estimator is smooth in albedo and turbidity).
+    # Finite-difference checks at the start point. The loss is linearised at a 64-spp start image
+    # (weights W = 2 (img - target), the same for every seed), so adjoint and central difference
+    # estimate the same derivative of sum(W * E[img]). Each seed renders the pair with common random
+    # numbers (fresh handles: the same pass indices). As configured (Russian roulette from depth 3:
+    # its albedo-dependent decisions make a single seed's difference jump) over `seeds` seeds, with
+    # the standard error of the mean per-seed gap; the Phong exponent's adjoint is a score-function
+    # estimate (a different estimator of the same derivative), so it needs the seeds too. With
+    # roulette off, albedo and turbidity on one seed (the estimator is smooth in them).
     a0 = start["albedo"].astype(np.float64)
     t0_ = float(start["turbidity"])
+    sun0 = np.asarray(start["sun_direction"], np.float64)
     hstep = 1e-3
+    phong_prim = 1 + 135  # a Phong sphere near the middle of the view (every 4th sphere is Phong)
 
-    def fd_check(prm):
-        kk = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), prm)
-        kk.update(w, h)
-        dd = DiffRenderer(kk)
-        img0 = dd.forward(a0, None, expo, t0_, sun, spp).astype(np.float64)
-        wgt = 2.0 * (img0 - target)
-        g0 = dd.backward(wgt.astype(np.float32))
-        kk.dispose()
+    def render(prm, theta, n_spp):
+        k2 = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), prm)
+        k2.update(w, h)
+        img = DiffRenderer(k2).forward(theta["albedo"], None, theta["exponent"], theta["turbidity"], theta["sun"], n_spp)
+        k2.dispose()
+        return img.astype(np.float64)
 
-        def lin(al, tb):
-            k2 = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), prm)
-            k2.update(w, h)
-            img = DiffRenderer(k2).forward(al, None, expo, tb, sun, spp).astype(np.float64)
-            k2.dispose()
-            return float(np.sum(wgt * img))
+    theta0 = {"albedo": a0, "exponent": expo.astype(np.float64), "turbidity": t0_, "sun": sun0}
+    wgt = 2.0 * (render(dict(params, seed=77), theta0, 64) - target)
 
+    def shifted(key, idx, dv):
+        t = {kk: (v.copy() if isinstance(v, np.ndarray) else v) for kk, v in theta0.items()}
+        if key == "turbidity":
+            t[key] = t[key] + dv
+        else:
+            t[key][idx] += dv
+        return t
+
+    checks = [("albedo[1,0]", "albedo", (1, 0), hstep), ("albedo[17,1]", "albedo", (17, 1), hstep),
+              ("albedo[100,2]", "albedo", (100, 2), hstep), ("albedo[200,0]", "albedo", (200, 0), hstep),
+              ("turbidity", "turbidity", None, hstep)]
+    more = [(f"phong_exponent[{phong_prim}]", "exponent", phong_prim, 1.0)] + \
+           [(f"sun_direction[{j}]", "sun", j, hstep) for j in range(3)]
+
+    def fd_check(prm, items, seeds):
+        per = {name: ([], []) for name, *_ in items}
+        for sd in range(seeds):
+            ps = dict(prm, seed=1000 + sd)
+            kk = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), ps)
+            kk.update(w, h)
+            dd = DiffRenderer(kk)
+            dd.forward(theta0["albedo"], None, theta0["exponent"], theta0["turbidity"], theta0["sun"], spp)
+            g = dd.backward(wgt.astype(np.float32))
+            kk.dispose()
+            adj = {"albedo": g["albedo"], "exponent": g["phong_exponent"], "turbidity": g["turbidity"], "sun": g["sun_direction"]}
+            for name, key, idx, hh in items:
+                plus = float(np.sum(wgt * render(ps, shifted(key, idx, hh), spp)))
+                minus = float(np.sum(wgt * render(ps, shifted(key, idx, -hh), spp)))
+                per[name][0].append(float(adj[key] if idx is None else adj[key][idx]))
+                per[name][1].append((plus - minus) / (2 * hh))
         out = {}
-        for prim, c in ((1, 0), (17, 1), (100, 2), (200, 0)):
-            ap_, am_ = a0.copy(), a0.copy()
-            ap_[prim, c] += hstep
-            am_[prim, c] -= hstep
-            out[f"albedo[{prim},{c}]"] = {"adjoint": float(g0["albedo"][prim, c]), "fd": (lin(ap_, t0_) - lin(am_, t0_)) / (2 * hstep)}
-        out["turbidity"] = {"adjoint": float(g0["turbidity"]), "fd": (lin(a0, t0_ + hstep) - lin(a0, t0_ - hstep)) / (2 * hstep)}
-        for v in out.values():
-            v["rel_err"] = abs(v["adjoint"] - v["fd"]) / max(abs(v["fd"]), 1e-30)
+        for name, (av, fv) in per.items():
+            av, fv = np.asarray(av), np.asarray(fv)
+            gap = fv - av
+            se = float(gap.std(ddof=1) / np.sqrt(len(gap))) if len(gap) > 1 else 0.0
+            rel = abs(float(av.mean() - fv.mean())) / max(abs(float(fv.mean())), 1e-30)
+            out[name] = {"adjoint": float(av.mean()), "fd": float(fv.mean()), "rel_err": rel, "se": se,
+                         "within": bool(rel <= 0.02 or abs(float(gap.mean())) <= 3 * se), "seeds": len(gap)}
         return out
 
-    fd = fd_check(params)
-    fd_no_rr = fd_check(dict(params, pt_ray_depth_russian_roulette=params["pt_ray_depth_maximum"] + 1))
+    fd = fd_check(params, checks + more, seeds=8)
+    fd_no_rr = fd_check(dict(params, pt_ray_depth_russian_roulette=params["pt_ray_depth_maximum"] + 1), checks, seeds=1)
     k.dispose()
     return {
         "metric": "adjoint iters/s", "value": world / t_adj, "unit": "iters/s", "t_adj_s": t_adj, "t_fwd_s": t_fwd,
         "t_adj_over_t_fwd": t_adj / t_fwd, "spp_per_iter": spp, "resolution": [w, h], "primitives": int(cs.primitives.size // 3),
         "loss_first": losses[0], "loss_last": losses[-1], "iters": len(losses),
-        "fd_check": fd, "fd_check_no_russian_roulette": fd_no_rr, "fd_step": hstep,
+        "fd_check": fd, "fd_check_no_russian_roulette": fd_no_rr, "fd_step": hstep, "fd_step_phong_exponent": 1.0,
+        "fd_note": "mean over seeds of adjoint and central difference (common random numbers per seed); se = standard "
+                   "error of the mean per-seed gap; within = rel_err <= 0.02 or |gap| <= 3 se",
         "trace_config": tuning["best"], "primitive_culling": tuning.get("primitive_culling", 0),
         "culling_ms_per_pass": {str(kk): round(v, 3) for kk, v in tuning.get("culling_ms_per_pass", {}).items()},
         "workload": "inverse_scene seed 6: 256 spheres (every 4th Phong) on a plane, Perez sky; albedo U(0.1,0.9)^3, T 3 -> start 0.5, T 2",
