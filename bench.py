@@ -408,7 +408,6 @@ def adjoint_leg(args, torch, barrier, dist, world):
     t0_ = float(start["turbidity"])
     sun0 = np.asarray(start["sun_direction"], np.float64)
     hstep = 1e-3
-    phong_prim = 1 + 135  # a Phong sphere near the middle of the view (every 4th sphere is Phong)
 
     def render(prm, theta, n_spp):
         k2 = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), prm)
@@ -418,7 +417,16 @@ def adjoint_leg(args, torch, barrier, dist, world):
         return img.astype(np.float64)
 
     theta0 = {"albedo": a0, "exponent": expo.astype(np.float64), "turbidity": t0_, "sun": sun0}
-    wgt = 2.0 * (render(dict(params, seed=77), theta0, 64) - target)
+    kp = RendererKernel(cs, SkyState(truth["sun_direction"], truth["turbidity"]), dict(params, seed=77))
+    kp.update(w, h)
+    dp_ = DiffRenderer(kp)
+    wgt = 2.0 * (dp_.forward(theta0["albedo"], None, theta0["exponent"], t0_, sun0, 64).astype(np.float64) - target)
+    # The Phong sphere checked is the one with the largest exponent gradient in this pilot (seed 77,
+    # independent of the checked seeds); every 4th sphere (primitives 4, 8, ...) is Phong.
+    pilot = np.abs(dp_.backward(wgt.astype(np.float32))["phong_exponent"])
+    kp.dispose()
+    phong = np.arange(4, pilot.size, 4)
+    phong_prim = int(phong[np.argmax(pilot[phong])])
 
     def shifted(key, idx, dv):
         t = {kk: (v.copy() if isinstance(v, np.ndarray) else v) for kk, v in theta0.items()}

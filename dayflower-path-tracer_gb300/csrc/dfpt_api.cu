@@ -1175,7 +1175,6 @@ int scene_upload(SceneStore& st, cudaStream_t s) {
         }
         st.scene.use_pairs = full_binary ? (empty_leaf ? 1 : 2) : 0;
         st.scene.pair_stack = 8;
-        st.scene.anyhit_walk = 0;
         CUDA_TRY(upload(st.pairs, pairs, s));
         CUDA_TRY(cudaStreamSynchronize(s));
     }
@@ -1538,15 +1537,6 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->wide_graph_valid = false;
         return DFPT_OK;
     }
-    if (std::strcmp(key, "anyhit_walk") == 0) {
-        // Any-hit queries with the compact pair records: 0 the threaded preorder walk, 1 the
-        // depth-first pair walk (same answers: an any-hit query's result does not depend on order).
-        if (value < 0 || value > 1) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "anyhit_walk %d outside [0, 1]", value);
-        h->sc.scene.anyhit_walk = value;
-        h->graph_valid = false;
-        h->wide_graph_valid = false;
-        return DFPT_OK;
-    }
     if (std::strcmp(key, "primitive_culling") == 0) {
         if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
         scene_set_culling(h->sc, value);
@@ -1563,7 +1553,6 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "trace_configs") == 0) { *value = h->fast.trace_configs; return DFPT_OK; }
     if (std::strcmp(key, "primitive_culling") == 0) { *value = h->sc.scene.use_culling; return DFPT_OK; }
     if (std::strcmp(key, "pair_stack") == 0) { *value = h->sc.scene.pair_stack; return DFPT_OK; }
-    if (std::strcmp(key, "anyhit_walk") == 0) { *value = h->sc.scene.anyhit_walk; return DFPT_OK; }
     if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }

@@ -375,10 +375,6 @@ template <bool ANY, int K>
 __device__ __forceinline__ bool mesh_walk_pair_compact(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo,
                                                        float dxo, float dyo, float dzo, Hit& h, TraceStats& st);
 
-template <int K>
-__device__ __forceinline__ bool mesh_anyhit_pairs(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo,
-                                                  float dxo, float dyo, float dzo, Hit& h, TraceStats& st);
-
 template <bool ANY, int V>
 __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo, float dxo,
                                           float dyo, float dzo, Hit& h, TraceStats& st) {
@@ -395,11 +391,6 @@ __device__ __forceinline__ bool mesh_walk(const DevScene& S, int root, int prim,
     // pending right children overflow the stack.
     if constexpr (V == 5 && !ANY) {
         if (S.use_pairs == 2) return mesh_walk_pair_compact<ANY, 8>(S, root, prim, oxo, oyo, ozo, dxo, dyo, dzo, h, st);
-    }
-    // Any-hit queries in an order of their own (mesh_anyhit_pairs): depth first over the pair records.
-    if constexpr (V == 5 && ANY) {
-        if (S.use_pairs == 2 && S.anyhit_walk == 1)
-            return mesh_anyhit_pairs<DFPT_ANYHIT_STACK>(S, root, prim, oxo, oyo, ozo, dxo, dyo, dzo, h, st);
     }
     const SlabRay sr = slab_ray(oxo, oyo, ozo, dxo, dyo, dzo);
     int node = root;
@@ -696,86 +687,6 @@ __device__ __forceinline__ bool mesh_walk_pair_compact(const DevScene& S, int ro
                 return false;
             }
         }
-    }
-}
-
-// Any-hit query of one mesh in an order of its own. The reference's any-hit walk (isTesting,
-// GRK:1097-1194) returns at the first triangle hit; until then its closest distance is the ray's
-// limit, so every box test and every triangle test it makes has operands that do not depend on
-// the order of the walk: the set of leaves it can reach, and whether one of them holds a hit, are
-// fixed. Any order that tests every reachable leaf until a hit therefore returns the same answer.
-// This one walks depth first over the pair records: an entered inner node's record gives both
-// children's boxes in one load, the nearer accepted child is entered first and the other waits
-// on a stack in shared memory, one entry per level at most. A tree deeper than the stack
-// (K entries) finishes with the threaded walk from the root, which gives the same answer.
-template <int K>
-__device__ __forceinline__ bool mesh_anyhit_pairs(const DevScene& S, int root, int prim, float oxo, float oyo, float ozo,
-                                                  float dxo, float dyo, float dzo, Hit& h, TraceStats& st) {
-    __shared__ int astk[K * 256];  // [entry][thread]: an inner node's index, or ~(first triangle) of a leaf
-    const int tid = threadIdx.x;
-    const SlabRay sr = slab_ray(oxo, oyo, ozo, dxo, dyo, dzo);
-    int cur, leaf;  // the node being entered (an inner node's index) / its first triangle (-1: inner)
-    {
-        const float4 n0 = __ldg(S.nodes + 2 * root), n1 = __ldg(S.nodes + 2 * root + 1);
-        st.nodes++;
-        float tmin, tmax;
-        slab_interval(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, sr, tmin, tmax);
-        if (!box_accepts(tmin, tmax, h.t)) return false;
-        cur = root;
-        leaf = __float_as_int(n1.w);
-    }
-    int top = 0;
-    for (;;) {
-        bool next_known = false;
-        if (leaf >= 0) {
-            for (int k = leaf;; ++k) {
-                const float4 a = __ldg(S.tris + 3 * k);
-                const float4 e0 = __ldg(S.tris + 3 * k + 1);
-                const float4 e1 = __ldg(S.tris + 3 * k + 2);
-                st.tris++;
-                const float t = isect_triangle(oxo, oyo, ozo, dxo, dyo, dzo, a, e0, e1, h.t);
-                if (t < h.t) {
-                    h.t = t;
-                    h.prim = prim;
-                    h.shape_type = DFPT_SHAPE_TRIANGLE;
-                    h.shape_offset = __float_as_int(a.w);
-                    return true;
-                }
-                if (__float_as_int(e0.w) != 0) break;
-            }
-        } else {
-            const float4* P = S.pairs + 4 * (size_t)cur;
-            const float4 p0 = __ldg(P), p1 = __ldg(P + 1), p2 = __ldg(P + 2);
-            const int4 p3 = __ldg(reinterpret_cast<const int4*>(P + 3));
-            float lmin, lmax, rmin, rmax;
-            slab_interval(p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, sr, lmin, lmax);
-            slab_interval(p1.z, p1.w, p2.x, p2.y, p2.z, p2.w, sr, rmin, rmax);
-            st.nodes += 2;
-            const bool acc_l = box_accepts(lmin, lmax, h.t), acc_r = box_accepts(rmin, rmax, h.t);
-            const int l_entry = p3.x >= 0 ? ~p3.x : cur + 1, r_entry = p3.y >= 0 ? ~p3.y : p3.z;
-            if (acc_l || acc_r) {
-                int go = acc_l ? l_entry : r_entry;
-                if (acc_l && acc_r) {
-                    const bool left_first = lmin <= rmin;
-                    go = left_first ? l_entry : r_entry;
-                    if (top == K) {
-                        // Deeper than the stack: the threaded walk from the root answers alone.
-                        return mesh_walk<true, 0>(S, root, prim, oxo, oyo, ozo, dxo, dyo, dzo, h, st);
-                    }
-                    astk[top * 256 + tid] = left_first ? r_entry : l_entry;
-                    ++top;
-                }
-                cur = go >= 0 ? go : -1;
-                leaf = go >= 0 ? -1 : ~go;
-                next_known = true;
-            }
-        }
-        if (next_known) continue;
-        if (top == 0) return false;
-        --top;
-        const int e = astk[top * 256 + tid];
-        cur = e >= 0 ? e : -1;
-        leaf = e >= 0 ? -1 : ~e;
     }
 }
 

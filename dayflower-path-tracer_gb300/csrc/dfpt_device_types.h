@@ -34,8 +34,6 @@ struct DevScene {
     int use_pairs;          // 1: every mesh BVH is a full binary tree, so pair records describe the walk;
                             // 2: the same, and no leaf is empty (the compact pair walk's condition)
     int pair_stack;         // entries of the compact pair walk's stack in use (1..8; 8 unless a test lowers it)
-    int anyhit_walk;        // any-hit queries (shadow rays, the final continuation) with use_pairs == 2:
-                            // 0 the threaded preorder walk, 1 a depth-first walk over the pair records
     const float4* shade_tris;  // per triangle (triangle offset / 12), the values surface() reads, copied from
                                // point3fs / point2fs / vector3fs: {a.xyz, b.x}, {b.yz, c.xy}, {c.z, uva.xy, uvb.x},
                                // {uvb.y, uvc.xy, na.x}, {na.yz, nb.xy}, {nb.z, nc.xyz}, {tga.xyz, tgb.x},
@@ -58,7 +56,6 @@ struct DevScene {
 };
 #define DFPT_CULL_CANDIDATES 16  // candidates a ray collects before falling back to the full loop
 #define DFPT_CULL_STACK 32
-#define DFPT_ANYHIT_STACK 24  // stack entries of the any-hit pair walk (deeper trees fall back to the threaded walk)
 
 // Renderer parameters and derived per-scene constants, in device memory (read through __ldg) so
 // captured CUDA graphs stay valid when they change.

@@ -223,10 +223,6 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *   "pair_stack"        stack entries of the compact pair walk (1..8, default 8); fewer entries
  *                       take its overflow path more often (same hits; a rejected node may then be
  *                       counted twice by the visit counters);
- *   "anyhit_walk"       any-hit queries (sun shadow rays, the final continuation) with the compact
- *                       pair records: 0 (default) the threaded preorder walk, 1 a depth-first walk
- *                       over the pair records, nearer child first (an any-hit query's answer does
- *                       not depend on the order of its walk);
  *   "trace_carveout"    shared-memory carveout preference of the current configuration's
  *                       closest-hit kernels (percent, -1 the driver's choice; process-wide);
  *   "primitive_culling" 0 the reference's full primitive loop, 1 a padded world-box test per

@@ -192,9 +192,7 @@ def test_trace_configs_agree(scenes):
     handle per configuration, so every run draws from pass 0 of the same stream). The compact pair
     walk also runs with 1- and 2-entry stacks, which drop stack entries on most walks: its hits
     stay exact, and its node counter may count a right child twice (the threaded continuation
-    re-tests one its parent's step rejected), never fewer. With the depth-first any-hit walk
-    (anyhit_walk 1) the shadow and continuation rays visit other nodes in another order: every
-    hit, segment and closest-hit visit stays the same, and so does every any-hit answer (the film)."""
+    re-tests one its parent's step rejected), never fewer."""
     scene, sky, params, (w, h) = scenes["meshes"]
     ref = None
     n = None
@@ -205,11 +203,9 @@ def test_trace_configs_agree(scenes):
         if cases is None:
             n = k.get_tuning("trace_configs")
             assert n > COMPACT_PAIR_CONFIG
-            cases = [(c, 8, 0) for c in range(n)] + [(COMPACT_PAIR_CONFIG, 1, 0), (COMPACT_PAIR_CONFIG, 2, 0),
-                                                     (COMPACT_PAIR_CONFIG, 8, 1)]
+            cases = [(c, 8) for c in range(n)] + [(COMPACT_PAIR_CONFIG, 1), (COMPACT_PAIR_CONFIG, 2)]
         k.set_tuning("trace_config", cases[cfg][0])
         k.set_tuning("pair_stack", cases[cfg][1])
-        k.set_tuning("anyhit_walk", cases[cfg][2])
         k.set_counting(True)
         k.execute(1)
         film, _ = k.film()
@@ -219,10 +215,7 @@ def test_trace_configs_agree(scenes):
             ref = got
         else:
             assert np.array_equal(got[0], ref[0]), cases[cfg]
-            if cases[cfg][2] == 1:
-                same = [0, 1, 4, 5]  # segments, closest-hit nodes and triangles
-                assert np.array_equal(got[2][same], ref[2][same]), (cases[cfg], got[2], ref[2])
-            elif cases[cfg][1] == 8:
+            if cases[cfg][1] == 8:
                 assert np.array_equal(got[2], ref[2]), (cases[cfg], got[2], ref[2])  # same segments, nodes and triangles
             else:
                 same = [0, 1, 3, 5]  # segments and triangles
