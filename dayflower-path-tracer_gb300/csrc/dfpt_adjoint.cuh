@@ -14,8 +14,9 @@
 //                             Russian roulette's survival probability is held constant)
 //   Phong exponent n          dL/dn   = (later radiance) * (1/(n+1) + ln cos)   (score of the
 //                             lobe density (n+1) cos^n the cosine was drawn from)
-//   sky (turbidity, sun)      forward-mode duals through the sky color of escaping rays and the
-//                             sun sample's cosine (shadow-ray visibility held fixed)
+//   sky (turbidity, sun)      forward-mode duals through the sky color of escaping rays; the sun
+//                             term's derivative over the rim of the sun's cone (sun_rim_tan),
+//                             visibility included
 // Tangents of the sky fields with respect to (turbidity, sun direction) come from the host.
 
 // ---- Dual numbers with four tangents: d/d(turbidity, sun x, sun y, sun z) ----
@@ -152,37 +153,59 @@ __device__ void sky_color_tan(const DevParams& P, float dx, float dy, float dz, 
     }
 }
 
-// The cosine term of sun_sample (same draws u, v) with the sun's fields as duals.
-__device__ D4 sun_dot_tan(const DevParams& P, float px, float py, float pz, float nx, float ny, float nz, float u, float v) {
+// The sun term's derivative with respect to (turbidity, sun direction), visibility included. The
+// sun sample is uniform over the cone C of directions towards the sun's disk (axis: the world sun
+// direction W, half-angle a with sin^2 a = 500^2 / |origin - p|^2), so the vertex's expected sun term
+// is the mean of G(w) = c max(w.n, 0) V(w) over C (c: the loss-weighted albedo factor / pi, V: the
+// shadow ray's visibility). Under a change of the sun direction C moves rigidly and its angle
+// changes with the distance to the sun's origin; the derivative of the mean over a moving domain is
+// an integral over its rim (Reynolds transport):
+//   d/dq mean_C G = (1 / Omega) * integral over the rim of (G - k) v_n dl,   Omega = 2 pi (1 - cos a),
+// with v_n = (w.dW/dq - d cos a/dq) / sin a the rim's outward speed and k any number independent of
+// the rim point (the rim integral of v_n is d Omega / dq). One rim direction at angle phi, uniform,
+// gives (G(w_phi) - k) (w_phi.dW/dq - d cos a/dq) / (1 - cos a); k = the forward sample's own G
+// (whose mean is the mean of G) makes the estimate small where the whole cone is lit or shadowed,
+// and leaves the shadow edges that cross the cone - which a derivative with the visibility held
+// fixed misses. phi comes from its own counter-based stream (pixel, pass, bounce), so the replay
+// draws nothing the forward did not. One extra any-hit ray per sun sample.
+__device__ void sun_rim_tan(const DevScene& S, const DevParams& P, uint32_t pixel, uint32_t pass, int bounce, float px, float py,
+                            float pz, float nx, float ny, float nz, float c, float g_forward, float gsky[4]) {
     const float sr2 = 500.0f * 500.0f;
     const D4 tx = d4f(P, SKY_SUN_ORIGIN, P.sun_origin[0]) - px;
     const D4 ty = d4f(P, SKY_SUN_ORIGIN + 1, P.sun_origin[1]) - py;
     const D4 tz = d4f(P, SKY_SUN_ORIGIN + 2, P.sun_origin[2]) - pz;
-    const D4 tl2 = tx * tx + ty * ty + tz * tz;
-    const D4 sin2 = d4c(sr2) / tl2;
-    const D4 one_m = 1.0f - sin2;
-    const D4 cos_max = one_m.v > 0.0f ? d4sqrt(one_m) : d4c(0.0f);
-    const D4 cos_t = u * (cos_max - 1.0f) + 1.0f;
-    const D4 st2 = 1.0f - cos_t * cos_t;
-    const D4 sin_t = st2.v > 0.0f ? d4sqrt(st2) : d4c(0.0f);
-    const float phi = TWO_PI * v;
-    const D4 x = cosf(phi) * sin_t, y = sinf(phi) * sin_t, z = cos_t;
-    const D4 wx = d4f(P, SKY_SUN_DIR_WORLD, P.sun_dir_world[0]);
-    const D4 wy = d4f(P, SKY_SUN_DIR_WORLD + 1, P.sun_dir_world[1]);
-    const D4 wz = d4f(P, SKY_SUN_DIR_WORLD + 2, P.sun_dir_world[2]);
-    const float ax = fabsf(wx.v), ay = fabsf(wy.v), az = fabsf(wz.v);
-    const bool xmin = ax < ay && ax < az, ylt = ay < az;
-    const D4 vx = xmin ? d4c(0.0f) : ylt ? wz : wy;
-    const D4 vy = xmin ? wz : ylt ? d4c(0.0f) : -wx;
-    const D4 vz = xmin ? -wy : ylt ? -wx : d4c(0.0f);
-    const D4 vr = d4rsqrt(vx * vx + vy * vy + vz * vz);
-    const D4 vnx = vx * vr, vny = vy * vr, vnz = vz * vr;
-    const D4 unx = vny * wz - vnz * wy, uny = vnz * wx - vnx * wz, unz = vnx * wy - vny * wx;
-    const D4 rx = unx * x + vnx * y + wx * z;
-    const D4 ry = uny * x + vny * y + wy * z;
-    const D4 rz = unz * x + vnz * y + wz * z;
-    const D4 rr = d4rsqrt(rx * rx + ry * ry + rz * rz);
-    return (rx * nx + ry * ny + rz * nz) * rr;
+    const D4 sin2 = d4c(sr2) / (tx * tx + ty * ty + tz * tz);
+    if (!(sin2.v > 0.0f && sin2.v < 1.0f)) return;
+    const D4 cos_a = d4sqrt(1.0f - sin2);
+    const float sin_a = sqrtf(sin2.v);
+    const float one_m_cos = sin2.v / (1.0f + cos_a.v);  // 1 - cos a without cancellation
+    const uint4 rb = philox4x32_10(make_uint4(pass, 0x40000000u | (uint32_t)bounce, P.seed_hi, 0x52494D21u), make_uint2(pixel, P.seed_lo));
+    const float phi = TWO_PI * ((float)(rb.x >> 8) * (1.0f / 16777216.0f));
+    const float wx = P.sun_dir_world[0], wy = P.sun_dir_world[1], wz = P.sun_dir_world[2];
+    const float ax = fabsf(wx), ay = fabsf(wy), az = fabsf(wz);
+    const float vx = ax < ay && ax < az ? 0.0f : ay < az ? wz : wy;
+    const float vy = ax < ay && ax < az ? wz : ay < az ? 0.0f : -wx;
+    const float vz = ax < ay && ax < az ? -wy : ay < az ? -wx : 0.0f;
+    const float vr = rsqrtf(vx * vx + vy * vy + vz * vz);
+    const float vnx = vx * vr, vny = vy * vr, vnz = vz * vr;
+    const float unx = vny * wz - vnz * wy, uny = vnz * wx - vnx * wz, unz = vnx * wy - vny * wx;
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    const float x = cp * sin_a, y = sp * sin_a, z = cos_a.v;
+    float rx = unx * x + vnx * y + wx * z, ry = uny * x + vny * y + wy * z, rz = unz * x + vnz * y + wz * z;
+    const float rr = rsqrtf(rx * rx + ry * ry + rz * rz);
+    rx *= rr; ry *= rr; rz *= rr;
+    const float dot0 = rx * wx + ry * wy + rz * wz, dot1 = rx * nx + ry * ny + rz * nz;
+    float g_rim = 0.0f;
+    if (dot0 > 0.0f && dot1 > 0.0f && c != 0.0f) {
+        TraceStats st{0, 0};
+        const Hit h = trace_v<true, 1>(S, true, px, py, pz, rx, ry, rz, st);
+        if (h.t >= INF - 0.0001f) g_rim = c * dot1;
+    }
+    const float k = (g_rim - g_forward) / one_m_cos;
+    if (k == 0.0f) return;
+    const D4 dwx = d4f(P, SKY_SUN_DIR_WORLD, wx), dwy = d4f(P, SKY_SUN_DIR_WORLD + 1, wy), dwz = d4f(P, SKY_SUN_DIR_WORLD + 2, wz);
+    for (int j = 0; j < 4; ++j) gsky[j] += k * (rx * dwx.d[j] + ry * dwy.d[j] + rz * dwz.d[j] - cos_a.d[j]);
 }
 
 // Per-block gradient accumulation: per-primitive entries in shared memory (float, one launch) when
@@ -300,16 +323,17 @@ __global__ void __launch_bounds__(256) k_shade_adj(DevScene S, const DevParams* 
                     const float u = rng.next(), v = rng.next();
                     float lx, ly, lz, dot1;
                     const int seen = (B.diff_vis[sample * npix + pixel] >> bounce) & 1;
+                    const float c = (w.x * T.x * ar + w.y * T.y * ag + w.z * T.z * ab) * INV_PI;
+                    float g_forward = 0.0f;
                     if (sun_sample(P, s.px, s.py, s.pz, wx, wy, wz, u, v, lx, ly, lz, dot1) && seen) {
                         const float k = dot1 * INV_PI;
                         Lu.x += T.x * (ar * 1.0f * k); Lu.y += T.y * (ag * 1.0f * k); Lu.z += T.z * (ab * 1.0f * k);
                         acc.add(h.prim, 0, w.x * T.x * tr * k);
                         acc.add(h.prim, 1, w.y * T.y * tg * k);
                         acc.add(h.prim, 2, w.z * T.z * tb * k);
-                        const D4 dd = sun_dot_tan(P, s.px, s.py, s.pz, wx, wy, wz, u, v);
-                        const float c = (w.x * T.x * ar + w.y * T.y * ag + w.z * T.z * ab) * INV_PI;
-                        for (int j = 0; j < 4; ++j) gsky[j] += c * dd.d[j];
+                        g_forward = c * dot1;
                     }
+                    sun_rim_tan(S, P, pixel, pass, bounce, s.px, s.py, s.pz, wx, wy, wz, c, g_forward, gsky);
                 }
                 const float a0r = ar, a0g = ag, a0b = ab;  // before Russian roulette's 1/q
                 const int depth = bounce + 1;

@@ -1414,30 +1414,44 @@ void sky_color_dual(const SunDual& k, bool active, double dX, double dY, double 
     }
 }
 
-// The sun sample's cosine (GRK:2238-2347, same draws) as a dual.
-Dual sun_cos_dual(const SunDual& k, const double* p, const double* n, double u, double v) {
-    const Dual tX = k.w[0] * 10000.0 - p[0], tY = k.w[1] * 10000.0 - p[1], tZ = k.w[2] * 10000.0 - p[2];
-    const Dual tl2 = tX * tX + tY * tY + tZ * tZ;
-    const Dual sin2 = (500.0 * 500.0) / tl2;
-    const Dual cosMax = dsqrt(1.0 - sin2);
-    const Dual cosT = u * (cosMax - 1.0) + 1.0;
-    const Dual sinT = dsqrt(1.0 - cosT * cosT);
-    const double phi = (double)(3.14159274101257324219f * 2.0f) * v;
-    const Dual x = std::cos(phi) * sinT, y = std::sin(phi) * sinT, z = cosT;
-    const Dual& sWX = k.w[0];
-    const Dual& sWY = k.w[1];
-    const Dual& sWZ = k.w[2];
-    const double aX = std::fabs(sWX.v), aY = std::fabs(sWY.v), aZ = std::fabs(sWZ.v);
-    const bool xmin = aX < aY && aX < aZ, ylt = aY < aZ;
-    const Dual vX = xmin ? dc(0) : ylt ? sWZ : sWY;
-    const Dual vY = xmin ? sWZ : ylt ? dc(0) : -sWX;
-    const Dual vZ = xmin ? -sWY : ylt ? -sWX : dc(0);
-    const Dual vl = 1.0 / dsqrt(vX * vX + vY * vY + vZ * vZ);
-    const Dual vnX = vX * vl, vnY = vY * vl, vnZ = vZ * vl;
-    const Dual unX = vnY * sWZ - vnZ * sWY, unY = vnZ * sWX - vnX * sWZ, unZ = vnX * sWY - vnY * sWX;
-    const Dual rX = unX * x + vnX * y + sWX * z, rY = unY * x + vnY * y + sWY * z, rZ = unZ * x + vnZ * y + sWZ * z;
-    const Dual rl = 1.0 / dsqrt(rX * rX + rY * rY + rZ * rZ);
-    return (rX * n[0] + rY * n[1] + rZ * n[2]) * rl;
+// The sun term's derivative over the rim of the sun's cone, visibility included (the estimator of the
+// GPU replay, here in FP64 with FP64 shadow rays): the cone of directions towards the sun's disk has
+// axis W and half-angle a, sin^2 a = 500^2 / |origin - p|^2 (GRK:2238-2347); for the mean of
+// G(w) = c max(w.n, 0) V(w) over it, d/dq = E_phi[(G(w_phi) - k) (w_phi.dW/dq - d cos a/dq) / (1 - cos a)]
+// for a rim direction at uniform angle phi and k = the forward sample's G (Reynolds transport over
+// the moving cone; k's mean is G's mean). phi: Philox4x32-10 at counter (pass, 2^30 + bounce,
+// seed_hi, "RIM!"), key (pixel, seed_lo), its first word.
+void sun_rim_dual(Kernel<double>& k, const SunDual& sd, const dfpt_sky* sky, uint32_t pixel, uint32_t pass, uint32_t seed_lo,
+                  uint32_t seed_hi, int bounce, const double* p, const double* n, double c, double g_forward, double* gsky) {
+    const Dual tX = sd.w[0] * 10000.0 - p[0], tY = sd.w[1] * 10000.0 - p[1], tZ = sd.w[2] * 10000.0 - p[2];
+    const double oX = (double)sky->sun_origin[0] - p[0], oY = (double)sky->sun_origin[1] - p[1], oZ = (double)sky->sun_origin[2] - p[2];
+    const double sin2 = (500.0 * 500.0) / (oX * oX + oY * oY + oZ * oZ);
+    if (!(sin2 > 0.0 && sin2 < 1.0)) return;
+    const Dual cosA = dsqrt(1.0 - (500.0 * 500.0) / (tX * tX + tY * tY + tZ * tZ));
+    const double cos_a = std::sqrt(1.0 - sin2), sin_a = std::sqrt(sin2), one_m_cos = sin2 / (1.0 + cos_a);
+    uint32_t cnt[4] = {pass, 0x40000000u | (uint32_t)bounce, seed_hi, 0x52494D21u};
+    philox(cnt, pixel, seed_lo);
+    const double phi = (double)(3.14159274101257324219f * 2.0f) * ((double)(cnt[0] >> 8) * (1.0 / 16777216.0));
+    const double wX = sky->sun_direction_world[0], wY = sky->sun_direction_world[1], wZ = sky->sun_direction_world[2];
+    const double aX = std::fabs(wX), aY = std::fabs(wY), aZ = std::fabs(wZ);
+    const double vX = aX < aY && aX < aZ ? 0.0 : aY < aZ ? wZ : wY;
+    const double vY = aX < aY && aX < aZ ? wZ : aY < aZ ? 0.0 : -wX;
+    const double vZ = aX < aY && aX < aZ ? -wY : aY < aZ ? -wX : 0.0;
+    const double vl = 1.0 / std::sqrt(vX * vX + vY * vY + vZ * vZ);
+    const double vnX = vX * vl, vnY = vY * vl, vnZ = vZ * vl;
+    const double unX = vnY * wZ - vnZ * wY, unY = vnZ * wX - vnX * wZ, unZ = vnX * wY - vnY * wX;
+    const double x = std::cos(phi) * sin_a, y = std::sin(phi) * sin_a, z = cos_a;
+    double rX = unX * x + vnX * y + wX * z, rY = unY * x + vnY * y + wY * z, rZ = unZ * x + vnZ * y + wZ * z;
+    const double rl = 1.0 / std::sqrt(rX * rX + rY * rY + rZ * rZ);
+    rX *= rl; rY *= rl; rZ *= rl;
+    const double dot0 = rX * wX + rY * wY + rZ * wZ, dot1 = rX * n[0] + rY * n[1] + rZ * n[2];
+    double g_rim = 0.0;
+    if (dot0 > 0.0 && dot1 > 0.0 && c != 0.0) {
+        const double t = k.intersect(p[0], p[1], p[2], rX, rY, rZ, true);
+        if (t >= K<double>::INF() - 0.0001) g_rim = c * dot1;
+    }
+    const double q = (g_rim - g_forward) / one_m_cos;
+    for (int j = 0; j < 4; ++j) gsky[j] += q * (rX * sd.w[0].d[j] + rY * sd.w[1].d[j] + rZ * sd.w[2].d[j] - cosA.d[j]);
 }
 
 // Renders with the parameters in FP64 and computes d(sum w * image)/d(parameters) by recording
@@ -1480,11 +1494,12 @@ void diff_rows(const Scene& S, const DiffIn& din, const SunDual& sd, int pass_be
                             for (int ch = 0; ch < 3; ++ch) later[ch] += ct.second[ch];
                     double* g = grad.data() + (size_t)v.prim * 7;
                     for (int ch = 0; ch < 3; ++ch) g[3 + ch] += w[ch] * v.T[ch];
-                    if (v.sun_vis) {
-                        for (int ch = 0; ch < 3; ++ch) g[ch] += w[ch] * v.T[ch] * v.tex[ch] * v.sun_dot * inv_pi;
-                        const Dual cd = sun_cos_dual(sd, v.p, v.w, v.sun_u, v.sun_v);
+                    if (v.sun) {
                         const double cw = (w[0] * v.T[0] * v.a0[0] + w[1] * v.T[1] * v.a0[1] + w[2] * v.T[2] * v.a0[2]) * inv_pi;
-                        for (int j = 0; j < 4; ++j) grad[(size_t)np * 7 + j] += cw * cd.d[j];
+                        if (v.sun_vis)
+                            for (int ch = 0; ch < 3; ++ch) g[ch] += w[ch] * v.T[ch] * v.tex[ch] * v.sun_dot * inv_pi;
+                        sun_rim_dual(k, sd, S.sky, (uint32_t)gid, (uint32_t)pass, (uint32_t)p->seed, (uint32_t)(p->seed >> 32), (int)vi,
+                                     v.p, v.w, cw, v.sun_vis ? cw * v.sun_dot : 0.0, grad.data() + (size_t)np * 7);
                     }
                     if (v.alive && v.albedo_mult)
                         for (int ch = 0; ch < 3; ++ch)
