@@ -368,11 +368,15 @@ def adjoint_leg(args, torch, barrier, dist, world):
     turb = float(start["turbidity"])
     expo, sun = start["phong_exponent"], start["sun_direction"]
 
+    target32 = target.astype(np.float32)
+
     def step(update=True):
-        img = d.forward(albedo, None, expo, turb, sun, spp).astype(np.float64)
-        r = img - target
-        loss = float(np.sum(r * r))
-        g = d.backward((2.0 * r).astype(np.float32))
+        # Residual in FP32 (the image's precision), the loss reduced in FP64, dL/dimage = 2 r.
+        r = d.forward(albedo, None, expo, turb, sun, spp) - target32
+        r64 = r.reshape(-1).astype(np.float64)
+        loss = float(r64 @ r64)
+        r *= 2.0
+        g = d.backward(r)
         return loss, g
 
     for _ in range(2):  # warm-up: graphs, buffers
