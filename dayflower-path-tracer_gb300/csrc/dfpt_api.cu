@@ -463,6 +463,7 @@ struct dfpt_handle {
     // Wide passes: dfpt_render's passes but the last run `wide_samples` at a time through the
     // batch stages (one scene), so each launch carries k samples per pixel (see render_wide).
     int wide_samples = 8;
+    bool pixel_tiles = false;  // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
     int wide_capacity = 0;
     size_t wide_shadow = 0;
     DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput;  // w_throughput: throughput + radiance records (PSI)
@@ -603,12 +604,20 @@ void dev_params_fill(DevParams& d, const dfpt_params& p, const dfpt_sky& k, cons
 
 namespace {
 
+bool is_simple_mode(int rt);
+
 void fill_dev_params(dfpt_handle* h) {
     DevParams& d = h->dev_params_host;
     dev_params_fill(d, h->params, h->sky, h->sc.host.camera.data(), h->width, h->height);
     d.record_hits = h->record_hits ? 1 : 0;
     d.counting = h->counting ? 1 : 0;
     d.clear_pass = h->clear_pass;
+    // Tile slot order: the counter stream keys samples by pixel, so the order is free; the LCG's
+    // per-pixel states, the wireframe overlay's per-pixel rays and the adjoint's per-pixel records
+    // keep slot = pixel.
+    // The per-pixel modes (k_simple) write their results at slot = pixel.
+    d.pixel_tiles = (h->pixel_tiles && h->params.rng_kind == DFPT_RNG_COUNTER && h->params.wireframes != 1 && !h->diff_on &&
+                     !is_simple_mode(h->params.renderer_type) && h->width % 8 == 0 && h->height % 4 == 0) ? 1 : 0;
     if (h->diff_on) {
         d.diff = 1;
         d.diff_pass0 = h->diff_pass0;
@@ -1537,6 +1546,10 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->wide_graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "pixel_tiles") == 0) {
+        h->pixel_tiles = value != 0;
+        return push_params(h);
+    }
     if (std::strcmp(key, "primitive_culling") == 0) {
         if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
         scene_set_culling(h->sc, value);
@@ -1555,6 +1568,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "pair_stack") == 0) { *value = h->sc.scene.pair_stack; return DFPT_OK; }
     if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
+    if (std::strcmp(key, "pixel_tiles") == 0) { *value = h->pixel_tiles ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }

@@ -78,6 +78,7 @@ struct DevParams {
     int record_hits;
     int counting;
     int clear_pass;  // the film is replaced (not averaged) on this pass index
+    int pixel_tiles; // plain passes: queue slot i holds a pixel of an 8 x 4 tile (pixel_of_slot)
     // Sky (float copies of the Perez model; den_l is the theta0-only denominator).
     float sky_u[3], sky_v[3], sky_w[3];
     float sun_dir[3], sun_dir_world[3], sun_origin[3];

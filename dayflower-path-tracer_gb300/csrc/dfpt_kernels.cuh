@@ -604,6 +604,23 @@ __device__ __forceinline__ unsigned rel_of_slot(unsigned slot, unsigned np, unsi
 }
 #endif
 
+// Slot order of a plain pass. With P.pixel_tiles the pass's queue slots run over 8 x 4 pixel tiles
+// (tiles in row-major order, a tile's 32 pixels row by row), so a warp's primary rays leave a
+// compact block of pixels instead of a 32-pixel strip; the bounces' queues keep that locality. A
+// path keeps its slot; its pixel (RNG key, selection buffer, hit records, film) follows from it.
+// Only for widths that are multiples of 8 and heights that are multiples of 4.
+__device__ __forceinline__ int pixel_of_slot(const DevParams& P, int i) {
+    if (!P.pixel_tiles) return i;
+    const int t = i >> 5, l = i & 31, tw = P.width >> 3;
+    const int ty = t / tw, tx = t - ty * tw;
+    return ((ty << 2) + (l >> 3)) * P.width + (tx << 3) + (l & 7);
+}
+__device__ __forceinline__ int slot_of_pixel(const DevParams& P, int p) {
+    if (!P.pixel_tiles) return p;
+    const int y = p / P.width, x = p - y * P.width;
+    return (((y >> 2) * (P.width >> 3) + (x >> 3)) << 5) | ((y & 3) << 3) | (x & 7);
+}
+
 __device__ __forceinline__ uint32_t camera_draws(const DevScene& S, const DevParams& P) {
     const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
                     (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
@@ -690,6 +707,7 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
         }
         const DevScene& S = scene_of<BATCH>(S0, Q, sid);
         const DevParams& P = params_of<BATCH>(Pp, Q, sid);
+        if constexpr (!BATCH) pixel = pixel_of_slot(P, i);
         float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 0, 0);
         bool live = false;
         if (valid) {
@@ -998,7 +1016,7 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
             const float sid_bits = BATCH ? d4.w : 0.0f;
             const DevScene& S = scene_of<BATCH>(S0, Q, sid);
             const DevParams& P = params_of<BATCH>(Pp, Q, sid);
-            uint32_t rng_pixel = (uint32_t)path, rng_pass = pass;
+            uint32_t rng_pixel = (uint32_t)(BATCH ? path : pixel_of_slot(P, path)), rng_pass = pass;
             if constexpr (BATCH) {
 #ifdef DFPT_ONE_SCENE
                 // One scene: the slot's pixel and pass follow from its index as k_camera derived
@@ -1029,7 +1047,7 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
             const bool fresh = bounce == 0 && lean_start<BATCH>(P);
             float4 T = fresh ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : B.throughput[PSI(path)];
             float4 L = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : B.radiance[PSI(path)];
-            if (!BATCH && bounce == 0) B.primitive_offsets[path] = h.prim >= 0 ? h.prim * 3 : -1;
+            if (!BATCH && bounce == 0) B.primitive_offsets[rng_pixel] = h.prim >= 0 ? h.prim * 3 : -1;
             // A handle's waves of passes: the selection buffer holds the first hits of the call's
             // last pass (wave record entry 4; batches of scenes have no selection buffer).
             if (BATCH && bounce == 0 && B.primitive_offsets != nullptr && (long long)rng_pass == Q.wave_base[4])
@@ -1041,16 +1059,17 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
                 L.z += T.z * sky.z * INV_PI;
                 B.radiance[PSI(path)] = L;
                 if (!BATCH && bounce == 0 && P.record_hits) {
-                    B.hit_prim_offset[path] = -1; B.hit_shape_type[path] = -1; B.hit_shape_offset[path] = -1;
-                    B.hit_distance[path] = INF;
+                    B.hit_prim_offset[rng_pixel] = -1; B.hit_shape_type[rng_pixel] = -1; B.hit_shape_offset[rng_pixel] = -1;
+                    B.hit_distance[rng_pixel] = INF;
                 }
             } else {
                 Rng rng = make_rng(P, rng_pixel, rng_pass, fresh ? (uint64_t)camera_draws(S, P) : B.rng[path]);
                 const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
                 if (!BATCH && bounce == 0 && P.record_hits) {
-                    B.hit_prim_offset[path] = h.prim * 3; B.hit_shape_type[path] = h.shape_type; B.hit_shape_offset[path] = h.shape_offset;
-                    B.hit_distance[path] = h.t;
-                    B.hit_normal[3 * path] = s.nx; B.hit_normal[3 * path + 1] = s.ny; B.hit_normal[3 * path + 2] = s.nz;
+                    const uint32_t px = rng_pixel;
+                    B.hit_prim_offset[px] = h.prim * 3; B.hit_shape_type[px] = h.shape_type; B.hit_shape_offset[px] = h.shape_offset;
+                    B.hit_distance[px] = h.t;
+                    B.hit_normal[3 * px] = s.nx; B.hit_normal[3 * px + 1] = s.ny; B.hit_normal[3 * px + 2] = s.nz;
                 }
                 const int so_off = __ldg(S.prim_info + h.prim).z;
                 const float dp = s.nx * d4.x + s.ny * d4.y + s.nz * d4.z;
@@ -1512,14 +1531,16 @@ __global__ void __launch_bounds__(256) k_film(const DevParams* __restrict__ Pp, 
     const int pass = *B.pass_index;
     const bool clear = pass == P.clear_pass;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        // Pixel i's path (its queue slot).
+        const int path = slot_of_pixel(P, i);
         float4 sum = B.film_sum[i], comp = B.film_comp[i];
         int cnt = B.film_n[i];
-        film_add(B.radiance[PSI(i)], B.pixel_flags[i], clear, sum, comp, cnt);
+        film_add(B.radiance[PSI(path)], B.pixel_flags[path], clear, sum, comp, cnt);
         if (P.diff) {
             const int k = pass - P.diff_pass0;
             if (k >= 0 && k < P.diff_spp) {
-                B.diff_L[(size_t)k * n + i] = B.radiance[PSI(i)];
-                B.diff_vis[(size_t)k * n + i] = (B.pixel_flags[i] & 1) ? 0 : B.vis[i];
+                B.diff_L[(size_t)k * n + i] = B.radiance[PSI(path)];
+                B.diff_vis[(size_t)k * n + i] = (B.pixel_flags[path] & 1) ? 0 : B.vis[path];
             }
         }
         B.film_sum[i] = sum; B.film_comp[i] = comp; B.film_n[i] = cnt;

@@ -293,3 +293,27 @@ def test_obj_model_raycast_bit_exact(oracle_mod):
     hit = prim >= 0
     assert hit.sum() > 100
     np.testing.assert_allclose(dist[hit], ref["hit_dist"][hit], rtol=1e-5, atol=0)
+
+
+def test_pixel_tile_order_keeps_every_pixel(scenes):
+    """Plain passes in 8 x 4 pixel-tile slot order (pixel_tiles) trace each pixel's sample from the
+    same counter-based stream as row order: the same films (sun contributions are added with float
+    atomics: a few ulps), hit records and selection buffer."""
+    scene, sky, params, (w, h) = scenes["meshes"]
+    assert w % 8 == 0 and h % 4 == 0
+    out = []
+    for tiles in (0, 1):
+        k = _kernel(scene, sky, dict(params, renderer_type=2), w, h, strict=False, hits=True)
+        k.set_tuning("wide_samples", 1)
+        k.set_tuning("pixel_tiles", tiles)
+        assert k.get_tuning("pixel_tiles") == tiles
+        k.execute(3)
+        film, samples = k.film()
+        out.append((film.copy(), samples.copy(), [x.copy() for x in k.hits()], k.primitive_offsets().copy()))
+        k.dispose()
+    (f0, s0, h0, p0), (f1, s1, h1, p1) = out
+    assert (s0 == 3).all() and (s1 == 3).all()
+    assert np.allclose(f0, f1, rtol=1e-5, atol=1e-6), np.abs(f0 - f1).max()
+    for a, b in zip(h0, h1):
+        assert np.array_equal(a, b)
+    assert np.array_equal(p0, p1)
