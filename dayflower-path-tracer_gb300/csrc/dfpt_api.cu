@@ -463,7 +463,8 @@ struct dfpt_handle {
     // Wide passes: dfpt_render's passes but the last run `wide_samples` at a time through the
     // batch stages (one scene), so each launch carries k samples per pixel (see render_wide).
     int wide_samples = 8;
-    bool pixel_tiles = false;  // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
+    bool pixel_tiles = true;   // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
+    int tail_bounce = 0;       // plain passes: first bounce of the tail launch (0: a launch per bounce)
     int wide_capacity = 0;
     size_t wide_shadow = 0;
     DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput;  // w_throughput: throughput + radiance records (PSI)
@@ -735,12 +736,18 @@ int issue_pass(dfpt_handle* h) {
         mark(h, KIND_SIMPLE); K.simple(c); ++k;
     } else {
         const int nb = h->params.pt_ray_depth_maximum < 1 ? 1 : (h->params.pt_ray_depth_maximum > DFPT_MAX_DEPTH ? DFPT_MAX_DEPTH : h->params.pt_ray_depth_maximum);
+        // With tail_bounce t, bounces t .. nb - 1 and the final any-hit run in one tail launch.
+        const int tb = (h->tail_bounce >= 1 && h->tail_bounce < nb && K.tail) ? h->tail_bounce : nb;
         mark(h, KIND_CAMERA); K.camera(c); ++k;
-        for (int b = 0; b < nb; ++b) {
+        for (int b = 0; b < tb; ++b) {
             mark(h, KIND_TRACE); K.trace_closest(c, b); ++k;
             mark(h, KIND_SHADE); K.shade(c, b); ++k;
         }
-        mark(h, KIND_FINAL); K.final_(c, nb); ++k;
+        if (tb < nb) {
+            mark(h, KIND_TRACE); K.tail(c, tb, nb); ++k;
+        } else {
+            mark(h, KIND_FINAL); K.final_(c, nb); ++k;
+        }
         // The sun shadow rays of all bounces, traced together.
         if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.shadow(c, 0); ++k; }
     }
@@ -1550,6 +1557,12 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->pixel_tiles = value != 0;
         return push_params(h);
     }
+    if (std::strcmp(key, "tail_bounce") == 0) {
+        if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %d outside [0, %d]", value, DFPT_MAX_DEPTH);
+        h->tail_bounce = value;
+        h->graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "primitive_culling") == 0) {
         if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
         scene_set_culling(h->sc, value);
@@ -1569,6 +1582,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "pixel_tiles") == 0) { *value = h->pixel_tiles ? 1 : 0; return DFPT_OK; }
+    if (std::strcmp(key, "tail_bounce") == 0) { *value = h->tail_bounce; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }

@@ -994,6 +994,127 @@ __device__ __forceinline__ int shadow_bin_in_wave(const DevBatch& Q, int first, 
     return (((sid - first) & 7) << 18) | cell_bits(Q.scenes[sid], o, 18);
 }
 
+// One ray's shading at one bounce: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
+// roulette, material sampling and the next ray (GRK:3185-3686). `o4`, `d4` are the ray (path id in
+// o4.w), `hr` its closest hit; the path's state (throughput, radiance, RNG) is read and written in
+// place. Returns the next ray in (emit_next, no, nd) and the sun shadow ray in (emit_shadow, so,
+// sd, sc); the caller queues them.
+template <bool BATCH>
+__device__ __forceinline__ void shade_ray(const DevScene& S0, const DevParams* __restrict__ Pp, DevPass& B, const DevBatch& Q, int bounce,
+                                          uint32_t pass, const float4 o4, const float4 d4, const int4 hr, int& path, bool& emit_next,
+                                          float4& no, float4& nd, bool& emit_shadow, float4& so, float4& sd, float4& sc) {
+    path = __float_as_int(o4.w);
+    const int sid = BATCH ? __float_as_int(d4.w) : 0;
+    const float sid_bits = BATCH ? d4.w : 0.0f;
+    const DevScene& S = scene_of<BATCH>(S0, Q, sid);
+    const DevParams& P = params_of<BATCH>(Pp, Q, sid);
+    uint32_t rng_pixel = (uint32_t)(BATCH ? path : pixel_of_slot(P, path)), rng_pass = pass;
+    if constexpr (BATCH) {
+#ifdef DFPT_ONE_SCENE
+        // One scene: the slot's pixel and pass follow from its index as k_camera derived
+        // them (slot i of the wave is sample base + i), without the random slot-key load.
+        const long long np = (long long)P.width * P.height;
+        const long long local = Q.wave_base[0] + rel_of_slot((unsigned)path, (unsigned)np, wave_passes(Q, np)) - Q.sample_begin[0];
+        if (local < 0x7FFFFFFFll) {
+            const unsigned q = (unsigned)local / (unsigned)np;
+            rng_pixel = (unsigned)local - q * (unsigned)np;
+            rng_pass = (uint32_t)(q + Q.wave_base[2]);
+        } else {
+            const long long j = local / np;
+            rng_pixel = (uint32_t)(local - j * np);
+            rng_pass = (uint32_t)(j + Q.wave_base[2]);
+        }
+#else
+        const int4 key = Q.slot_key[path];
+        rng_pixel = (uint32_t)key.y;
+        rng_pass = (uint32_t)key.z;
+#endif
+    }
+    Hit h;
+    h.t = __int_as_float(hr.x);
+    h.prim = hr.y;
+    h.shape_type = hr.z;
+    h.shape_offset = hr.w;
+    const bool fresh = bounce == 0 && lean_start<BATCH>(P);
+    float4 T = fresh ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : B.throughput[PSI(path)];
+    float4 L = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : B.radiance[PSI(path)];
+    if (!BATCH && bounce == 0) B.primitive_offsets[rng_pixel] = h.prim >= 0 ? h.prim * 3 : -1;
+    // A handle's waves of passes: the selection buffer holds the first hits of the call's
+    // last pass (wave record entry 4; batches of scenes have no selection buffer).
+    if (BATCH && bounce == 0 && B.primitive_offsets != nullptr && (long long)rng_pass == Q.wave_base[4])
+        B.primitive_offsets[rng_pixel] = h.prim >= 0 ? h.prim * 3 : -1;
+    if (h.t == INF || h.prim == -1) {
+        const float3 sky = sky_color(P, d4.x, d4.y, d4.z);
+        L.x += T.x * sky.x * INV_PI;
+        L.y += T.y * sky.y * INV_PI;
+        L.z += T.z * sky.z * INV_PI;
+        B.radiance[PSI(path)] = L;
+        if (!BATCH && bounce == 0 && P.record_hits) {
+            B.hit_prim_offset[rng_pixel] = -1; B.hit_shape_type[rng_pixel] = -1; B.hit_shape_offset[rng_pixel] = -1;
+            B.hit_distance[rng_pixel] = INF;
+        }
+    } else {
+        Rng rng = make_rng(P, rng_pixel, rng_pass, fresh ? (uint64_t)camera_draws(S, P) : B.rng[path]);
+        const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
+        if (!BATCH && bounce == 0 && P.record_hits) {
+            const uint32_t px = rng_pixel;
+            B.hit_prim_offset[px] = h.prim * 3; B.hit_shape_type[px] = h.shape_type; B.hit_shape_offset[px] = h.shape_offset;
+            B.hit_distance[px] = h.t;
+            B.hit_normal[3 * px] = s.nx; B.hit_normal[3 * px + 1] = s.ny; B.hit_normal[3 * px + 2] = s.nz;
+        }
+        const int so_off = __ldg(S.prim_info + h.prim).z;
+        const float dp = s.nx * d4.x + s.ny * d4.y + s.nz * d4.z;
+        const float dp2 = dp * 2.0f;
+        const bool correct = dp < 0.0f;
+        const float wx = correct ? s.nx : -s.nx, wy = correct ? s.ny : -s.ny, wz = correct ? s.nz : -s.nz;
+        const int albedo = texture_color(S, f2i(__ldg(S.surfaces + so_off + 1)), s);
+        const int emission = texture_color(S, f2i(__ldg(S.surfaces + so_off + 2)), s);
+        float ar = cr(albedo), ag = cg(albedo), ab = cb(albedo);
+        float er = cr(emission), eg = cg(emission), eb = cb(emission);
+        const int material = f2i(__ldg(S.surfaces + so_off + 0));
+        float exponent = 50.0f;  // the reference's fixed Phong exponent (GRK:3524)
+        if (S.prim_ext) primitive_extension(S, h.prim, er, eg, eb, exponent);
+        if (P.diff) diff_surface(P, h.prim, ar, ag, ab, er, eg, eb, exponent);
+        if ((material == DFPT_MATERIAL_CLEAR_COAT || material == DFPT_MATERIAL_LAMBERTIAN || material == DFPT_MATERIAL_PHONG) &&
+            P.sun_active == 1) {
+            const float u = rng.next(), v = rng.next();
+            float lx, ly, lz, dot1;
+            if (sun_sample(P, s.px, s.py, s.pz, wx, wy, wz, u, v, lx, ly, lz, dot1)) {
+                emit_shadow = true;
+                so = make_float4(s.px, s.py, s.pz, __int_as_float(path));
+                sd = make_float4(lx, ly, lz, sid_bits);
+                sc = make_float4(T.x * (ar * 1.0f * dot1 * INV_PI), T.y * (ag * 1.0f * dot1 * INV_PI), T.z * (ab * 1.0f * dot1 * INV_PI),
+                                 __int_as_float(bounce));
+            }
+        }
+        L.x += T.x * er;
+        L.y += T.y * eg;
+        L.z += T.z * eb;
+        const int depth = bounce + 1;
+        bool alive = true;
+        if (depth >= P.depth_rr) {
+            const float q = jmax(ar, jmax(ag, ab));
+            const float r = rng.next();
+            // The reference then tests the same ray for any hit; it just hit, so the
+            // test always hits and adds no sky (GRK:3293-3311).
+            if (r >= q) alive = false;
+            else {
+                const float qr = 1.0f / q;
+                ar *= qr; ag *= qr; ab *= qr;
+            }
+        }
+        if (alive) {
+            const Scatter sct = scatter(s, material, wx, wy, wz, o4, d4, dp2, ar, ag, ab, exponent, rng, T);
+            emit_next = true;
+            no = make_float4(sct.o.x, sct.o.y, sct.o.z, __int_as_float(path));
+            nd = make_float4(sct.d.x, sct.d.y, sct.d.z, sid_bits);
+        }
+        B.throughput[PSI(path)] = T;
+        B.radiance[PSI(path)] = L;
+        B.rng[path] = rng.state;
+    }
+}
+
 // One bounce of shading: miss -> sky; hit -> emission, sun sample (a shadow ray), Russian
 // roulette, material sampling and the next ray (GRK:3185-3686).
 template <bool BATCH>
@@ -1009,120 +1130,8 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
         float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
         float4 so = make_float4(0, 0, 0, 0), sd = make_float4(0, 0, 0, 0), sc = make_float4(0, 0, 0, 0);
         int path = 0;
-        if (i < n) {
-            const float4 o4 = B.q_o[qi][i], d4 = B.q_d[qi][i];
-            path = __float_as_int(o4.w);
-            const int sid = BATCH ? __float_as_int(d4.w) : 0;
-            const float sid_bits = BATCH ? d4.w : 0.0f;
-            const DevScene& S = scene_of<BATCH>(S0, Q, sid);
-            const DevParams& P = params_of<BATCH>(Pp, Q, sid);
-            uint32_t rng_pixel = (uint32_t)(BATCH ? path : pixel_of_slot(P, path)), rng_pass = pass;
-            if constexpr (BATCH) {
-#ifdef DFPT_ONE_SCENE
-                // One scene: the slot's pixel and pass follow from its index as k_camera derived
-                // them (slot i of the wave is sample base + i), without the random slot-key load.
-                const long long np = (long long)P.width * P.height;
-                const long long local = Q.wave_base[0] + rel_of_slot((unsigned)path, (unsigned)np, wave_passes(Q, np)) - Q.sample_begin[0];
-                if (local < 0x7FFFFFFFll) {
-                    const unsigned q = (unsigned)local / (unsigned)np;
-                    rng_pixel = (unsigned)local - q * (unsigned)np;
-                    rng_pass = (uint32_t)(q + Q.wave_base[2]);
-                } else {
-                    const long long j = local / np;
-                    rng_pixel = (uint32_t)(local - j * np);
-                    rng_pass = (uint32_t)(j + Q.wave_base[2]);
-                }
-#else
-                const int4 key = Q.slot_key[path];
-                rng_pixel = (uint32_t)key.y;
-                rng_pass = (uint32_t)key.z;
-#endif
-            }
-            const int4 hr = B.q_hit[i];
-            Hit h;
-            h.t = __int_as_float(hr.x);
-            h.prim = hr.y;
-            h.shape_type = hr.z;
-            h.shape_offset = hr.w;
-            const bool fresh = bounce == 0 && lean_start<BATCH>(P);
-            float4 T = fresh ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : B.throughput[PSI(path)];
-            float4 L = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : B.radiance[PSI(path)];
-            if (!BATCH && bounce == 0) B.primitive_offsets[rng_pixel] = h.prim >= 0 ? h.prim * 3 : -1;
-            // A handle's waves of passes: the selection buffer holds the first hits of the call's
-            // last pass (wave record entry 4; batches of scenes have no selection buffer).
-            if (BATCH && bounce == 0 && B.primitive_offsets != nullptr && (long long)rng_pass == Q.wave_base[4])
-                B.primitive_offsets[rng_pixel] = h.prim >= 0 ? h.prim * 3 : -1;
-            if (h.t == INF || h.prim == -1) {
-                const float3 sky = sky_color(P, d4.x, d4.y, d4.z);
-                L.x += T.x * sky.x * INV_PI;
-                L.y += T.y * sky.y * INV_PI;
-                L.z += T.z * sky.z * INV_PI;
-                B.radiance[PSI(path)] = L;
-                if (!BATCH && bounce == 0 && P.record_hits) {
-                    B.hit_prim_offset[rng_pixel] = -1; B.hit_shape_type[rng_pixel] = -1; B.hit_shape_offset[rng_pixel] = -1;
-                    B.hit_distance[rng_pixel] = INF;
-                }
-            } else {
-                Rng rng = make_rng(P, rng_pixel, rng_pass, fresh ? (uint64_t)camera_draws(S, P) : B.rng[path]);
-                const Surf s = surface(S, P, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, h);
-                if (!BATCH && bounce == 0 && P.record_hits) {
-                    const uint32_t px = rng_pixel;
-                    B.hit_prim_offset[px] = h.prim * 3; B.hit_shape_type[px] = h.shape_type; B.hit_shape_offset[px] = h.shape_offset;
-                    B.hit_distance[px] = h.t;
-                    B.hit_normal[3 * px] = s.nx; B.hit_normal[3 * px + 1] = s.ny; B.hit_normal[3 * px + 2] = s.nz;
-                }
-                const int so_off = __ldg(S.prim_info + h.prim).z;
-                const float dp = s.nx * d4.x + s.ny * d4.y + s.nz * d4.z;
-                const float dp2 = dp * 2.0f;
-                const bool correct = dp < 0.0f;
-                const float wx = correct ? s.nx : -s.nx, wy = correct ? s.ny : -s.ny, wz = correct ? s.nz : -s.nz;
-                const int albedo = texture_color(S, f2i(__ldg(S.surfaces + so_off + 1)), s);
-                const int emission = texture_color(S, f2i(__ldg(S.surfaces + so_off + 2)), s);
-                float ar = cr(albedo), ag = cg(albedo), ab = cb(albedo);
-                float er = cr(emission), eg = cg(emission), eb = cb(emission);
-                const int material = f2i(__ldg(S.surfaces + so_off + 0));
-                float exponent = 50.0f;  // the reference's fixed Phong exponent (GRK:3524)
-                if (S.prim_ext) primitive_extension(S, h.prim, er, eg, eb, exponent);
-                if (P.diff) diff_surface(P, h.prim, ar, ag, ab, er, eg, eb, exponent);
-                if ((material == DFPT_MATERIAL_CLEAR_COAT || material == DFPT_MATERIAL_LAMBERTIAN || material == DFPT_MATERIAL_PHONG) &&
-                    P.sun_active == 1) {
-                    const float u = rng.next(), v = rng.next();
-                    float lx, ly, lz, dot1;
-                    if (sun_sample(P, s.px, s.py, s.pz, wx, wy, wz, u, v, lx, ly, lz, dot1)) {
-                        emit_shadow = true;
-                        so = make_float4(s.px, s.py, s.pz, __int_as_float(path));
-                        sd = make_float4(lx, ly, lz, sid_bits);
-                        sc = make_float4(T.x * (ar * 1.0f * dot1 * INV_PI), T.y * (ag * 1.0f * dot1 * INV_PI), T.z * (ab * 1.0f * dot1 * INV_PI),
-                                         __int_as_float(bounce));
-                    }
-                }
-                L.x += T.x * er;
-                L.y += T.y * eg;
-                L.z += T.z * eb;
-                const int depth = bounce + 1;
-                bool alive = true;
-                if (depth >= P.depth_rr) {
-                    const float q = jmax(ar, jmax(ag, ab));
-                    const float r = rng.next();
-                    // The reference then tests the same ray for any hit; it just hit, so the
-                    // test always hits and adds no sky (GRK:3293-3311).
-                    if (r >= q) alive = false;
-                    else {
-                        const float qr = 1.0f / q;
-                        ar *= qr; ag *= qr; ab *= qr;
-                    }
-                }
-                if (alive) {
-                    const Scatter sct = scatter(s, material, wx, wy, wz, o4, d4, dp2, ar, ag, ab, exponent, rng, T);
-                    emit_next = true;
-                    no = make_float4(sct.o.x, sct.o.y, sct.o.z, __int_as_float(path));
-                    nd = make_float4(sct.d.x, sct.d.y, sct.d.z, sid_bits);
-                }
-                B.throughput[PSI(path)] = T;
-                B.radiance[PSI(path)] = L;
-                B.rng[path] = rng.state;
-            }
-        }
+        if (i < n) shade_ray<BATCH>(S0, Pp, B, Q, bounce, pass, B.q_o[qi][i], B.q_d[qi][i], B.q_hit[i], path, emit_next, no, nd,
+                                    emit_shadow, so, sd, sc);
         const int slot = warp_push(B.counts + bounce + 1, emit_next);
         if (slot >= 0) {
             B.q_o[qi ^ 1][slot] = no;
@@ -1239,6 +1248,69 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S0, const DevPar
             const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
             if (valid && !(h.t < INF)) escaped(o, d);
             warp_add_stats(P0, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
+        }
+    }
+}
+
+// The last bounces of a plain pass in one launch. Each lane takes a path whose ray waits for bounce
+// b0 and carries it to its end - closest hit, shading, the next ray - through bounces b0 .. nb - 1
+// and the any-hit test of the continuation after the last (k_final). Late bounces hold few rays,
+// and a launch per bounce costs the slowest ray of every bounce; here a warp costs the slowest of
+// its paths' remaining walks. Each path takes exactly the steps of the per-bounce kernels (same
+// hits, same draws, same order of its radiance sums); sun shadow rays join the deferred queue as
+// there. The loop is warp-uniform: every lane calls the traversal and the queue append together.
+template <int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int b0, int nb) {
+    constexpr int TV = V == 3 ? 1 : V;  // the lane-refill walk has its own loop: its per-lane form here
+    const DevParams& P = *Pp;
+    const int n = B.counts[b0];
+    const int qi = b0 & 1;
+    const uint32_t pass = (uint32_t)*B.pass_index;
+    const DevBatch Q{};
+    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + b0) {
+        bool alive = i < n;
+        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+        if (alive) {
+            o = __ldcs(B.q_o[qi] + i);
+            d = __ldcs(B.q_d[qi] + i);
+        }
+        for (int b = b0; b < nb; ++b) {
+            if (!__any_sync(0xFFFFFFFFu, alive)) break;
+            TraceStats st{0, 0};
+            const Hit h = trace_v<false, TV>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            warp_add_stats(P, B.stats, 0, alive ? 1u : 0u, st.nodes, st.tris);
+            bool emit_next = false, emit_shadow = false;
+            float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
+            float4 so = make_float4(0, 0, 0, 0), sd = make_float4(0, 0, 0, 0), sc = make_float4(0, 0, 0, 0);
+            int path = 0;
+            if (alive)
+                shade_ray<false>(S, Pp, B, Q, b, pass, o, d, make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset), path,
+                                 emit_next, no, nd, emit_shadow, so, sd, sc);
+            const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
+            if (sslot >= 0) {
+                B.s_o[sslot] = so;
+                B.s_d[sslot] = sd;
+                B.s_c[sslot] = sc;
+            }
+            alive = emit_next;
+            o = no;
+            d = nd;
+        }
+        // The continuation after the last bounce: any hit, else the sky (GRK:3689-3701).
+        if (__any_sync(0xFFFFFFFFu, alive)) {
+            TraceStats st{0, 0};
+            const Hit h = trace_v<true, TV>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            warp_add_stats(P, B.stats, 1, alive ? 1u : 0u, st.nodes, st.tris);
+            if (alive && !(h.t < INF)) {
+                const int path = __float_as_int(o.w);
+                const float4 T = B.throughput[PSI(path)];
+                const float3 sky = sky_color(P, d.x, d.y, d.z);
+                float4 L = B.radiance[PSI(path)];
+                L.x += T.x * sky.x * INV_PI;
+                L.y += T.y * sky.y * INV_PI;
+                L.z += T.z * sky.z * INV_PI;
+                B.radiance[PSI(path)] = L;
+            }
         }
     }
 }
@@ -1850,6 +1922,19 @@ struct TraceCfg {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<false, false, V, BLOCK, MINB>, BLOCK, 0);
         return sms * (b > 0 ? b : 1);
     }
+    // The tail kernel: traversal and shading in one kernel, compiled for two resident blocks; its
+    // grid (SMs x resident blocks) is found once per process.
+    static void tail(const LaunchCtx& c, int b0, int nb) {
+        static int grid_tail = 0;
+        if (grid_tail == 0) {
+            int dev = 0, sms = 0, b = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tail<V, 256, 2>, 256, 0);
+            grid_tail = (sms > 0 ? sms : 1) * (b > 0 ? b : 1);
+        }
+        k_tail<V, 256, 2><<<grid_tail, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, b0, nb);
+    }
 #endif
 #ifdef DFPT_EXTENDED_KERNELS
     // Batch traversal: per-lane walks only (a warp may hold rays of several scenes).
@@ -1888,6 +1973,14 @@ static void launch_shadow(const LaunchCtx& c, int bounce) {
         TRACE_CONFIGS(X)
 #undef X
         default: TraceCfg<0, 256, 4>::shadow(c, bounce);
+    }
+}
+static void launch_tail(const LaunchCtx& c, int b0, int nb) {
+    switch (c.trace_config) {
+#define X(id, v, b, m) case id: TraceCfg<v, b, m>::tail(c, b0, nb); break;
+        TRACE_CONFIGS(X)
+#undef X
+        default: TraceCfg<0, 256, 4>::tail(c, b0, nb);
     }
 }
 static void launch_final(const LaunchCtx& c, int bounce) {
@@ -2021,6 +2114,7 @@ KernelSet kernel_set() {
     k.shade = launch_shade;
     k.shadow = launch_shadow;
     k.final_ = launch_final;
+    k.tail = launch_tail;
     k.simple = launch_simple;
     k.wireframe = launch_wireframe;
     k.film = launch_film;

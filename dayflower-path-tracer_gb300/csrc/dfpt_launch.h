@@ -24,6 +24,7 @@ struct KernelSet {
     void (*shade)(const LaunchCtx&, int bounce);
     void (*shadow)(const LaunchCtx&, int bounce);
     void (*final_)(const LaunchCtx&, int bounce);
+    void (*tail)(const LaunchCtx&, int first_bounce, int bounces) = nullptr;  // bounces first .. bounces-1 + the final any-hit
     void (*simple)(const LaunchCtx&);
     void (*wireframe)(const LaunchCtx&);
     void (*film)(const LaunchCtx&);

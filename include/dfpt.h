@@ -232,6 +232,11 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       access-policy window on the handle's stream; 0 turns it off;
  *   "wide_samples"      passes per wave when dfpt_render renders several passes (1..64, default
  *                       8; 1 renders pass by pass); the film is the same either way;
+ *   "pixel_tiles"       1 (default) runs a plain pass's queue slots over 8 x 4 pixel tiles (a warp's
+ *                       primary rays leave a compact block of pixels; width a multiple of 8, height
+ *                       of 4, counter-based RNG, path tracer without wireframes), 0 in row order;
+ *   "tail_bounce"       t >= 1: a plain pass runs bounces t .. depth-1 and the final any-hit of each
+ *                       path in one launch (same steps per path); 0 (default) a launch per bounce;
  *   "ray_sort"          1 (default) bins rays by direction and origin cell between the bounces of
  *                       wide passes (processing order only);
  *   "shadow_sort"       with ray_sort, 1 (default) also bins the sun shadow rays by origin cell
