@@ -163,3 +163,24 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbos
     return {"best": best, "ms_per_step": {str(k): round(v, 3) for k, v in results.items()},
             "ray_sort": kernel.get_tuning("ray_sort"), "sort_ms_per_step": {str(k): round(v, 3) for k, v in sort.items()},
             "shadow_defer": kernel.get_tuning("shadow_defer"), "defer_ms_per_step": {str(k): round(v, 3) for k, v in defer.items()}}
+
+
+def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), verbose: bool = False) -> dict:
+    """Picks the tail launch for one-pass calls (the interactive frame loop): times `frames` calls of
+    dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and sets the fastest.
+    Every candidate gives each path the same steps; only the launch structure changes."""
+    results = {}
+    for t in candidates:
+        kernel.set_tuning("tail_bounce", t)
+        kernel.execute(1)
+        kernel.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            kernel.execute(1)
+        kernel.synchronize()
+        results[t] = (time.perf_counter() - t0) / frames * 1e3
+        if verbose:
+            print(f"tail_bounce {t}: {results[t]:.3f} ms/frame", flush=True)
+    best = min(results, key=results.get)
+    kernel.set_tuning("tail_bounce", best)
+    return {"tail_bounce": best, "ms_per_frame": results}
