@@ -682,7 +682,12 @@ def main():
         k.get(host_img)
     barrier()
     e2e_s = time.perf_counter() - t0
-    # The interactive loop: one pass per call, as many frames as one step has passes.
+    # The interactive loop: one pass per call, as many frames as one step has passes (the tail
+    # launch for one-pass calls picked first, outside the timed frames).
+    from dfpt.autotune import tune_frame
+
+    frame_tuning = tune_frame(k)
+    k_pixel_tiles = k.get_tuning("pixel_tiles")
     fl_s = frame_loop(k, cam, host_img, S, max(3, args.warmup), barrier)
     if dist is not None:
         t = torch.tensor([e2e_s, fl_s], device="cuda")
@@ -761,7 +766,9 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 19 * 4, "d2h_bytes_per_step": n_pix * 4,
                 "loop": "dfpt_set_camera(pinned host) + dfpt_render(S passes) + dfpt_read_bgra8(pinned host) per step"},
         "frame_loop": {"value": fl_value, "unit": UNIT, "frames": S, "ms_per_frame": fl_s / S * 1e3,
-                       "fraction_of_value": fl_value / value,
+                       "fraction_of_value": fl_value / value, "tail_bounce": frame_tuning["tail_bounce"],
+                       "tail_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["ms_per_frame"].items()},
+                       "pixel_tiles": k_pixel_tiles,
                        "loop": "per frame: dfpt_set_camera(pinned host) + dfpt_render(1 pass) + dfpt_read_bgra8(pinned host), "
                                "as DayflowerApplication's execute/get loop"},
         "gpu_launches": int(launches),

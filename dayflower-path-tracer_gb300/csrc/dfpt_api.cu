@@ -465,7 +465,6 @@ struct dfpt_handle {
     int wide_samples = 8;
     bool pixel_tiles = true;   // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
     int tail_bounce = 0;       // plain passes: first bounce of the tail launch (0: a launch per bounce)
-    int wave_tail_bounce = 0;  // waves of passes: first bounce of the tail launch (0: a launch per bounce)
     int wide_capacity = 0;
     size_t wide_shadow = 0;
     DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput;  // w_throughput: throughput + radiance records (PSI)
@@ -907,20 +906,13 @@ int issue_wide_wave(dfpt_handle* h) {
         }
         mark(h, KIND_END); K.b_shadow_reset(c, 0); ++k;
     };
-    // With wave_tail_bounce t, bounces t .. nb - 1 and the final any-hit run in one tail launch
-    // (its shadow rays queued when they are deferred, else traced inline).
-    const int tb = (h->wave_tail_bounce >= 1 && h->wave_tail_bounce < nb && K.b_tail) ? h->wave_tail_bounce : nb;
-    for (int b = 0; b < tb; ++b) {
+    for (int b = 0; b < nb; ++b) {
         mark(h, KIND_TRACE); K.b_trace_closest(c, b); ++k;
         mark(h, KIND_SHADE); K.b_shade(c, b); ++k;
         if (h->wpass.sorted_queues) { mark(h, KIND_SORT); k += K.b_sort(c, b, true); }
         if (!h->shadow_defer) shadows();
     }
-    if (tb < nb) {
-        mark(h, KIND_TRACE); K.b_tail(c, tb, nb, h->shadow_defer ? 0 : 1); ++k;
-    } else {
-        mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
-    }
+    mark(h, KIND_FINAL); K.b_final(c, nb); ++k;
     if (h->shadow_defer) shadows();
     mark(h, KIND_FILM); K.b_film(c, 0); ++k;
     mark(h, KIND_END); K.b_end(c, 0); ++k;
@@ -1571,12 +1563,6 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->graph_valid = false;
         return DFPT_OK;
     }
-    if (std::strcmp(key, "wave_tail_bounce") == 0) {
-        if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "wave_tail_bounce %d outside [0, %d]", value, DFPT_MAX_DEPTH);
-        h->wave_tail_bounce = value;
-        h->wide_graph_valid = false;
-        return DFPT_OK;
-    }
     if (std::strcmp(key, "primitive_culling") == 0) {
         if (value < 0 || value > 2) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "primitive_culling %d: 0 none, 1 box test, 2 BVH", value);
         scene_set_culling(h->sc, value);
@@ -1597,7 +1583,6 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "pixel_tiles") == 0) { *value = h->pixel_tiles ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "tail_bounce") == 0) { *value = h->tail_bounce; return DFPT_OK; }
-    if (std::strcmp(key, "wave_tail_bounce") == 0) { *value = h->wave_tail_bounce; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }

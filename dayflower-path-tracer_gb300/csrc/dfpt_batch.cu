@@ -56,7 +56,6 @@ struct dfpt_batch {
     DevBatch Q{};
     LaunchCtx ctx{};
     int trace_config = DFPT_DEFAULT_TRACE_CONFIG;
-    int tail_bounce = 0;  // first bounce of the tail launch (0: a launch per bounce)
     bool use_graph = true;
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -220,10 +219,7 @@ int issue_wave(dfpt_batch* b) {
     cudaMemsetAsync(b->counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), b->stream);
     K.b_wave(c, 0); ++k;
     K.b_camera(c, 0); ++k;
-    // With tail_bounce t, bounces t .. depth - 1 and the final any-hit run in one tail launch whose
-    // lanes trace their sun shadow rays inline.
-    const int tb = (b->tail_bounce >= 1 && b->tail_bounce < b->depth && K.b_tail) ? b->tail_bounce : b->depth;
-    for (int i = 0; i < tb; ++i) {
+    for (int i = 0; i < b->depth; ++i) {
         K.b_trace_closest(c, i); ++k;
         K.b_shade(c, i); ++k;
         if (b->pass.sorted_queues) k += K.b_sort(c, i, true);
@@ -237,11 +233,7 @@ int issue_wave(dfpt_batch* b) {
             K.b_shadow_reset(c, 0); ++k;
         }
     }
-    if (tb < b->depth) {
-        K.b_tail(c, tb, b->depth, 1); ++k;
-    } else {
-        K.b_final(c, b->depth); ++k;
-    }
+    K.b_final(c, b->depth); ++k;
     K.b_film(c, 0); ++k;
     K.b_end(c, 0); ++k;
     return k;
@@ -371,9 +363,6 @@ int dfpt_batch_set_tuning(dfpt_batch* b, const char* key, int64_t value) {
         b->use_graph = value != 0;
     } else if (k == "ray_sort") {
         b->ray_sort = value != 0;
-    } else if (k == "tail_bounce") {
-        if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %lld outside [0, %d]", (long long)value, DFPT_MAX_DEPTH);
-        b->tail_bounce = (int)value;
     } else {
         return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
     }
@@ -389,7 +378,6 @@ int dfpt_batch_get_tuning(dfpt_batch* b, const char* key, int64_t* value) {
     else if (k == "trace_configs") *value = b->ks.trace_configs;
     else if (k == "graphs") *value = b->use_graph ? 1 : 0;
     else if (k == "ray_sort") *value = b->ray_sort ? 1 : 0;
-    else if (k == "tail_bounce") *value = b->tail_bounce;
     else if (k == "scenes") *value = (int64_t)b->stores.size();
     else if (k == "total_samples") *value = total_samples(b);
     else if (k == "depth") *value = b->depth;

@@ -1252,23 +1252,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S0, const DevPar
     }
 }
 
-// The last bounces of a pass or a wave in one launch. Each lane takes a path whose ray waits for
-// bounce b0 and carries it to its end - closest hit, shading, the next ray - through bounces
-// b0 .. nb - 1 and the any-hit test of the continuation after the last (k_final). Late bounces
-// hold few rays, and a launch per bounce costs the slowest ray of every bounce; here a warp costs
-// the slowest of its paths' remaining walks. Each path takes exactly the steps of the per-bounce
-// kernels (same hits, same draws). Sun shadow rays either join the deferred queue (binned when the
-// wave bins them) or, with inline_shadow, are traced right after their shading and added to the
-// path's radiance, as a per-bounce shadow launch does before the next bounce. The loop is
-// warp-uniform: every lane calls the traversals, the bin counts and the queue append together.
-template <bool BATCH, int V, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int b0, int nb,
-                                                      int inline_shadow) {
-    constexpr int TV = V;
-    const DevParams& P0 = *Pp;  // run-wide flags (statistics counting)
+// The last bounces of a plain pass in one launch. Each lane takes a path whose ray waits for bounce
+// b0 and carries it to its end - closest hit, shading, the next ray - through bounces b0 .. nb - 1
+// and the any-hit test of the continuation after the last (k_final). Late bounces hold few rays,
+// and a launch per bounce costs the slowest ray of every bounce; here a warp costs the slowest of
+// its paths' remaining walks. Each path takes exactly the steps of the per-bounce kernels (same
+// hits, same draws, same order of its radiance sums); sun shadow rays join the deferred queue as
+// there. The loop is warp-uniform: every lane calls the traversal and the queue append together.
+template <int V, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int b0, int nb) {
+    const DevParams& P = *Pp;
     const int n = B.counts[b0];
-    const int qi = B.sorted_queues ? 0 : (b0 & 1);
-    const uint32_t pass = BATCH ? 0u : (uint32_t)*B.pass_index;
+    const int qi = b0 & 1;
+    const uint32_t pass = (uint32_t)*B.pass_index;
+    const DevBatch Q{};
     WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + b0) {
         bool alive = i < n;
         float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
@@ -1278,40 +1275,21 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S0, const DevPara
         }
         for (int b = b0; b < nb; ++b) {
             if (!__any_sync(0xFFFFFFFFu, alive)) break;
-            const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
             TraceStats st{0, 0};
-            const Hit h = trace_v<false, TV>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            warp_add_stats(P0, B.stats, 0, alive ? 1u : 0u, st.nodes, st.tris);
+            const Hit h = trace_v<false, V>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            warp_add_stats(P, B.stats, 0, alive ? 1u : 0u, st.nodes, st.tris);
             bool emit_next = false, emit_shadow = false;
             float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
             float4 so = make_float4(0, 0, 0, 0), sd = make_float4(0, 0, 0, 0), sc = make_float4(0, 0, 0, 0);
             int path = 0;
             if (alive)
-                shade_ray<BATCH>(S0, Pp, B, Q, b, pass, o, d, make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset), path,
+                shade_ray<false>(S, Pp, B, Q, b, pass, o, d, make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset), path,
                                  emit_next, no, nd, emit_shadow, so, sd, sc);
-            if (inline_shadow) {
-                TraceStats ss{0, 0};
-                const Hit hs = trace_v<true, TV>(S, emit_shadow, so.x, so.y, so.z, sd.x, sd.y, sd.z, ss);
-                warp_add_stats(P0, B.stats, 1, emit_shadow ? 1u : 0u, ss.nodes, ss.tris);
-                if (emit_shadow && hs.t >= INF - 0.0001f) {
-                    float4 L = B.radiance[PSI(path)];
-                    L.x += sc.x;
-                    L.y += sc.y;
-                    L.z += sc.z;
-                    B.radiance[PSI(path)] = L;
-                    if (params_of<BATCH>(Pp, Q, BATCH ? __float_as_int(sd.w) : 0).diff) B.vis[path] |= 1 << __float_as_int(sc.w);
-                }
-            } else {
-                if constexpr (BATCH) {
-                    if (B.sorted_queues && B.sort_count_shadow)
-                        bin_count(B.sort_count_shadow, emit_shadow ? shadow_bin_in_wave(Q, wave_first_scene(Q), so, sd) : -1);
-                }
-                const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
-                if (sslot >= 0) {
-                    B.s_o[sslot] = so;
-                    B.s_d[sslot] = sd;
-                    B.s_c[sslot] = sc;
-                }
+            const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
+            if (sslot >= 0) {
+                B.s_o[sslot] = so;
+                B.s_d[sslot] = sd;
+                B.s_c[sslot] = sc;
             }
             alive = emit_next;
             o = no;
@@ -1319,13 +1297,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S0, const DevPara
         }
         // The continuation after the last bounce: any hit, else the sky (GRK:3689-3701).
         if (__any_sync(0xFFFFFFFFu, alive)) {
-            const int sid = BATCH ? __float_as_int(d.w) : 0;
-            const DevScene& S = scene_of<BATCH>(S0, Q, sid);
             TraceStats st{0, 0};
-            const Hit h = trace_v<true, TV>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            warp_add_stats(P0, B.stats, 1, alive ? 1u : 0u, st.nodes, st.tris);
+            const Hit h = trace_v<true, V>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            warp_add_stats(P, B.stats, 1, alive ? 1u : 0u, st.nodes, st.tris);
             if (alive && !(h.t < INF)) {
-                const DevParams& P = params_of<BATCH>(Pp, Q, sid);
                 const int path = __float_as_int(o.w);
                 const float4 T = B.throughput[PSI(path)];
                 const float3 sky = sky_color(P, d.x, d.y, d.z);
@@ -1958,10 +1933,10 @@ struct TraceCfg {
             int dev = 0, sms = 0, b = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tail<false, TVV, 256, 2>, 256, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tail<TVV, 256, 2>, 256, 0);
             grid_tail = (sms > 0 ? sms : 1) * (b > 0 ? b : 1);
         }
-        k_tail<false, TVV, 256, 2><<<grid_tail, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, DevBatch{}, b0, nb, 0);
+        k_tail<TVV, 256, 2><<<grid_tail, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, b0, nb);
     }
 #endif
 #ifdef DFPT_EXTENDED_KERNELS
@@ -1975,18 +1950,6 @@ struct TraceCfg {
     }
     static void b_final(const LaunchCtx& c, int bounce) {
         k_final<true, BV, BLOCK, MINB><<<c.grid_trace, BLOCK, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch, bounce);
-    }
-    static constexpr int BTV = (V == 0 || V == 5) ? V : 1;  // as TVV
-    static void b_tail(const LaunchCtx& c, int b0, int nb, int inline_shadow) {
-        static int grid_tail = 0;
-        if (grid_tail == 0) {
-            int dev = 0, sms = 0, b = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tail<true, BTV, 256, 2>, 256, 0);
-            grid_tail = (sms > 0 ? sms : 1) * (b > 0 ? b : 1);
-        }
-        k_tail<true, BTV, 256, 2><<<grid_tail, 256, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch, b0, nb, inline_shadow);
     }
 #ifdef DFPT_ONE_SCENE
     static int grid(int sms) {
@@ -2068,14 +2031,6 @@ static void launch_shade(const LaunchCtx& c, int bounce) { k_shade<false><<<c.gr
 BATCH_DISPATCH(closest)
 BATCH_DISPATCH(shadow)
 BATCH_DISPATCH(final)
-static void launch_b_tail(const LaunchCtx& c, int b0, int nb, int inline_shadow) {
-    switch (c.trace_config) {
-#define X(id, v, b, m) case id: TraceCfg<v, b, m>::b_tail(c, b0, nb, inline_shadow); break;
-        TRACE_CONFIGS(X)
-#undef X
-        default: TraceCfg<0, 256, 4>::b_tail(c, b0, nb, inline_shadow);
-    }
-}
 #undef BATCH_DISPATCH
 #undef BATCH_CASE_closest
 #undef BATCH_CASE_shadow
@@ -2183,7 +2138,6 @@ KernelSet kernel_set() {
     k.b_shade = launch_b_shade;
     k.b_shadow = launch_b_shadow;
     k.b_final = launch_b_final;
-    k.b_tail = launch_b_tail;
     k.b_wave = launch_b_wave;
     k.b_film = launch_b_film;
     k.b_resolve = launch_b_resolve;

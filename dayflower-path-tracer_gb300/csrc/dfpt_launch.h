@@ -44,8 +44,6 @@ struct KernelSet {
     void (*b_shade)(const LaunchCtx&, int) = nullptr;
     void (*b_shadow)(const LaunchCtx&, int) = nullptr;
     void (*b_final)(const LaunchCtx&, int) = nullptr;
-    // Bounces first .. bounces-1 + the final any-hit in one launch; shadow rays traced inline (1) or queued (0).
-    void (*b_tail)(const LaunchCtx&, int first_bounce, int bounces, int inline_shadow) = nullptr;
     void (*b_wave)(const LaunchCtx&, int) = nullptr;
     void (*b_film)(const LaunchCtx&, int) = nullptr;
     void (*b_resolve)(const LaunchCtx&, int) = nullptr;

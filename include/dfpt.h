@@ -237,8 +237,6 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       of 4, counter-based RNG, path tracer without wireframes), 0 in row order;
  *   "tail_bounce"       t >= 1: a plain pass runs bounces t .. depth-1 and the final any-hit of each
  *                       path in one launch (same steps per path); 0 (default) a launch per bounce;
- *   "wave_tail_bounce"  the same for the waves of passes of a multi-pass dfpt_render (their shadow
- *                       rays queued when deferred, else traced inline); 0 (default) off;
  *   "ray_sort"          1 (default) bins rays by direction and origin cell between the bounces of
  *                       wide passes (processing order only);
  *   "shadow_sort"       with ray_sort, 1 (default) also bins the sun shadow rays by origin cell
@@ -368,10 +366,8 @@ int dfpt_batch_add(dfpt_batch* batch, const dfpt_scene_desc* scene, const dfpt_s
                    const dfpt_params* params, int32_t width, int32_t height, int32_t spp, int32_t* index);
 int dfpt_batch_set_stream(dfpt_batch* batch, void* cuda_stream);
 /* Keys: "wave_capacity" (path slots per wave, 1024..2^27), "trace_config" (traversal launch
- * configuration, as dfpt_set_tuning), "graphs" (0/1), "ray_sort" (0/1), "tail_bounce" (t >= 1:
- * bounces t .. depth-1 and the final any-hit of every path in one launch, its sun shadow rays
- * traced inline; 0 a launch per bounce). Read-only for get: "trace_configs", "scenes",
- * "total_samples", "depth". */
+ * configuration, as dfpt_set_tuning), "graphs" (0/1), "ray_sort" (0/1). Read-only for get:
+ * "trace_configs", "scenes", "total_samples", "depth". */
 int dfpt_batch_set_tuning(dfpt_batch* batch, const char* key, int64_t value);
 int dfpt_batch_get_tuning(dfpt_batch* batch, const char* key, int64_t* value);
 /* Clears every film, renders all samples of all scenes, tone maps the images (asynchronous). */

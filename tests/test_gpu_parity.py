@@ -232,16 +232,15 @@ def test_wide_passes_equal_pass_by_pass(scenes, name):
     film of n single passes: same samples per pixel, same Kahan order; float atomics of the sun
     contributions leave a few ulps (rtol 1e-5). A clear between calls restarts both the same way;
     the selection buffer and the image come from the last (normal) pass in both. The same holds
-    with deferred shadow rays and with the wave's late bounces in one tail launch."""
+    with the shadow rays of all bounces deferred to one launch."""
     scene, sky, params, (w, h) = scenes[name]
     out = []
-    # (passes per wave, ray binning, deferred shadow rays, first bounce of the wave's tail launch)
-    for wide, sort, defer, tail in ((1, 0, 0, 0), (8, 1, 0, 0), (8, 0, 0, 0), (8, 1, 1, 2), (8, 1, 0, 1), (8, 0, 1, 3)):
+    # (passes per wave, ray binning, deferred shadow rays)
+    for wide, sort, defer in ((1, 0, 0), (8, 1, 0), (8, 0, 0), (8, 1, 1), (8, 0, 1)):
         k = _kernel(scene, sky, dict(params, renderer_type=2), w, h)
         k.set_tuning("wide_samples", wide)
         k.set_tuning("ray_sort", sort)
         k.set_tuning("shadow_defer", defer)
-        k.set_tuning("wave_tail_bounce", tail)
         k.execute(13)
         k.clear()
         k.execute(11)
