@@ -301,6 +301,7 @@ def batch_leg(args, stream, torch, barrier, dist, world):
     barrier()
     for k in handles:
         k.set_tuning("wide_samples", 8)
+        k.set_tuning("shadow_defer", tuning["best"].get("shadow_defer", 0))  # the batch's shadow schedule
         k.execute(9)  # builds the wave graph
     torch.cuda.synchronize()
     barrier()
@@ -334,7 +335,8 @@ def batch_leg(args, stream, torch, barrier, dist, world):
         "speedup_vs_sequential": seq_s / batch_s, "samples": samples,
         "sequential_wide_value": world * n / seq_wide_s, "speedup_vs_sequential_wide": seq_wide_s / batch_s,
         "sequential": "64 RendererKernel handles on one stream, clear + dfpt_render(spp) each: pass by pass "
-                      "(wide_samples 1, the plain kernel) and with 8-pass waves (sequential_wide_*)",
+                      "(wide_samples 1, the plain kernel) and with 8-pass waves and the batch's shadow schedule "
+                      "(sequential_wide_*)",
         "m_samples_per_s": world * samples / batch_s / 1e6, "sequential_m_samples_per_s": world * samples / seq_s / 1e6,
         "batch_s": batch_s, "sequential_s": seq_s, "gpu_launches": int(batch_launches),
         "triangles_total": sum(x["triangles"] for x in work), "scenes": n, "scene_build_s": round(build_s, 1),

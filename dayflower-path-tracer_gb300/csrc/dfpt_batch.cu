@@ -56,6 +56,7 @@ struct dfpt_batch {
     DevBatch Q{};
     LaunchCtx ctx{};
     int trace_config = DFPT_DEFAULT_TRACE_CONFIG;
+    bool shadow_defer = false;  // every bounce's sun shadow rays traced in one launch after the last
     bool use_graph = true;
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -141,14 +142,15 @@ int batch_prepare(dfpt_batch* b) {
     }
     const long long want = std::min<long long>(b->capacity_request, total_samples(b));
     const int cap = (int)std::max<long long>(want, 1);
-    const size_t shadow = (size_t)cap;  // one bounce of shadow rays (traced before the next bounce)
+    // One bounce of shadow rays (traced before the next bounce), or every bounce's when deferred.
+    const size_t shadow = (size_t)cap * (size_t)(b->shadow_defer ? std::max(b->depth, 1) : 1);
     if (cap != b->capacity || shadow != b->shadow_slots) {
         batch_release_buffers(b);
         const size_t c = (size_t)cap;
         CUDA_TRY(b->q_o0.alloc(c)); CUDA_TRY(b->q_o1.alloc(c)); CUDA_TRY(b->q_d0.alloc(c)); CUDA_TRY(b->q_d1.alloc(c));
         CUDA_TRY(b->q_hit.alloc(c)); CUDA_TRY(b->slot_key.alloc(c));
         CUDA_TRY(b->throughput.alloc(2 * c)); CUDA_TRY(b->rng.alloc(c)); CUDA_TRY(b->pixel_flags.alloc(c));
-        // Each path leaves at most one sun shadow ray per bounce; a bounce's are traced at once.
+        // Each path leaves at most one sun shadow ray per bounce.
         CUDA_TRY(b->s_o.alloc(shadow)); CUDA_TRY(b->s_d.alloc(shadow)); CUDA_TRY(b->s_c.alloc(shadow));
         b->capacity = cap;
         b->shadow_slots = shadow;
@@ -219,21 +221,26 @@ int issue_wave(dfpt_batch* b) {
     cudaMemsetAsync(b->counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), b->stream);
     K.b_wave(c, 0); ++k;
     K.b_camera(c, 0); ++k;
+    // Sun shadow rays: after each bounce's shading, or (shadow_defer) all bounces' in one launch
+    // after the last bounce; they only add to their paths' radiance.
+    auto shadows = [&]() {
+        if (!b->any_sun) return;
+        if (b->pass.sorted_queues) {
+            k += K.b_sort_shadow(c, b->pass_shadow);
+            K.b_shadow(b->ctx_shadow, 0); ++k;
+        } else {
+            K.b_shadow(c, 0); ++k;
+        }
+        K.b_shadow_reset(c, 0); ++k;
+    };
     for (int i = 0; i < b->depth; ++i) {
         K.b_trace_closest(c, i); ++k;
         K.b_shade(c, i); ++k;
         if (b->pass.sorted_queues) k += K.b_sort(c, i, true);
-        if (b->any_sun) {
-            if (b->pass.sorted_queues) {
-                k += K.b_sort_shadow(c, b->pass_shadow);
-                K.b_shadow(b->ctx_shadow, 0); ++k;
-            } else {
-                K.b_shadow(c, 0); ++k;
-            }
-            K.b_shadow_reset(c, 0); ++k;
-        }
+        if (!b->shadow_defer) shadows();
     }
     K.b_final(c, b->depth); ++k;
+    if (b->shadow_defer) shadows();
     K.b_film(c, 0); ++k;
     K.b_end(c, 0); ++k;
     return k;
@@ -363,6 +370,8 @@ int dfpt_batch_set_tuning(dfpt_batch* b, const char* key, int64_t value) {
         b->use_graph = value != 0;
     } else if (k == "ray_sort") {
         b->ray_sort = value != 0;
+    } else if (k == "shadow_defer") {
+        b->shadow_defer = value != 0;
     } else {
         return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
     }
@@ -378,6 +387,7 @@ int dfpt_batch_get_tuning(dfpt_batch* b, const char* key, int64_t* value) {
     else if (k == "trace_configs") *value = b->ks.trace_configs;
     else if (k == "graphs") *value = b->use_graph ? 1 : 0;
     else if (k == "ray_sort") *value = b->ray_sort ? 1 : 0;
+    else if (k == "shadow_defer") *value = b->shadow_defer ? 1 : 0;
     else if (k == "scenes") *value = (int64_t)b->stores.size();
     else if (k == "total_samples") *value = total_samples(b);
     else if (k == "depth") *value = b->depth;

@@ -111,10 +111,23 @@ def tune_batch(batch, capacities=(1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26), 
     batch.synchronize()
     sort[0] = span / (time.perf_counter() - t0) / 1e6
     batch.set_tuning("ray_sort", max(sort, key=sort.get))
+    # Sun shadow rays per bounce or all bounces' in one launch (the queue then holds depth x as many).
+    defer = {0: sort[max(sort, key=sort.get)]}
+    batch.set_tuning("shadow_defer", 1)
     batch.clear()
-    return {"best": {"wave_capacity": best[0], "trace_config": best[1], "ray_sort": max(sort, key=sort.get)},
+    batch.render_range(first, min(span, best[0]))
+    batch.synchronize()
+    t0 = time.perf_counter()
+    batch.render_range(first, span)
+    batch.synchronize()
+    defer[1] = span / (time.perf_counter() - t0) / 1e6
+    batch.set_tuning("shadow_defer", max(defer, key=defer.get))
+    batch.clear()
+    return {"best": {"wave_capacity": best[0], "trace_config": best[1], "ray_sort": max(sort, key=sort.get),
+                     "shadow_defer": max(defer, key=defer.get)},
             "m_samples_per_s": {f"{k[0]}/{k[1]}": round(v, 2) for k, v in results.items()},
-            "ray_sort_m_samples_per_s": {str(k): round(v, 2) for k, v in sort.items()}}
+            "ray_sort_m_samples_per_s": {str(k): round(v, 2) for k, v in sort.items()},
+            "shadow_defer_m_samples_per_s": {str(k): round(v, 2) for k, v in defer.items()}}
 
 
 def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbose: bool = False) -> dict:

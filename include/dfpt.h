@@ -366,8 +366,10 @@ int dfpt_batch_add(dfpt_batch* batch, const dfpt_scene_desc* scene, const dfpt_s
                    const dfpt_params* params, int32_t width, int32_t height, int32_t spp, int32_t* index);
 int dfpt_batch_set_stream(dfpt_batch* batch, void* cuda_stream);
 /* Keys: "wave_capacity" (path slots per wave, 1024..2^27), "trace_config" (traversal launch
- * configuration, as dfpt_set_tuning), "graphs" (0/1), "ray_sort" (0/1). Read-only for get:
- * "trace_configs", "scenes", "total_samples", "depth". */
+ * configuration, as dfpt_set_tuning), "graphs" (0/1), "ray_sort" (0/1), "shadow_defer" (0: each
+ * bounce's sun shadow rays traced before the next bounce; 1: all bounces' in one launch after the
+ * last, with a shadow queue of depth x wave_capacity entries). Read-only for get: "trace_configs",
+ * "scenes", "total_samples", "depth". */
 int dfpt_batch_set_tuning(dfpt_batch* batch, const char* key, int64_t value);
 int dfpt_batch_get_tuning(dfpt_batch* batch, const char* key, int64_t* value);
 /* Clears every film, renders all samples of all scenes, tone maps the images (asynchronous). */

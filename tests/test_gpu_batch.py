@@ -42,14 +42,19 @@ def single_renders(batch_scenes):
     return res
 
 
-@pytest.mark.parametrize("capacity", [1024, 4096, 1 << 20])
-def test_batch_films_equal_single_scene_films(batch_scenes, single_renders, capacity):
+@pytest.mark.parametrize("capacity, defer", [(1024, 0), (4096, 0), (1 << 20, 0), (4096, 1), (1 << 20, 1)])
+def test_batch_films_equal_single_scene_films(batch_scenes, single_renders, capacity, defer):
+    """Every scene's film equals its single-scene render with waves of any capacity, with the sun
+    shadow rays traced per bounce or all bounces' deferred to one launch (float atomics of the
+    sun contributions: a few ulps)."""
     from dfpt.batch import BatchRenderer
 
     b = BatchRenderer()
     for cs, sky, params, w, h, spp in batch_scenes:
         b.add(cs, w, h, spp, sky, params)
     b.set_tuning("wave_capacity", capacity)
+    b.set_tuning("shadow_defer", defer)
+    assert b.get_tuning("shadow_defer") == defer
     assert b.total_samples == sum(w * h * spp for *_, w, h, spp in batch_scenes)
     b.render()
     b.synchronize()
