@@ -517,18 +517,36 @@ def frame_loop(k, cam, host_img, frames, warmup, barrier):
     """The reference's interactive render loop (DayflowerApplication.java:853-855): per frame
     dfpt_set_camera from host memory, dfpt_render of ONE pass (1 spp) and dfpt_read_bgra8 into host
     memory. Host clock around `frames` frames; M samples/s of the whole image."""
+    import torch
+
     for _ in range(warmup):
         k.update_camera(cam)
         k.execute(1)
         k.get(host_img)
     barrier()
+    torch.cuda.nvtx.range_push("frame_loop")  # lets a profiler take the frames' kernels alone
     t0 = time.perf_counter()
     for _ in range(frames):
         k.update_camera(cam)
         k.execute(1)
         k.get(host_img)
     barrier()
-    return time.perf_counter() - t0
+    dt = time.perf_counter() - t0
+    torch.cuda.nvtx.range_pop()
+    return dt
+
+
+def frame_kernels(k, frames=8):
+    """Per-kernel milliseconds of one frame (1-pass calls with an event between kernels)."""
+    k.set_profiling(True)
+    tot = {}
+    for _ in range(frames):
+        k.execute(1)
+        k.synchronize()
+        for kk, (ms, n) in k.read_profile().items():
+            tot[kk] = tot.get(kk, 0.0) + ms / frames
+    k.set_profiling(False)
+    return {kk: round(v, 4) for kk, v in tot.items() if v > 0}
 
 
 # ncu figures of the closest-hit traversal kernel on mesh_scene (960x540, 4-pass waves, pixel-major
@@ -691,6 +709,7 @@ def main():
     frame_tuning = tune_frame(k)
     k_pixel_tiles = k.get_tuning("pixel_tiles")
     fl_s = frame_loop(k, cam, host_img, S, max(3, args.warmup), barrier)
+    fl_kernels = frame_kernels(k)
     if dist is not None:
         t = torch.tensor([e2e_s, fl_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -770,7 +789,7 @@ def main():
         "frame_loop": {"value": fl_value, "unit": UNIT, "frames": S, "ms_per_frame": fl_s / S * 1e3,
                        "fraction_of_value": fl_value / value, "tail_bounce": frame_tuning["tail_bounce"],
                        "tail_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["ms_per_frame"].items()},
-                       "pixel_tiles": k_pixel_tiles,
+                       "pixel_tiles": k_pixel_tiles, "kernels_ms_per_frame": fl_kernels,
                        "loop": "per frame: dfpt_set_camera(pinned host) + dfpt_render(1 pass) + dfpt_read_bgra8(pinned host), "
                                "as DayflowerApplication's execute/get loop"},
         "gpu_launches": int(launches),
