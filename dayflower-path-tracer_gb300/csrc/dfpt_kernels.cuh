@@ -1255,10 +1255,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_final(DevScene S0, const DevPar
 // The last bounces of a plain pass in one launch. Each lane takes a path whose ray waits for bounce
 // b0 and carries it to its end - closest hit, shading, the next ray - through bounces b0 .. nb - 1
 // and the any-hit test of the continuation after the last (k_final). Late bounces hold few rays,
-// and a launch per bounce costs the slowest ray of every bounce; here a warp costs the slowest of
-// its paths' remaining walks. Each path takes exactly the steps of the per-bounce kernels (same
-// hits, same draws, same order of its radiance sums); sun shadow rays join the deferred queue as
-// there. The loop is warp-uniform: every lane calls the traversal and the queue append together.
+// and a launch per bounce costs the slowest ray of every bounce; here the paths' remaining walks
+// overlap. A lane whose path ends takes the next waiting path from the queue (warp-aggregated
+// fetch), so lanes stay busy while paths of different lengths finish; lanes of a warp may stand at
+// different bounces. Each path takes exactly the steps of the per-bounce kernels (same hits, same
+// draws, same order of its radiance sums); sun shadow rays join the deferred queue as there. Every
+// lane calls the traversals, the fetch and the queue append together (warp-uniform loop).
 template <int V, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S, const DevParams* __restrict__ Pp, DevPass B, int b0, int nb) {
     const DevParams& P = *Pp;
@@ -1266,23 +1268,42 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S, const DevParam
     const int qi = b0 & 1;
     const uint32_t pass = (uint32_t)*B.pass_index;
     const DevBatch Q{};
-    WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + b0) {
-        bool alive = i < n;
-        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
-        if (alive) {
-            o = __ldcs(B.q_o[qi] + i);
-            d = __ldcs(B.q_d[qi] + i);
+    int* const fetch = B.counts + DFPT_COUNTS_FETCH + b0;
+    const int lane = threadIdx.x & 31;
+    bool have = false;      // the lane holds a path: its ray waits at bounce b (b == nb: the final any-hit)
+    bool drained = false;   // warp-uniform: the queue has no more paths
+    int b = nb;
+    float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+    for (;;) {
+        if (!drained) {
+            const unsigned need = __ballot_sync(0xFFFFFFFFu, !have);
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(fetch, __popc(need));
+                base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                if (base + __popc(need) >= n) drained = true;
+                const int idx = base + __popc(need & ((1u << lane) - 1u));
+                if (!have && idx < n) {
+                    o = __ldcs(B.q_o[qi] + idx);
+                    d = __ldcs(B.q_d[qi] + idx);
+                    b = b0;
+                    have = true;
+                }
+            }
         }
-        for (int b = b0; b < nb; ++b) {
-            if (!__any_sync(0xFFFFFFFFu, alive)) break;
+        if (!__any_sync(0xFFFFFFFFu, have)) break;
+        // One closest-hit bounce for the lanes whose ray waits at a bounce below nb.
+        const bool step = have && b < nb;
+        {
             TraceStats st{0, 0};
-            const Hit h = trace_v<false, V>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            warp_add_stats(P, B.stats, 0, alive ? 1u : 0u, st.nodes, st.tris);
+            const Hit h = trace_v<false, V>(S, step, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            warp_add_stats(P, B.stats, 0, step ? 1u : 0u, st.nodes, st.tris);
             bool emit_next = false, emit_shadow = false;
             float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
             float4 so = make_float4(0, 0, 0, 0), sd = make_float4(0, 0, 0, 0), sc = make_float4(0, 0, 0, 0);
             int path = 0;
-            if (alive)
+            if (step)
                 shade_ray<false>(S, Pp, B, Q, b, pass, o, d, make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset), path,
                                  emit_next, no, nd, emit_shadow, so, sd, sc);
             const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
@@ -1291,24 +1312,34 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S, const DevParam
                 B.s_d[sslot] = sd;
                 B.s_c[sslot] = sc;
             }
-            alive = emit_next;
-            o = no;
-            d = nd;
+            if (step) {
+                if (emit_next) {
+                    o = no;
+                    d = nd;
+                    ++b;
+                } else {
+                    have = false;
+                }
+            }
         }
         // The continuation after the last bounce: any hit, else the sky (GRK:3689-3701).
-        if (__any_sync(0xFFFFFFFFu, alive)) {
+        const bool fin = have && b == nb;
+        if (__any_sync(0xFFFFFFFFu, fin)) {
             TraceStats st{0, 0};
-            const Hit h = trace_v<true, V>(S, alive, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            warp_add_stats(P, B.stats, 1, alive ? 1u : 0u, st.nodes, st.tris);
-            if (alive && !(h.t < INF)) {
-                const int path = __float_as_int(o.w);
-                const float4 T = B.throughput[PSI(path)];
-                const float3 sky = sky_color(P, d.x, d.y, d.z);
-                float4 L = B.radiance[PSI(path)];
-                L.x += T.x * sky.x * INV_PI;
-                L.y += T.y * sky.y * INV_PI;
-                L.z += T.z * sky.z * INV_PI;
-                B.radiance[PSI(path)] = L;
+            const Hit h = trace_v<true, V>(S, fin, o.x, o.y, o.z, d.x, d.y, d.z, st);
+            warp_add_stats(P, B.stats, 1, fin ? 1u : 0u, st.nodes, st.tris);
+            if (fin) {
+                if (!(h.t < INF)) {
+                    const int path = __float_as_int(o.w);
+                    const float4 T = B.throughput[PSI(path)];
+                    const float3 sky = sky_color(P, d.x, d.y, d.z);
+                    float4 L = B.radiance[PSI(path)];
+                    L.x += T.x * sky.x * INV_PI;
+                    L.y += T.y * sky.y * INV_PI;
+                    L.z += T.z * sky.z * INV_PI;
+                    B.radiance[PSI(path)] = L;
+                }
+                have = false;
             }
         }
     }
