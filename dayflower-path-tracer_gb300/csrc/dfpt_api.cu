@@ -1393,6 +1393,7 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     TRY_R(cudaMemsetAsync(h->stats.p, 0, 6 * sizeof(unsigned long long), st));
     TRY_R(cudaMemsetAsync(h->pass_index.p, 0, sizeof(int), st));
     TRY_R(cudaMemsetAsync(h->pixel_flags.p, 0, n * sizeof(int), st));
+    TRY_R(cudaMemsetAsync(h->sun.p, 0, n * sizeof(float4), st));
     DevPass& B = h->pass;
     B.n_pixels = h->n_pixels;
     B.q_o[0] = h->q_o0.p; B.q_o[1] = h->q_o1.p; B.q_d[0] = h->q_d0.p; B.q_d[1] = h->q_d1.p;

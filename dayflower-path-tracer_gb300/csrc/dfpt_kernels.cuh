@@ -1519,6 +1519,7 @@ __global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __r
                 }
             }
             B.radiance[PSI(i)] = make_float4(cr_, cg_, cb_, 0.0f);
+            if (B.sun) B.sun[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // k_film adds it: nothing here
             B.rng[i] = rng.state;
         }
         warp_add_stats(P, B.stats, 0, segs, st.nodes, st.tris);
