@@ -421,11 +421,6 @@ struct dfpt_handle {
     int width = 0, height = 0, n_pixels = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    // The second stream of a plain pass (the earlier bounces' shadow rays beside the tail launch)
-    // and the events that fork it from and join it to `stream`; made at first use.
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    bool shadow_overlap = true;
     int sms = 0;
     KernelSet fast{}, strict{}, wide{};  // wide: the batch stages over this handle's scene
     bool use_strict = false;
@@ -435,7 +430,7 @@ struct dfpt_handle {
     DevParams dev_params_host{};
     DevBuf<DevParams> dev_params;
     // Pass buffers.
-    DevBuf<float4> q_o0, q_o1, q_d0, q_d1, s_o, s_d, s_c, throughput, primary_o, primary_d, film_sum, film_comp, sun;
+    DevBuf<float4> q_o0, q_o1, q_d0, q_d1, s_o, s_d, s_c, throughput, primary_o, primary_d, film_sum, film_comp;
     DevBuf<int4> q_hit;
     DevBuf<uint64_t> rng;
     DevBuf<int> pixel_flags, counts, pass_index, film_n, primitive_offsets, hit_prim, hit_type, hit_off;
@@ -539,12 +534,6 @@ void release(dfpt_handle* h) {
     h->dev_params.release();
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
-    if (h->side) cudaStreamDestroy(h->side);
-    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-    if (h->ev_join) cudaEventDestroy(h->ev_join);
-    h->side = nullptr;
-    h->ev_fork = h->ev_join = nullptr;
-    h->sun.release();
     // Lines the window marked persisting go back to normal with the records they cached.
     if (h->l2_window.num_bytes > 0) (void)cudaCtxResetPersistingL2Cache();
     h->l2_window = cudaAccessPolicyWindow{};
@@ -754,31 +743,13 @@ int issue_pass(dfpt_handle* h) {
             mark(h, KIND_TRACE); K.trace_closest(c, b); ++k;
             mark(h, KIND_SHADE); K.shade(c, b); ++k;
         }
-        const bool sun = h->sky.is_sun_active == 1;
-        if (tb < nb && sun && h->shadow_overlap && !h->profiling && h->side && K.split_count) {
-            // The shadow rays of bounces 0 .. tb - 1 are traced on the side stream while the tail
-            // launch runs (it leaves most of each SM idle); their contributions go to the paths'
-            // sun records, so they never meet the tail's updates of the radiance. The tail's own
-            // shadow rays follow once both are done.
-            LaunchCtx cs = c;
-            cs.stream = h->side;
-            K.split_count(c); ++k;
-            cudaEventRecord(h->ev_fork, h->stream);
-            cudaStreamWaitEvent(h->side, h->ev_fork, 0);
-            K.shadow(cs, 1); ++k;
+        if (tb < nb) {
             mark(h, KIND_TRACE); K.tail(c, tb, nb); ++k;
-            cudaEventRecord(h->ev_join, h->side);
-            cudaStreamWaitEvent(h->stream, h->ev_join, 0);
-            mark(h, KIND_SHADOW); K.shadow(c, 2); ++k;
         } else {
-            if (tb < nb) {
-                mark(h, KIND_TRACE); K.tail(c, tb, nb); ++k;
-            } else {
-                mark(h, KIND_FINAL); K.final_(c, nb); ++k;
-            }
-            // The sun shadow rays of all bounces, traced together.
-            if (sun) { mark(h, KIND_SHADOW); K.shadow(c, 0); ++k; }
+            mark(h, KIND_FINAL); K.final_(c, nb); ++k;
         }
+        // The sun shadow rays of all bounces, traced together.
+        if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.shadow(c, 0); ++k; }
     }
     if (h->params.wireframes == 1) { mark(h, KIND_WIREFRAME); K.wireframe(c); ++k; }
     mark(h, KIND_FILM); K.film(c); ++k;
@@ -1380,10 +1351,6 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     TRY_R(h->primitive_offsets.alloc(n));
     TRY_R(h->hit_prim.alloc(n)); TRY_R(h->hit_type.alloc(n)); TRY_R(h->hit_off.alloc(n)); TRY_R(h->hit_dist.alloc(n)); TRY_R(h->hit_normal.alloc(3 * n));
     TRY_R(h->scratch_rgb.alloc(3 * n));
-    TRY_R(h->sun.alloc(n));
-    TRY_R(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
-    TRY_R(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
-    TRY_R(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
     TRY_R(h->dev_params.alloc(1));
     TRY_R(cudaMemsetAsync(h->film_sum.p, 0, n * sizeof(float4), st));
     TRY_R(cudaMemsetAsync(h->film_comp.p, 0, n * sizeof(float4), st));
@@ -1393,7 +1360,6 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     TRY_R(cudaMemsetAsync(h->stats.p, 0, 6 * sizeof(unsigned long long), st));
     TRY_R(cudaMemsetAsync(h->pass_index.p, 0, sizeof(int), st));
     TRY_R(cudaMemsetAsync(h->pixel_flags.p, 0, n * sizeof(int), st));
-    TRY_R(cudaMemsetAsync(h->sun.p, 0, n * sizeof(float4), st));
     DevPass& B = h->pass;
     B.n_pixels = h->n_pixels;
     B.q_o[0] = h->q_o0.p; B.q_o[1] = h->q_o1.p; B.q_d[0] = h->q_d0.p; B.q_d[1] = h->q_d1.p;
@@ -1404,7 +1370,6 @@ int dfpt_create(const dfpt_scene_desc* sd, const dfpt_sky* sky, int32_t width, i
     B.bgra = h->bgra.p; B.primitive_offsets = h->primitive_offsets.p;
     B.hit_prim_offset = h->hit_prim.p; B.hit_shape_type = h->hit_type.p; B.hit_shape_offset = h->hit_off.p;
     B.hit_distance = h->hit_dist.p; B.hit_normal = h->hit_normal.p;
-    B.sun = h->sun.p;
 
     // Noise tables (both kernel sets own a copy).
     r = noise_tables_init(h->fast, st);
@@ -1592,11 +1557,6 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->pixel_tiles = value != 0;
         return push_params(h);
     }
-    if (std::strcmp(key, "shadow_overlap") == 0) {
-        h->shadow_overlap = value != 0;
-        h->graph_valid = false;
-        return DFPT_OK;
-    }
     if (std::strcmp(key, "tail_bounce") == 0) {
         if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %d outside [0, %d]", value, DFPT_MAX_DEPTH);
         h->tail_bounce = value;
@@ -1623,7 +1583,6 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "pixel_tiles") == 0) { *value = h->pixel_tiles ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "tail_bounce") == 0) { *value = h->tail_bounce; return DFPT_OK; }
-    if (std::strcmp(key, "shadow_overlap") == 0) { *value = h->shadow_overlap ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }

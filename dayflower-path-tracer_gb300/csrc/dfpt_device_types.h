@@ -126,9 +126,6 @@ struct DevPass {
     float4* s_o;          // shadow rays {origin.xyz, path id}
     float4* s_d;          // {direction.xyz, 0}
     float4* s_c;          // pending sun contribution {rgb, 0}
-    float4* sun;          // plain passes: per path, the unoccluded sun contributions (k_shadow adds them
-                          // here, k_film to the radiance), so shadow rays may be traced while the
-                          // path's later bounces still update its radiance; null: k_shadow adds to the radiance
     float4* throughput;   // per path, index PSI(path): one 32-byte record holds a path's throughput
     float4* radiance;     // and radiance (radiance = throughput + 1), read and written together
     uint64_t* rng;        // per pixel: LCG state or draw counter
@@ -212,7 +209,6 @@ struct DevBatch {
 };
 
 #define DFPT_COUNTS_SHADOW 32
-#define DFPT_COUNTS_SHADOW_SPLIT 33  // deferred shadow rays queued before the tail launch began
-#define DFPT_COUNTS_FETCH 64  // [64..96]: work-fetch counters of the traversal launches
+#define DFPT_COUNTS_FETCH 64  // [64..95]: work-fetch counters of the traversal launches
 #define DFPT_MAX_DEPTH 30
 #define DFPT_COUNTS_SIZE 128

@@ -716,7 +716,6 @@ __global__ void __launch_bounds__(256) k_camera(DevScene S0, const DevParams* __
             Rng rng = make_rng(P, (uint32_t)pixel, sample, (!BATCH && P.rng_kind == DFPT_RNG_LCG) ? B.rng[i] : 0ull);
             live = primary_ray(S, P, pixel, pt, rng, o, d);
             B.pixel_flags[i] = live ? 0 : 1;
-            if (!BATCH && B.sun) B.sun[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             if (!BATCH && !live) record_rejected(P, B, pixel);
             if (!lean_start<BATCH>(P)) {
                 B.rng[i] = rng.state;
@@ -1161,23 +1160,14 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
 template <bool BATCH, int V, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevParams* __restrict__ Pp, DevPass B, DevBatch Q, int bounce) {
     const DevParams& P = *Pp;
-    // `bounce` selects the part of the queue: 0 all of it, 1 the rays queued before the tail launch
-    // began (DFPT_COUNTS_SHADOW_SPLIT), 2 the rest.
-    int first = 0, n = B.counts[DFPT_COUNTS_SHADOW];
-    int* fetch = B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1;
-    if (bounce == 1) {
-        n = B.counts[DFPT_COUNTS_SHADOW_SPLIT];
-    } else if (bounce == 2) {
-        first = B.counts[DFPT_COUNTS_SHADOW_SPLIT];
-        n -= first;
-        fetch = B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 2;
-    }
-    // Unoccluded: the pending contribution joins the path radiance (or its sun record). A path has
-    // up to one shadow ray per bounce in this queue, so several threads may add to the same path:
-    // atomics (the sum's order, and so its last bit, may vary).
+    const int n = B.counts[DFPT_COUNTS_SHADOW];
+    (void)bounce;
+    // Unoccluded: the pending contribution joins the path radiance. A path has up to one shadow
+    // ray per bounce in this queue, so several threads may add to the same path: atomics (the
+    // sum's order, and so its last bit, may vary).
     auto unoccluded = [&](int i, const float4& o, const float4& c) {
         const int path = __float_as_int(o.w);
-        float* L = B.sun ? reinterpret_cast<float*>(B.sun + path) : reinterpret_cast<float*>(B.radiance + PSI(path));
+        float* L = reinterpret_cast<float*>(B.radiance + PSI(path));
         atomicAdd(L, c.x);
         atomicAdd(L + 1, c.y);
         atomicAdd(L + 2, c.z);
@@ -1187,27 +1177,27 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_shadow(DevScene S0, const DevPa
         TraceStats st{0, 0};
         uint32_t segs = 0;
         trace_refill<true>(
-            n, fetch,
+            n, B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1,
             [&](int, const float4& d) -> const DevScene& { return scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0); },
-            [&](int i, float4& o, float4& d) { o = B.s_o[first + i]; d = B.s_d[first + i]; },
+            [&](int i, float4& o, float4& d) { o = B.s_o[i]; d = B.s_d[i]; },
             [&](int i, const float4& o, const float4&, const Hit& h) {
                 ++segs;
-                if (h.t >= INF - 0.0001f) unoccluded(i, o, B.s_c[first + i]);
+                if (h.t >= INF - 0.0001f) unoccluded(i, o, B.s_c[i]);
             },
             st);
         warp_add_stats(P, B.stats, 1, segs, st.nodes, st.tris);
     } else {
-        WARP_DYNAMIC(i, n, fetch) {
+        WARP_DYNAMIC(i, n, B.counts + DFPT_COUNTS_FETCH + DFPT_MAX_DEPTH + 1) {
             TraceStats st{0, 0};
             const bool valid = i < n;
             float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
             if (valid) {
-                o = __ldcs(B.s_o + first + i);  // read once: streaming
-                d = __ldcs(B.s_d + first + i);
+                o = __ldcs(B.s_o + i);  // read once: streaming
+                d = __ldcs(B.s_d + i);
             }
             const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
             const Hit h = trace_v<true, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
-            if (valid && h.t >= INF - 0.0001f) unoccluded(i, o, __ldcs(B.s_c + first + i));
+            if (valid && h.t >= INF - 0.0001f) unoccluded(i, o, __ldcs(B.s_c + i));
             warp_add_stats(P, B.stats, 1, valid ? 1u : 0u, st.nodes, st.tris);
         }
     }
@@ -1519,7 +1509,6 @@ __global__ void __launch_bounds__(128) k_simple(DevScene S, const DevParams* __r
                 }
             }
             B.radiance[PSI(i)] = make_float4(cr_, cg_, cb_, 0.0f);
-            if (B.sun) B.sun[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // k_film adds it: nothing here
             B.rng[i] = rng.state;
         }
         warp_add_stats(P, B.stats, 0, segs, st.nodes, st.tris);
@@ -1648,27 +1637,17 @@ __global__ void __launch_bounds__(256) k_film(const DevParams* __restrict__ Pp, 
         const int path = slot_of_pixel(P, i);
         float4 sum = B.film_sum[i], comp = B.film_comp[i];
         int cnt = B.film_n[i];
-        float4 L = B.radiance[PSI(path)];
-        if (B.sun) {
-            const float4 sun = B.sun[path];
-            L.x += sun.x; L.y += sun.y; L.z += sun.z;
-        }
-        film_add(L, B.pixel_flags[path], clear, sum, comp, cnt);
+        film_add(B.radiance[PSI(path)], B.pixel_flags[path], clear, sum, comp, cnt);
         if (P.diff) {
             const int k = pass - P.diff_pass0;
             if (k >= 0 && k < P.diff_spp) {
-                B.diff_L[(size_t)k * n + i] = L;
+                B.diff_L[(size_t)k * n + i] = B.radiance[PSI(path)];
                 B.diff_vis[(size_t)k * n + i] = (B.pixel_flags[path] & 1) ? 0 : B.vis[path];
             }
         }
         B.film_sum[i] = sum; B.film_comp[i] = comp; B.film_n[i] = cnt;
         reinterpret_cast<uchar4*>(B.bgra)[i] = tone_map_bgra(P, sum, cnt, B.primitive_offsets[i]);
     }
-}
-
-// Marks where the deferred shadow queue stands when the tail launch begins.
-__global__ void k_split_count(DevPass B) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) B.counts[DFPT_COUNTS_SHADOW_SPLIT] = B.counts[DFPT_COUNTS_SHADOW];
 }
 
 __global__ void k_end_pass(DevPass B) {
@@ -2140,7 +2119,6 @@ static void launch_simple(const LaunchCtx& c) { k_simple<<<c.grid_simple, 128, 0
 static void launch_wireframe(const LaunchCtx& c) { k_wireframe<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_film(const LaunchCtx& c) { k_film<<<c.grid, 256, 0, c.stream>>>(c.params, *c.pass); }
 static void launch_end_pass(const LaunchCtx& c) { k_end_pass<<<1, 32, 0, c.stream>>>(*c.pass); }
-static void launch_split_count(const LaunchCtx& c) { k_split_count<<<1, 32, 0, c.stream>>>(*c.pass); }
 static void launch_film_mean(const LaunchCtx& c, double* out3) { k_film_mean<<<c.grid, 256, 0, c.stream>>>(*c.pass, out3); }
 static void launch_film_average(const LaunchCtx& c, float* rgb, int* samples) {
     k_film_average<<<c.grid, 256, 0, c.stream>>>(*c.pass, rgb, samples);
@@ -2175,7 +2153,6 @@ KernelSet kernel_set() {
     k.wireframe = launch_wireframe;
     k.film = launch_film;
     k.end_pass = launch_end_pass;
-    k.split_count = launch_split_count;
     k.film_mean = launch_film_mean;
     k.film_average = launch_film_average;
 #endif

@@ -22,14 +22,13 @@ struct KernelSet {
     void (*camera)(const LaunchCtx&);
     void (*trace_closest)(const LaunchCtx&, int bounce);
     void (*shade)(const LaunchCtx&, int bounce);
-    void (*shadow)(const LaunchCtx&, int part);  // part of the deferred queue: 0 all, 1 before the split, 2 after
+    void (*shadow)(const LaunchCtx&, int bounce);
     void (*final_)(const LaunchCtx&, int bounce);
     void (*tail)(const LaunchCtx&, int first_bounce, int bounces) = nullptr;  // bounces first .. bounces-1 + the final any-hit
     void (*simple)(const LaunchCtx&);
     void (*wireframe)(const LaunchCtx&);
     void (*film)(const LaunchCtx&);
     void (*end_pass)(const LaunchCtx&);
-    void (*split_count)(const LaunchCtx&) = nullptr;  // marks the deferred shadow queue's length (DFPT_COUNTS_SHADOW_SPLIT)
     void (*film_mean)(const LaunchCtx&, double* out3);
     void (*film_average)(const LaunchCtx&, float* rgb, int* samples);
     void (*init_tables)(cudaStream_t, const int* perm256, const float* grad36);

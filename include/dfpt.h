@@ -237,8 +237,6 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       of 4, counter-based RNG, path tracer without wireframes), 0 in row order;
  *   "tail_bounce"       t >= 1: a plain pass runs bounces t .. depth-1 and the final any-hit of each
  *                       path in one launch (same steps per path); 0 (default) a launch per bounce;
- *   "shadow_overlap"    1 (default): with a tail launch, the sun shadow rays of the earlier bounces
- *                       are traced on a second stream while it runs; 0 after it;
  *   "ray_sort"          1 (default) bins rays by direction and origin cell between the bounces of
  *                       wide passes (processing order only);
  *   "shadow_sort"       with ray_sort, 1 (default) also bins the sun shadow rays by origin cell

@@ -327,16 +327,14 @@ def test_tail_launch_equals_per_bounce_launches(scenes, name):
     """The tail kernel (tail_bounce t: bounces t .. depth-1 and the final any-hit of each path in
     one launch) takes every path through the same steps as a launch per bounce: the same films
     (sun contributions are added with float atomics: a few ulps), the same segments, nodes and
-    triangles, the same selection buffer - with the earlier bounces' shadow rays traced beside it
-    on a second stream (shadow_overlap) or after it."""
+    triangles, the same selection buffer."""
     scene, sky, params, (w, h) = scenes[name]
     params = dict(params, renderer_type=2, pt_ray_depth_maximum=6, pt_ray_depth_russian_roulette=3)
     ref = None
-    for tb, overlap in ((0, 1), (1, 1), (2, 1), (5, 1), (2, 0)):
+    for tb in (0, 1, 2, 5):
         k = _kernel(scene, sky, params, w, h, strict=False)
         k.set_tuning("wide_samples", 1)
         k.set_tuning("tail_bounce", tb)
-        k.set_tuning("shadow_overlap", overlap)
         k.set_counting(True)
         k.execute(4)
         film, samples = k.film()
@@ -346,6 +344,6 @@ def test_tail_launch_equals_per_bounce_launches(scenes, name):
         if ref is None:
             ref = got
             continue
-        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, overlap, np.abs(got[0] - ref[0]).max())
-        assert np.array_equal(got[1], ref[1]), (tb, overlap, got[1], ref[1])
-        assert np.array_equal(got[2], ref[2]), (tb, overlap)
+        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, np.abs(got[0] - ref[0]).max())
+        assert np.array_equal(got[1], ref[1]), (tb, got[1], ref[1])
+        assert np.array_equal(got[2], ref[2]), tb
