@@ -465,6 +465,12 @@ struct dfpt_handle {
     int wide_samples = 8;
     bool pixel_tiles = true;   // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
     int tail_bounce = 0;       // plain passes: first bounce of the tail launch (0: a launch per bounce)
+    // Plain passes: the deferred shadow rays binned by origin cell before their launch.
+    bool pass_shadow_sort = false;
+    DevBuf<int> p_sort_bins;                  // offsets, (unused), shadow counts, chunk sums
+    DevBuf<float4> p_s2_o, p_s2_d, p_s2_c;    // the binned copy of the shadow queue
+    size_t p_s2_capacity = 0;
+    DevPass pass_shadow2{};                   // `pass` reading the binned copy
     int wide_capacity = 0;
     size_t wide_shadow = 0;
     DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput;  // w_throughput: throughput + radiance records (PSI)
@@ -532,6 +538,7 @@ void release(dfpt_handle* h) {
     h->stats.release();
     h->mean.release();
     h->dev_params.release();
+    h->p_sort_bins.release(); h->p_s2_o.release(); h->p_s2_d.release(); h->p_s2_c.release();
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     // Lines the window marked persisting go back to normal with the records they cached.
@@ -748,8 +755,18 @@ int issue_pass(dfpt_handle* h) {
         } else {
             mark(h, KIND_FINAL); K.final_(c, nb); ++k;
         }
-        // The sun shadow rays of all bounces, traced together.
-        if (h->sky.is_sun_active == 1) { mark(h, KIND_SHADOW); K.shadow(c, 0); ++k; }
+        // The sun shadow rays of all bounces, traced together (binned by origin cell first when
+        // pass_shadow_sort is on: shading and the tail counted the bins).
+        if (h->sky.is_sun_active == 1) {
+            if (h->pass.sort_count_shadow && K.sort_shadow) {
+                mark(h, KIND_SORT); k += K.sort_shadow(c, h->pass_shadow2);
+                LaunchCtx c2 = c;
+                c2.pass = &h->pass_shadow2;
+                mark(h, KIND_SHADOW); K.shadow(c2, 0); ++k;
+            } else {
+                mark(h, KIND_SHADOW); K.shadow(c, 0); ++k;
+            }
+        }
     }
     if (h->params.wireframes == 1) { mark(h, KIND_WIREFRAME); K.wireframe(c); ++k; }
     mark(h, KIND_FILM); K.film(c); ++k;
@@ -991,6 +1008,41 @@ int ensure_shadow_capacity(dfpt_handle* h) {
     h->pass.s_o = h->s_o.p; h->pass.s_d = h->s_d.p; h->pass.s_c = h->s_c.p;
     h->graph_valid = false;
     h->wide_graph_valid = false;
+    return DFPT_OK;
+}
+
+// Plain passes' shadow binning: the bins and the binned copy of the shadow queue (as large as the
+// queue), or none; `pass` gets the bin pointers its shading counts into.
+int pass_shadow_sort_prepare(dfpt_handle* h) {
+    DevPass& B = h->pass;
+    if (!h->pass_shadow_sort) {
+        if (B.sort_count_shadow) {
+            B.sort_bins = B.sort_count = B.sort_count_shadow = B.sort_partials = nullptr;
+            h->graph_valid = false;
+        }
+        return DFPT_OK;
+    }
+    if (!h->p_sort_bins.p) {
+        CUDA_TRY(h->p_sort_bins.alloc(3 * DFPT_SORT_BINS + DFPT_SORT_CHUNKS));
+        CUDA_TRY(cudaMemsetAsync(h->p_sort_bins.p, 0, (3 * DFPT_SORT_BINS + DFPT_SORT_CHUNKS) * sizeof(int), h->stream));
+    }
+    if (h->p_s2_capacity < h->shadow_capacity) {
+        h->p_s2_o.release(); h->p_s2_d.release(); h->p_s2_c.release();
+        CUDA_TRY(h->p_s2_o.alloc(h->shadow_capacity));
+        CUDA_TRY(h->p_s2_d.alloc(h->shadow_capacity));
+        CUDA_TRY(h->p_s2_c.alloc(h->shadow_capacity));
+        h->p_s2_capacity = h->shadow_capacity;
+        h->graph_valid = false;
+    }
+    if (B.sort_count_shadow != h->p_sort_bins.p + 2 * DFPT_SORT_BINS) h->graph_valid = false;
+    B.sort_bins = h->p_sort_bins.p;
+    B.sort_count = nullptr;  // the bounces' rays stay unbinned
+    B.sort_count_shadow = h->p_sort_bins.p + 2 * DFPT_SORT_BINS;
+    B.sort_partials = h->p_sort_bins.p + 3 * DFPT_SORT_BINS;
+    h->pass_shadow2 = B;
+    h->pass_shadow2.s_o = h->p_s2_o.p;
+    h->pass_shadow2.s_d = h->p_s2_d.p;
+    h->pass_shadow2.s_c = h->p_s2_c.p;
     return DFPT_OK;
 }
 
@@ -1557,6 +1609,11 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->pixel_tiles = value != 0;
         return push_params(h);
     }
+    if (std::strcmp(key, "pass_shadow_sort") == 0) {
+        h->pass_shadow_sort = value != 0;
+        h->graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "tail_bounce") == 0) {
         if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %d outside [0, %d]", value, DFPT_MAX_DEPTH);
         h->tail_bounce = value;
@@ -1583,6 +1640,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "wide_samples") == 0) { *value = h->wide_samples; return DFPT_OK; }
     if (std::strcmp(key, "pixel_tiles") == 0) { *value = h->pixel_tiles ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "tail_bounce") == 0) { *value = h->tail_bounce; return DFPT_OK; }
+    if (std::strcmp(key, "pass_shadow_sort") == 0) { *value = h->pass_shadow_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }
@@ -1621,6 +1679,7 @@ int dfpt_render(dfpt_handle* h, int32_t passes) {
     h->events_used = 0;
     {
         int r = ensure_shadow_capacity(h);
+        if (!r) r = pass_shadow_sort_prepare(h);
         if (r) return r;
     }
     if (passes >= 2 && wide_eligible(h)) {

@@ -1144,6 +1144,9 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
                 bin_count(B.sort_count, emit_next ? ray_bin_in_wave(Q, first, no, nd) : -1);
                 if (B.sort_count_shadow) bin_count(B.sort_count_shadow, emit_shadow ? shadow_bin_in_wave(Q, first, so, sd) : -1);
             }
+        } else {
+            // Plain passes may bin the deferred shadow rays alone (origin cells).
+            if (B.sort_count_shadow) bin_count(B.sort_count_shadow, emit_shadow ? cell_bits(S0, so, DFPT_SHADOW_CELL_BITS) : -1);
         }
         const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
         if (sslot >= 0) {
@@ -1306,6 +1309,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_tail(DevScene S, const DevParam
             if (step)
                 shade_ray<false>(S, Pp, B, Q, b, pass, o, d, make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset), path,
                                  emit_next, no, nd, emit_shadow, so, sd, sc);
+            if (B.sort_count_shadow) bin_count(B.sort_count_shadow, emit_shadow ? cell_bits(S, so, DFPT_SHADOW_CELL_BITS) : -1);
             const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
             if (sslot >= 0) {
                 B.s_o[sslot] = so;
@@ -1835,6 +1839,32 @@ __global__ void __launch_bounds__(256) k_sort_chunk_scan(DevPass B, int* counts)
     reinterpret_cast<int4*>(B.sort_bins + (size_t)blockIdx.x * 1024)[threadIdx.x] =
         make_int4(before, before + c.x, before + c.x + c.y, before + c.x + c.y + c.z);
 }
+// A plain pass's deferred shadow rays into `out` in origin-cell order (the counts come from its
+// shading, the offsets from the scan).
+__global__ void __launch_bounds__(256) k_sort_shadow_scatter_plain(DevScene S, DevPass B, float4* out_o, float4* out_d, float4* out_c) {
+    const int n = B.counts[DFPT_COUNTS_SHADOW];
+    GRID_STRIDE_UNIFORM(i, n) {
+        int key = -1;
+        float4 o, d, c;
+        if (i < n) {
+            o = B.s_o[i];
+            d = B.s_d[i];
+            c = B.s_c[i];
+            key = cell_bits(S, o, DFPT_SHADOW_CELL_BITS);
+        }
+        const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
+        const int leader = __ffs(same) - 1;
+        int base = 0;
+        if (key >= 0 && (int)(threadIdx.x & 31) == leader) base = atomicAdd(B.sort_bins + key, __popc(same));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (key >= 0) {
+            const int pos = base + __popc(same & ((1u << (threadIdx.x & 31)) - 1u));
+            out_o[pos] = o;
+            out_d[pos] = d;
+            out_c[pos] = c;
+        }
+    }
+}
 static void launch_sort_scan(const LaunchCtx& c, int* counts) {
     k_sort_chunk_sums<<<DFPT_SORT_CHUNKS, 256, 0, c.stream>>>(*c.pass, counts);
     k_sort_chunk_offsets<<<1, 256, 0, c.stream>>>(*c.pass);
@@ -2119,6 +2149,13 @@ static void launch_simple(const LaunchCtx& c) { k_simple<<<c.grid_simple, 128, 0
 static void launch_wireframe(const LaunchCtx& c) { k_wireframe<<<c.grid_simple, 128, 0, c.stream>>>(*c.scene, c.params, *c.pass); }
 static void launch_film(const LaunchCtx& c) { k_film<<<c.grid, 256, 0, c.stream>>>(c.params, *c.pass); }
 static void launch_end_pass(const LaunchCtx& c) { k_end_pass<<<1, 32, 0, c.stream>>>(*c.pass); }
+// Bins a plain pass's deferred shadow rays into `to` (a pass record whose s_* point at the second
+// set); shading counted the bins. Returns the kernels launched.
+static int launch_sort_shadow(const LaunchCtx& c, const DevPass& to) {
+    launch_sort_scan(c, c.pass->sort_count_shadow);
+    k_sort_shadow_scatter_plain<<<c.grid, 256, 0, c.stream>>>(*c.scene, *c.pass, to.s_o, to.s_d, to.s_c);
+    return 4;
+}
 static void launch_film_mean(const LaunchCtx& c, double* out3) { k_film_mean<<<c.grid, 256, 0, c.stream>>>(*c.pass, out3); }
 static void launch_film_average(const LaunchCtx& c, float* rgb, int* samples) {
     k_film_average<<<c.grid, 256, 0, c.stream>>>(*c.pass, rgb, samples);
@@ -2153,6 +2190,7 @@ KernelSet kernel_set() {
     k.wireframe = launch_wireframe;
     k.film = launch_film;
     k.end_pass = launch_end_pass;
+    k.sort_shadow = launch_sort_shadow;
     k.film_mean = launch_film_mean;
     k.film_average = launch_film_average;
 #endif

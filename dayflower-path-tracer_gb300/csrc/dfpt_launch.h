@@ -29,6 +29,7 @@ struct KernelSet {
     void (*wireframe)(const LaunchCtx&);
     void (*film)(const LaunchCtx&);
     void (*end_pass)(const LaunchCtx&);
+    int (*sort_shadow)(const LaunchCtx&, const DevPass& to) = nullptr;  // plain passes: bins the deferred shadow rays
     void (*film_mean)(const LaunchCtx&, double* out3);
     void (*film_average)(const LaunchCtx&, float* rgb, int* samples);
     void (*init_tables)(cudaStream_t, const int* perm256, const float* grad36);

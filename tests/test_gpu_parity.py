@@ -327,14 +327,16 @@ def test_tail_launch_equals_per_bounce_launches(scenes, name):
     """The tail kernel (tail_bounce t: bounces t .. depth-1 and the final any-hit of each path in
     one launch) takes every path through the same steps as a launch per bounce: the same films
     (sun contributions are added with float atomics: a few ulps), the same segments, nodes and
-    triangles, the same selection buffer."""
+    triangles, the same selection buffer - with the deferred shadow rays binned by origin cell
+    before their launch (pass_shadow_sort) or not."""
     scene, sky, params, (w, h) = scenes[name]
     params = dict(params, renderer_type=2, pt_ray_depth_maximum=6, pt_ray_depth_russian_roulette=3)
     ref = None
-    for tb in (0, 1, 2, 5):
+    for tb, sort in ((0, 0), (1, 0), (2, 0), (5, 0), (0, 1), (2, 1)):
         k = _kernel(scene, sky, params, w, h, strict=False)
         k.set_tuning("wide_samples", 1)
         k.set_tuning("tail_bounce", tb)
+        k.set_tuning("pass_shadow_sort", sort)
         k.set_counting(True)
         k.execute(4)
         film, samples = k.film()
@@ -344,6 +346,6 @@ def test_tail_launch_equals_per_bounce_launches(scenes, name):
         if ref is None:
             ref = got
             continue
-        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, np.abs(got[0] - ref[0]).max())
-        assert np.array_equal(got[1], ref[1]), (tb, got[1], ref[1])
-        assert np.array_equal(got[2], ref[2]), tb
+        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, sort, np.abs(got[0] - ref[0]).max())
+        assert np.array_equal(got[1], ref[1]), (tb, sort, got[1], ref[1])
+        assert np.array_equal(got[2], ref[2]), (tb, sort)
