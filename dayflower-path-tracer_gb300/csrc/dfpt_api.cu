@@ -466,7 +466,7 @@ struct dfpt_handle {
     bool pixel_tiles = true;   // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
     int tail_bounce = 0;       // plain passes: first bounce of the tail launch (0: a launch per bounce)
     // Plain passes: the deferred shadow rays binned by origin cell before their launch.
-    bool pass_shadow_sort = false;
+    bool pass_shadow_sort = true;
     DevBuf<int> p_sort_bins;                  // offsets, (unused), shadow counts, chunk sums
     DevBuf<float4> p_s2_o, p_s2_d, p_s2_c;    // the binned copy of the shadow queue
     size_t p_s2_capacity = 0;
