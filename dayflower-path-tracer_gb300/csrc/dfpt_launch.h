@@ -46,6 +46,7 @@ struct KernelSet {
     void (*b_shadow)(const LaunchCtx&, int) = nullptr;
     void (*b_final)(const LaunchCtx&, int) = nullptr;
     void (*b_wave)(const LaunchCtx&, int) = nullptr;
+    void (*b_wave_count)(const LaunchCtx&, int) = nullptr;  // bounce 0's ray count when the camera is fused
     void (*b_film)(const LaunchCtx&, int) = nullptr;
     void (*b_resolve)(const LaunchCtx&, int) = nullptr;
     void (*b_end)(const LaunchCtx&, int) = nullptr;
