@@ -463,8 +463,6 @@ struct dfpt_handle {
     // Wide passes: dfpt_render's passes but the last run `wide_samples` at a time through the
     // batch stages (one scene), so each launch carries k samples per pixel (see render_wide).
     int wide_samples = 8;
-    bool fuse_camera = true;       // waves: bounce 0's rays made inside traversal and shading (when lean)
-    int wide_camera_fused = -1;    // the choice the wave graph was captured with
     bool pixel_tiles = true;   // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
     int tail_bounce = 0;       // plain passes: first bounce of the tail launch (0: a launch per bounce)
     // Plain passes: the deferred shadow rays binned by origin cell before their launch.
@@ -855,14 +853,6 @@ int wide_prepare(dfpt_handle* h) {
     B.counts = h->w_counts.p; B.stats = h->stats.p; B.pass_index = h->pass_index.p;
     B.film_sum = h->film_sum.p; B.film_comp = h->film_comp.p; B.film_n = h->film_n.p; B.bgra = h->bgra.p;
     B.sorted_queues = (h->ray_sort && h->wide.b_sort) ? 1 : 0;
-    // The camera inside bounce 0's kernels: lean waves (counter RNG, no differentiation) with a lens
-    // that keeps every pixel (not the fisheye), so the wave's slots are the bounce-0 queue.
-    B.camera_fused = (h->fuse_camera && !h->diff_on && h->params.rng_kind == DFPT_RNG_COUNTER && h->wide.b_wave_count &&
-                      h->sc.host.camera.size() > 18 && h->sc.host.camera[18] != 2.0f) ? 1 : 0;
-    if (B.camera_fused != h->wide_camera_fused) {
-        h->wide_camera_fused = B.camera_fused;
-        h->wide_graph_valid = false;
-    }
     B.sort_bins = h->w_sort_bins.p;
     B.primitive_offsets = h->primitive_offsets.p;  // selection buffer: first hits of the call's last pass
     B.sort_count = h->w_sort_bins.p + DFPT_SORT_BINS;
@@ -919,11 +909,7 @@ int issue_wide_wave(dfpt_handle* h) {
     int k = 0;
     cudaMemsetAsync(h->w_counts.p, 0, DFPT_COUNTS_SIZE * sizeof(int), h->stream);
     K.b_wave(c, 0); ++k;
-    if (h->wpass.camera_fused) {
-        K.b_wave_count(c, 0); ++k;
-    } else {
-        mark(h, KIND_CAMERA); K.b_camera(c, 0); ++k;
-    }
+    mark(h, KIND_CAMERA); K.b_camera(c, 0); ++k;
     const int nb = bounces_of(h);
     // Sun shadow rays: traced right after each bounce's shading (the queue holds one bounce), or,
     // with shadow_defer, all bounces' at once after the last bounce (queue of slots x depth).
@@ -1623,11 +1609,6 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->pixel_tiles = value != 0;
         return push_params(h);
     }
-    if (std::strcmp(key, "fuse_camera") == 0) {
-        h->fuse_camera = value != 0;
-        h->wide_graph_valid = false;
-        return DFPT_OK;
-    }
     if (std::strcmp(key, "pass_shadow_sort") == 0) {
         h->pass_shadow_sort = value != 0;
         h->graph_valid = false;
@@ -1660,7 +1641,6 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "pixel_tiles") == 0) { *value = h->pixel_tiles ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "tail_bounce") == 0) { *value = h->tail_bounce; return DFPT_OK; }
     if (std::strcmp(key, "pass_shadow_sort") == 0) { *value = h->pass_shadow_sort ? 1 : 0; return DFPT_OK; }
-    if (std::strcmp(key, "fuse_camera") == 0) { *value = h->fuse_camera ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }

@@ -130,8 +130,6 @@ struct DevPass {
     float4* radiance;     // and radiance (radiance = throughput + 1), read and written together
     uint64_t* rng;        // per pixel: LCG state or draw counter
     int* pixel_flags;     // bit 0: film set to black this pass
-    int camera_fused;     // one-scene waves: bounce 0's rays come from the camera inside the traversal
-                          // and shading kernels (no camera launch, no ray queue at bounce 0)
     float4* primary_o;    // primary rays (wireframe overlay)
     float4* primary_d;
     int* counts;          // [0..31] ray queue counts per bounce, [32] deferred shadow rays, [64..95] work fetch

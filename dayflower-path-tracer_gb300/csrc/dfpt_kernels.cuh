@@ -621,38 +621,6 @@ __device__ __forceinline__ int slot_of_pixel(const DevParams& P, int p) {
     return (((y >> 2) * (P.width >> 3) + (x >> 3)) << 5) | ((y & 3) << 3) | (x & 7);
 }
 
-#ifdef DFPT_ONE_SCENE
-// One-scene waves: the primary ray of wave slot i, from the slot's pixel and sample as k_camera
-// derives them (pixel-major slots) and the same RNG draws. False when the slot holds no sample of
-// the wave or the lens rejects it. With DevPass::camera_fused the traversal and shading kernels of
-// bounce 0 call it instead of reading a ray queue that a camera launch wrote.
-__device__ __forceinline__ bool wave_slot_ray(const DevScene& S, const DevParams& P, const DevBatch& Q, int i, float4& o, float4& d) {
-    const unsigned np = (unsigned)((long long)P.width * P.height);
-    const unsigned wave_p = wave_passes(Q, (long long)np);
-    const long long base = Q.wave_base[0], end = Q.wave_base[1];
-    const long long g = wave_p == 0u ? base + i : (unsigned)i < wave_p * np ? base + rel_of_slot((unsigned)i, np, wave_p) : end;
-    if (g >= end) return false;
-    const long long local = g - Q.sample_begin[0];
-    int pixel;
-    long long j;
-    if (local < 0x7FFFFFFFll) {
-        const unsigned q = (unsigned)local / np;
-        j = q;
-        pixel = (int)((unsigned)local - q * np);
-    } else {
-        j = local / (long long)np;
-        pixel = (int)(local - j * (long long)np);
-    }
-    const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
-                    (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
-    Rng rng = make_rng(P, (uint32_t)pixel, (uint32_t)(j + Q.wave_base[2]), 0ull);
-    if (!primary_ray(S, P, pixel, pt, rng, o, d)) return false;
-    o.w = __int_as_float(i);
-    d.w = __int_as_float(0);
-    return true;
-}
-#endif
-
 __device__ __forceinline__ uint32_t camera_draws(const DevScene& S, const DevParams& P) {
     const bool pt = P.renderer_type == DFPT_RENDERER_PATH_TRACER ||
                     (P.renderer_type < DFPT_RENDERER_AMBIENT_OCCLUSION || P.renderer_type > DFPT_RENDERER_SURFACE_NORMALS);
@@ -784,17 +752,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S0, const DevPar
         trace_refill<ANY>(
             n, B.counts + DFPT_COUNTS_FETCH + bounce,
             [&](int, const float4& d) -> const DevScene& { return scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0); },
-            [&](int i, float4& o, float4& d) {
-#ifdef DFPT_ONE_SCENE
-                if (B.camera_fused && bounce == 0) {
-                    wave_slot_ray(S0, *Pp, Q, i, o, d);
-                    B.pixel_flags[i] = 0;
-                    return;
-                }
-#endif
-                o = qo[i];
-                d = qd[i];
-            },
+            [&](int i, float4& o, float4& d) { o = qo[i]; d = qd[i]; },
             [&](int i, const float4&, const float4&, const Hit& h) {
                 B.q_hit[i] = make_int4(__float_as_int(h.t), h.prim, h.shape_type, h.shape_offset);
                 ++segs;
@@ -807,19 +765,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace(DevScene S0, const DevPar
             const bool valid = i < n;
             float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
             if (valid) {
-#ifdef DFPT_ONE_SCENE
-                if (B.camera_fused && bounce == 0) {
-                    // The wave's slots are the queue (a dense camera: every slot holds a live ray).
-                    wave_slot_ray(S0, *Pp, Q, i, o, d);
-                    B.pixel_flags[i] = 0;
-                } else
-#endif
-                {
-                    // Streaming accesses: each ray and hit is touched once here, and the BVH
-                    // records keep the L1.
-                    o = __ldcs(qo + i);
-                    d = __ldcs(qd + i);
-                }
+                // Streaming accesses: each ray and hit is touched once here, and the BVH records
+                // keep the L1.
+                o = __ldcs(qo + i);
+                d = __ldcs(qd + i);
             }
             const DevScene& S = scene_of<BATCH>(S0, Q, BATCH ? __float_as_int(d.w) : 0);
             const Hit h = trace_v<ANY, V>(S, valid, o.x, o.y, o.z, d.x, d.y, d.z, st);
@@ -1181,19 +1130,8 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
         float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
         float4 so = make_float4(0, 0, 0, 0), sd = make_float4(0, 0, 0, 0), sc = make_float4(0, 0, 0, 0);
         int path = 0;
-        if (i < n) {
-            float4 o4, d4;
-#ifdef DFPT_ONE_SCENE
-            if (B.camera_fused && bounce == 0) {
-                wave_slot_ray(S0, *Pp, Q, i, o4, d4);
-            } else
-#endif
-            {
-                o4 = B.q_o[qi][i];
-                d4 = B.q_d[qi][i];
-            }
-            shade_ray<BATCH>(S0, Pp, B, Q, bounce, pass, o4, d4, B.q_hit[i], path, emit_next, no, nd, emit_shadow, so, sd, sc);
-        }
+        if (i < n) shade_ray<BATCH>(S0, Pp, B, Q, bounce, pass, B.q_o[qi][i], B.q_d[qi][i], B.q_hit[i], path, emit_next, no, nd,
+                                    emit_shadow, so, sd, sc);
         const int slot = warp_push(B.counts + bounce + 1, emit_next);
         if (slot >= 0) {
             B.q_o[qi ^ 1][slot] = no;
@@ -1750,13 +1688,6 @@ __global__ void k_bwave(DevBatch Q) {
     *Q.wave_entries = e;
 }
 
-// With a fused camera: bounce 0's ray count, the wave's valid slots (k_camera's count).
-__global__ void k_wave_count(DevBatch Q, DevPass B) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const long long valid = Q.wave_base[1] - Q.wave_base[0];
-    B.counts[0] = (int)(valid < (long long)Q.capacity ? (valid > 0 ? valid : 0) : (long long)Q.capacity);
-}
-
 // One thread per film task: adds the pixel's samples of this wave in sample order, so each pixel
 // sees the same Kahan sequence as one-scene rendering, pass after pass.
 __global__ void __launch_bounds__(256) k_bfilm(DevBatch Q, DevPass B) {
@@ -2168,7 +2099,6 @@ BATCH_DISPATCH(final)
 static void launch_b_camera(const LaunchCtx& c, int) { k_camera<true><<<c.grid, 256, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch); }
 static void launch_b_shade(const LaunchCtx& c, int bounce) { k_shade<true><<<c.grid, 256, 0, c.stream>>>(BATCH_SCENE(c), c.params, *c.pass, *c.batch, bounce); }
 static void launch_b_wave(const LaunchCtx& c, int) { k_bwave<<<1, 32, 0, c.stream>>>(*c.batch); }
-static void launch_b_wave_count(const LaunchCtx& c, int) { k_wave_count<<<1, 32, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_film(const LaunchCtx& c, int) { k_bfilm<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_resolve(const LaunchCtx& c, int) { k_bresolve<<<c.grid, 256, 0, c.stream>>>(*c.batch, *c.pass); }
 static void launch_b_end(const LaunchCtx& c, int) { k_bend_wave<<<1, 32, 0, c.stream>>>(*c.batch); }
@@ -2278,7 +2208,6 @@ KernelSet kernel_set() {
     k.b_shadow = launch_b_shadow;
     k.b_final = launch_b_final;
     k.b_wave = launch_b_wave;
-    k.b_wave_count = launch_b_wave_count;
     k.b_film = launch_b_film;
     k.b_resolve = launch_b_resolve;
     k.b_end = launch_b_end;

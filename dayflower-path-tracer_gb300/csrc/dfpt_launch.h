@@ -46,7 +46,6 @@ struct KernelSet {
     void (*b_shadow)(const LaunchCtx&, int) = nullptr;
     void (*b_final)(const LaunchCtx&, int) = nullptr;
     void (*b_wave)(const LaunchCtx&, int) = nullptr;
-    void (*b_wave_count)(const LaunchCtx&, int) = nullptr;  // bounce 0's ray count when the camera is fused
     void (*b_film)(const LaunchCtx&, int) = nullptr;
     void (*b_resolve)(const LaunchCtx&, int) = nullptr;
     void (*b_end)(const LaunchCtx&, int) = nullptr;

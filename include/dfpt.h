@@ -237,9 +237,6 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       of 4, counter-based RNG, path tracer without wireframes), 0 in row order;
  *   "tail_bounce"       t >= 1: a plain pass runs bounces t .. depth-1 and the final any-hit of each
  *                       path in one launch (same steps per path); 0 (default) a launch per bounce;
- *   "fuse_camera"       1 (default): waves of passes with the counter-based RNG and a lens that keeps
- *                       every pixel make bounce 0's camera rays inside the traversal and shading
- *                       kernels (no camera launch, no ray queue at bounce 0); 0 a camera launch;
  *   "pass_shadow_sort"  1 (default): a plain pass bins its deferred sun shadow rays by origin cell
  *                       before their launch (processing order only; a second copy of the shadow
  *                       queue); 0 in queue order;

@@ -232,17 +232,15 @@ def test_wide_passes_equal_pass_by_pass(scenes, name):
     film of n single passes: same samples per pixel, same Kahan order; float atomics of the sun
     contributions leave a few ulps (rtol 1e-5). A clear between calls restarts both the same way;
     the selection buffer and the image come from the last (normal) pass in both. The same holds
-    with the shadow rays of all bounces deferred to one launch, and with the camera rays made
-    inside bounce 0's kernels or by a camera launch."""
+    with the shadow rays of all bounces deferred to one launch."""
     scene, sky, params, (w, h) = scenes[name]
     out = []
-    # (passes per wave, ray binning, deferred shadow rays, camera inside bounce 0's kernels)
-    for wide, sort, defer, fuse in ((1, 0, 0, 1), (8, 1, 0, 1), (8, 0, 0, 1), (8, 1, 1, 1), (8, 0, 1, 1), (8, 1, 1, 0)):
+    # (passes per wave, ray binning, deferred shadow rays)
+    for wide, sort, defer in ((1, 0, 0), (8, 1, 0), (8, 0, 0), (8, 1, 1), (8, 0, 1)):
         k = _kernel(scene, sky, dict(params, renderer_type=2), w, h)
         k.set_tuning("wide_samples", wide)
         k.set_tuning("ray_sort", sort)
         k.set_tuning("shadow_defer", defer)
-        k.set_tuning("fuse_camera", fuse)
         k.execute(13)
         k.clear()
         k.execute(11)
