@@ -1947,7 +1947,7 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
     X(0, 0, 256, 4) X(1, 1, 256, 4) X(2, 1, 256, 3) X(3, 0, 128, 8) X(4, 2, 256, 4) X(5, 2, 128, 8) X(6, 2, 256, 3) \
     X(7, 3, 256, 4) X(8, 3, 128, 8) X(9, 3, 256, 3) X(10, 3, 256, 2) \
     X(11, 0, 256, 6) X(12, 1, 256, 6) X(13, 0, 256, 8) X(14, 1, 256, 8) \
-    X(15, 4, 256, 4) X(16, 5, 256, 4)
+    X(15, 4, 256, 4) X(16, 5, 256, 4) X(17, 5, 256, 5) X(18, 5, 128, 8)
 
 // The scene argument of the batch stages: the context's scene in a one-scene set, else none (the
 // kernels read each item's scene from the batch).
@@ -1984,9 +1984,9 @@ struct TraceCfg {
     }
     // The tail kernel: traversal and shading in one kernel, compiled for two resident blocks; its
     // grid (SMs x resident blocks) is found once per process. Its walk is the configuration's when
-    // that is the threaded walk (0) or the compact pair walk (5), else the prefetching walk (1):
-    // the warp-synchronous, lane-refill and stacked pair walks are built for whole launches of
-    // rays, not for a loop whose lanes retire one by one.
+    // that is the threaded walk (0) or the compact pair walk (5), else the prefetching walk (1),
+    // so that three instantiations serve every configuration (the other walks lost to these in
+    // whole launches).
     static constexpr int TVV = (V == 0 || V == 5) ? V : 1;
     static void tail(const LaunchCtx& c, int b0, int nb) {
         static int grid_tail = 0;
