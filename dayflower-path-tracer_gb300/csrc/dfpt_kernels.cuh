@@ -1947,7 +1947,7 @@ __global__ void k_init_tables(const int* perm256, const float* grad36) {
     X(0, 0, 256, 4) X(1, 1, 256, 4) X(2, 1, 256, 3) X(3, 0, 128, 8) X(4, 2, 256, 4) X(5, 2, 128, 8) X(6, 2, 256, 3) \
     X(7, 3, 256, 4) X(8, 3, 128, 8) X(9, 3, 256, 3) X(10, 3, 256, 2) \
     X(11, 0, 256, 6) X(12, 1, 256, 6) X(13, 0, 256, 8) X(14, 1, 256, 8) \
-    X(15, 4, 256, 4) X(16, 5, 256, 4) X(17, 5, 256, 5) X(18, 5, 128, 8)
+    X(15, 4, 256, 4) X(16, 5, 256, 4) X(17, 5, 256, 5)
 
 // The scene argument of the batch stages: the context's scene in a one-scene set, else none (the
 // kernels read each item's scene from the batch).

@@ -75,7 +75,7 @@ def tune_batch(batch, capacities=(1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26), 
         # The per-lane walks at 4 and 3 blocks per SM, the lane-refill walk and the pair walks: the
         # warp-synchronous walk (4-6) maps to the per-lane walk in a batch, and the 6-8 block
         # configurations (11-14) spill and lose on every workload measured.
-        configs = [c for c in (0, 1, 2, 3, 9, 15, 16) if c < batch.get_tuning("trace_configs")]
+        configs = [c for c in (0, 1, 2, 3, 9, 15, 16, 17) if c < batch.get_tuning("trace_configs")]
     results = {}
     # One window of the batch's sample sequence for every candidate, so the rates compare.
     span = int(min(total, window if window is not None else 2 * max(capacities)))
