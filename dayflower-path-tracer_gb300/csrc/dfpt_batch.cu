@@ -7,7 +7,8 @@
 // to - and runs the path tracer's stages over them, one launch per stage:
 //   wave table -> camera -> [trace closest -> shade -> sun shadow rays] x depth -> final any-hit ->
 //   film -> advance
-// captured once as a CUDA graph and replayed per wave. A pixel's samples enter its film in sample
+// (with shadow_defer, every bounce's sun shadow rays wait in one queue and go in one launch after
+// the final any-hit), captured once as a CUDA graph and replayed per wave. A pixel's samples enter its film in sample
 // order, so each scene's film is the one a single-scene handle gives after `spp` passes with the
 // same seed (the path tracer's counter-based RNG is keyed by pixel and sample, not by launch).
 #include <cuda_runtime.h>
