@@ -789,6 +789,8 @@ def main():
         "frame_loop": {"value": fl_value, "unit": UNIT, "frames": S, "ms_per_frame": fl_s / S * 1e3,
                        "fraction_of_value": fl_value / value, "tail_bounce": frame_tuning["tail_bounce"],
                        "tail_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["ms_per_frame"].items()},
+                       "shadow_sort": frame_tuning["pass_shadow_sort"],
+                       "shadow_sort_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["shadow_sort_ms_per_frame"].items()},
                        "pixel_tiles": k_pixel_tiles, "kernels_ms_per_frame": fl_kernels,
                        "loop": "per frame: dfpt_set_camera(pinned host) + dfpt_render(1 pass) + dfpt_read_bgra8(pinned host), "
                                "as DayflowerApplication's execute/get loop"},

@@ -179,21 +179,32 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbos
 
 
 def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), verbose: bool = False) -> dict:
-    """Picks the tail launch for one-pass calls (the interactive frame loop): times `frames` calls of
-    dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and sets the fastest.
-    Every candidate gives each path the same steps; only the launch structure changes."""
-    results = {}
-    for t in candidates:
-        kernel.set_tuning("tail_bounce", t)
+    """Picks the launch structure of one-pass calls (the interactive frame loop): times `frames`
+    calls of dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and sets the
+    fastest, then keeps or drops the binning of the shadow rays (`pass_shadow_sort`: its scan has a
+    fixed cost that small frames may not earn back). Every choice gives each path the same steps;
+    only the launch structure and the processing order change."""
+    def frame_ms():
         kernel.execute(1)
         kernel.synchronize()
         t0 = time.perf_counter()
         for _ in range(frames):
             kernel.execute(1)
         kernel.synchronize()
-        results[t] = (time.perf_counter() - t0) / frames * 1e3
+        return (time.perf_counter() - t0) / frames * 1e3
+
+    results = {}
+    for t in candidates:
+        kernel.set_tuning("tail_bounce", t)
+        results[t] = frame_ms()
         if verbose:
             print(f"tail_bounce {t}: {results[t]:.3f} ms/frame", flush=True)
     best = min(results, key=results.get)
     kernel.set_tuning("tail_bounce", best)
-    return {"tail_bounce": best, "ms_per_frame": results}
+    sort = {kernel.get_tuning("pass_shadow_sort"): results[best]}
+    other = 1 - next(iter(sort))
+    kernel.set_tuning("pass_shadow_sort", other)
+    sort[other] = frame_ms()
+    kernel.set_tuning("pass_shadow_sort", min(sort, key=sort.get))
+    return {"tail_bounce": best, "ms_per_frame": results, "pass_shadow_sort": min(sort, key=sort.get),
+            "shadow_sort_ms_per_frame": sort}
