@@ -791,6 +791,8 @@ def main():
                        "tail_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["ms_per_frame"].items()},
                        "shadow_sort": frame_tuning["pass_shadow_sort"],
                        "shadow_sort_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["shadow_sort_ms_per_frame"].items()},
+                       "ray_sort": frame_tuning["pass_ray_sort"],
+                       "ray_sort_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["ray_sort_ms_per_frame"].items()},
                        "pixel_tiles": k_pixel_tiles, "kernels_ms_per_frame": fl_kernels,
                        "loop": "per frame: dfpt_set_camera(pinned host) + dfpt_render(1 pass) + dfpt_read_bgra8(pinned host), "
                                "as DayflowerApplication's execute/get loop"},

@@ -471,6 +471,12 @@ struct dfpt_handle {
     DevBuf<float4> p_s2_o, p_s2_d, p_s2_c;    // the binned copy of the shadow queue
     size_t p_s2_capacity = 0;
     DevPass pass_shadow2{};                   // `pass` reading the binned copy
+    // Plain passes: bounce 1's rays binned (direction bin over an origin grid of pass_ray_sort
+    // bits; 0 = off) between the shading of bounce 0 and their traversal.
+    int pass_ray_sort = 0;
+    DevBuf<float4> p_r2_o, p_r2_d;            // the binned copy of bounce 1's queue
+    DevPass pass_ray_count{};                 // `pass` with the bin counts (bounce 0's shading)
+    DevPass pass_ray_read{};                  // `pass` reading the binned copy (bounce 1)
     int wide_capacity = 0;
     size_t wide_shadow = 0;
     DevBuf<float4> w_q_o0, w_q_o1, w_q_d0, w_q_d1, w_s_o, w_s_d, w_s_c, w_throughput;  // w_throughput: throughput + radiance records (PSI)
@@ -539,6 +545,7 @@ void release(dfpt_handle* h) {
     h->mean.release();
     h->dev_params.release();
     h->p_sort_bins.release(); h->p_s2_o.release(); h->p_s2_d.release(); h->p_s2_c.release();
+    h->p_r2_o.release(); h->p_r2_d.release();
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
     // Lines the window marked persisting go back to normal with the records they cached.
@@ -746,14 +753,27 @@ int issue_pass(dfpt_handle* h) {
         // With tail_bounce t, bounces t .. nb - 1 and the final any-hit run in one tail launch.
         const int tb = (h->tail_bounce >= 1 && h->tail_bounce < nb && K.tail) ? h->tail_bounce : nb;
         mark(h, KIND_CAMERA); K.camera(c); ++k;
+        // With pass_ray_sort, bounce 0's shading counts the bins of the rays it queues, and bounce
+        // 1 (its traversal and shading, or the tail from there) reads them in bin order.
+        const bool sort_rays = h->pass_ray_sort > 0 && K.sort_rays && nb > 1 && h->pass_ray_read.q_o[1];
+        LaunchCtx c1 = c;
         for (int b = 0; b < tb; ++b) {
-            mark(h, KIND_TRACE); K.trace_closest(c, b); ++k;
-            mark(h, KIND_SHADE); K.shade(c, b); ++k;
+            mark(h, KIND_TRACE); K.trace_closest(c1, b); ++k;
+            if (b == 0 && sort_rays) {
+                LaunchCtx c0 = c;
+                c0.pass = &h->pass_ray_count;
+                mark(h, KIND_SHADE); K.shade(c0, b); ++k;
+                mark(h, KIND_SORT); k += K.sort_rays(c0, 1, h->pass_ray_read);
+                c1.pass = &h->pass_ray_read;
+            } else {
+                mark(h, KIND_SHADE); K.shade(c1, b); ++k;
+                c1.pass = &h->pass;
+            }
         }
         if (tb < nb) {
-            mark(h, KIND_TRACE); K.tail(c, tb, nb); ++k;
+            mark(h, KIND_TRACE); K.tail(c1, tb, nb); ++k;
         } else {
-            mark(h, KIND_FINAL); K.final_(c, nb); ++k;
+            mark(h, KIND_FINAL); K.final_(c1, nb); ++k;
         }
         // The sun shadow rays of all bounces, traced together (binned by origin cell first when
         // pass_shadow_sort is on: shading and the tail counted the bins).
@@ -1011,15 +1031,17 @@ int ensure_shadow_capacity(dfpt_handle* h) {
     return DFPT_OK;
 }
 
-// Plain passes' shadow binning: the bins and the binned copy of the shadow queue (as large as the
-// queue), or none; `pass` gets the bin pointers its shading counts into.
+// Plain passes' binning: the bins, the binned copy of the shadow queue (as large as the queue) and
+// of bounce 1's queue (a ray per pixel), or none; `pass` gets the bin pointers its shading counts
+// the shadow rays into, pass_ray_count those of bounce 1's rays.
 int pass_shadow_sort_prepare(dfpt_handle* h) {
     DevPass& B = h->pass;
-    if (!h->pass_shadow_sort) {
-        if (B.sort_count_shadow) {
+    if (!h->pass_shadow_sort && h->pass_ray_sort <= 0) {
+        if (B.sort_bins) {
             B.sort_bins = B.sort_count = B.sort_count_shadow = B.sort_partials = nullptr;
             h->graph_valid = false;
         }
+        h->pass_ray_read = DevPass{};
         return DFPT_OK;
     }
     if (!h->p_sort_bins.p) {
@@ -1034,15 +1056,30 @@ int pass_shadow_sort_prepare(dfpt_handle* h) {
         h->p_s2_capacity = h->shadow_capacity;
         h->graph_valid = false;
     }
-    if (B.sort_count_shadow != h->p_sort_bins.p + 2 * DFPT_SORT_BINS) h->graph_valid = false;
+    if (h->pass_ray_sort > 0 && !h->p_r2_o.p) {
+        CUDA_TRY(h->p_r2_o.alloc((size_t)h->n_pixels));
+        CUDA_TRY(h->p_r2_d.alloc((size_t)h->n_pixels));
+        h->graph_valid = false;
+    }
+    int* const shadow_counts = h->pass_shadow_sort ? h->p_sort_bins.p + 2 * DFPT_SORT_BINS : nullptr;
+    if (B.sort_count_shadow != shadow_counts || B.sort_bins != h->p_sort_bins.p) h->graph_valid = false;
     B.sort_bins = h->p_sort_bins.p;
-    B.sort_count = nullptr;  // the bounces' rays stay unbinned
-    B.sort_count_shadow = h->p_sort_bins.p + 2 * DFPT_SORT_BINS;
+    B.sort_count = nullptr;  // counted by bounce 0's shading only (pass_ray_count)
+    B.sort_count_shadow = shadow_counts;
     B.sort_partials = h->p_sort_bins.p + 3 * DFPT_SORT_BINS;
+    B.sort_ray_bits = h->pass_ray_sort;
     h->pass_shadow2 = B;
     h->pass_shadow2.s_o = h->p_s2_o.p;
     h->pass_shadow2.s_d = h->p_s2_d.p;
     h->pass_shadow2.s_c = h->p_s2_c.p;
+    h->pass_ray_count = B;
+    h->pass_ray_count.sort_count = h->p_sort_bins.p + DFPT_SORT_BINS;
+    h->pass_ray_read = DevPass{};
+    if (h->pass_ray_sort > 0) {
+        h->pass_ray_read = B;
+        h->pass_ray_read.q_o[1] = h->p_r2_o.p;
+        h->pass_ray_read.q_d[1] = h->p_r2_d.p;
+    }
     return DFPT_OK;
 }
 
@@ -1614,6 +1651,13 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "pass_ray_sort") == 0) {
+        if (value < 0 || value > 15 || value % 3 != 0)
+            return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "pass_ray_sort %d: 0 or origin-grid bits 3, 6, 9, 12, 15", value);
+        h->pass_ray_sort = value;
+        h->graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "tail_bounce") == 0) {
         if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %d outside [0, %d]", value, DFPT_MAX_DEPTH);
         h->tail_bounce = value;
@@ -1641,6 +1685,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "pixel_tiles") == 0) { *value = h->pixel_tiles ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "tail_bounce") == 0) { *value = h->tail_bounce; return DFPT_OK; }
     if (std::strcmp(key, "pass_shadow_sort") == 0) { *value = h->pass_shadow_sort ? 1 : 0; return DFPT_OK; }
+    if (std::strcmp(key, "pass_ray_sort") == 0) { *value = h->pass_ray_sort; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }

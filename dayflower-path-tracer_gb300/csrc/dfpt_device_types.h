@@ -161,6 +161,7 @@ struct DevPass {
     int* sort_count;           // DFPT_SORT_BINS ray counts of the next bounce; zero at rest (the scan clears them)
     int* sort_count_shadow;    // the same for the sun shadow rays
     int* sort_partials;        // DFPT_SORT_CHUNKS chunk sums of the scan
+    int sort_ray_bits;         // plain passes: origin-grid bits of the bounce rays' bins (plain_ray_bin)
 };
 // Bins: waves of several scenes use 3 bits of scene (within a wave) x a 6 x 4 x 4 cube-map
 // direction bin (7 bits) x 12 bits of origin cell (bounce rays), or 3 bits of scene x 18 bits of

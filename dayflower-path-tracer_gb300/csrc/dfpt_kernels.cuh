@@ -953,6 +953,12 @@ __device__ __forceinline__ int ray_bin_in_wave(const DevBatch& Q, int first, flo
 #endif
 }
 
+// A plain pass's bounce ray: a 6 x 4 x 4 cube-map direction bin over an origin grid of `bits`
+// bits (a multiple of 3, at most 15).
+__device__ __forceinline__ int plain_ray_bin(const DevScene& S, float4 o, float4 d, int bits) {
+    return (cube_dir_bin<4>(d) << bits) | cell_bits(S, o, bits);
+}
+
 // Bin counts with one atomic per distinct bin of a warp.
 __device__ __forceinline__ void bin_count(int* bins, int key) {
     const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
@@ -1145,7 +1151,9 @@ __global__ void __launch_bounds__(256, DFPT_SHADE_MINB) k_shade(DevScene S0, con
                 if (B.sort_count_shadow) bin_count(B.sort_count_shadow, emit_shadow ? shadow_bin_in_wave(Q, first, so, sd) : -1);
             }
         } else {
-            // Plain passes may bin the deferred shadow rays alone (origin cells).
+            // Plain passes may bin the next bounce's rays (the record of one bounce carries
+            // sort_count) and the deferred shadow rays (origin cells).
+            if (B.sort_count) bin_count(B.sort_count, emit_next ? plain_ray_bin(S0, no, nd, B.sort_ray_bits) : -1);
             if (B.sort_count_shadow) bin_count(B.sort_count_shadow, emit_shadow ? cell_bits(S0, so, DFPT_SHADOW_CELL_BITS) : -1);
         }
         const int sslot = warp_push(B.counts + DFPT_COUNTS_SHADOW, emit_shadow);
@@ -1822,13 +1830,22 @@ __global__ void __launch_bounds__(256) k_sort_chunk_sums(DevPass B, const int* _
     block_exclusive_scan_256(c.x + c.y + c.z + c.w, total);
     if (threadIdx.x == 0) B.sort_partials[blockIdx.x] = total;
 }
-__global__ void __launch_bounds__(256) k_sort_chunk_offsets(DevPass B) {
+// Scans the first `chunks` chunk sums (the rest of the bins are empty).
+__global__ void __launch_bounds__(256) k_sort_chunk_offsets(DevPass B, int chunks) {
     constexpr int PER = DFPT_SORT_CHUNKS / 256;
     int v[PER], sum = 0;
-    for (int j = 0; j < PER; ++j) { v[j] = B.sort_partials[PER * threadIdx.x + j]; sum += v[j]; }
+    for (int j = 0; j < PER; ++j) {
+        const int k = PER * threadIdx.x + j;
+        v[j] = k < chunks ? B.sort_partials[k] : 0;
+        sum += v[j];
+    }
     int total;
     int run = block_exclusive_scan_256(sum, total);
-    for (int j = 0; j < PER; ++j) { B.sort_partials[PER * threadIdx.x + j] = run; run += v[j]; }
+    for (int j = 0; j < PER; ++j) {
+        const int k = PER * threadIdx.x + j;
+        if (k < chunks) B.sort_partials[k] = run;
+        run += v[j];
+    }
 }
 __global__ void __launch_bounds__(256) k_sort_chunk_scan(DevPass B, int* counts) {
     int4* cp = reinterpret_cast<int4*>(counts + (size_t)blockIdx.x * 1024) + threadIdx.x;
@@ -1865,10 +1882,36 @@ __global__ void __launch_bounds__(256) k_sort_shadow_scatter_plain(DevScene S, D
         }
     }
 }
-static void launch_sort_scan(const LaunchCtx& c, int* counts) {
-    k_sort_chunk_sums<<<DFPT_SORT_CHUNKS, 256, 0, c.stream>>>(*c.pass, counts);
-    k_sort_chunk_offsets<<<1, 256, 0, c.stream>>>(*c.pass);
-    k_sort_chunk_scan<<<DFPT_SORT_CHUNKS, 256, 0, c.stream>>>(*c.pass, counts);
+// The rays a plain pass's shading queued for `bounce` into `out` in bin order (direction bin over
+// origin cell; the counts come from that shading, the offsets from the scan).
+__global__ void __launch_bounds__(256) k_sort_rays_scatter_plain(DevScene S, DevPass B, int bounce, float4* out_o, float4* out_d) {
+    const int n = B.counts[bounce];
+    const int qi = bounce & 1;
+    GRID_STRIDE_UNIFORM(i, n) {
+        int key = -1;
+        float4 o, d;
+        if (i < n) {
+            o = B.q_o[qi][i];
+            d = B.q_d[qi][i];
+            key = plain_ray_bin(S, o, d, B.sort_ray_bits);
+        }
+        const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
+        const int leader = __ffs(same) - 1;
+        int base = 0;
+        if (key >= 0 && (int)(threadIdx.x & 31) == leader) base = atomicAdd(B.sort_bins + key, __popc(same));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (key >= 0) {
+            const int pos = base + __popc(same & ((1u << (threadIdx.x & 31)) - 1u));
+            out_o[pos] = o;
+            out_d[pos] = d;
+        }
+    }
+}
+// `chunks` chunks of 1024 bins hold every key (keys below chunks x 1024).
+static void launch_sort_scan(const LaunchCtx& c, int* counts, int chunks = DFPT_SORT_CHUNKS) {
+    k_sort_chunk_sums<<<chunks, 256, 0, c.stream>>>(*c.pass, counts);
+    k_sort_chunk_offsets<<<1, 256, 0, c.stream>>>(*c.pass, chunks);
+    k_sort_chunk_scan<<<chunks, 256, 0, c.stream>>>(*c.pass, counts);
 }
 
 __global__ void __launch_bounds__(256) k_sort_scatter(DevBatch Q, DevPass B, int bounce) {
@@ -2152,8 +2195,16 @@ static void launch_end_pass(const LaunchCtx& c) { k_end_pass<<<1, 32, 0, c.strea
 // Bins a plain pass's deferred shadow rays into `to` (a pass record whose s_* point at the second
 // set); shading counted the bins. Returns the kernels launched.
 static int launch_sort_shadow(const LaunchCtx& c, const DevPass& to) {
-    launch_sort_scan(c, c.pass->sort_count_shadow);
+    launch_sort_scan(c, c.pass->sort_count_shadow, (1 << DFPT_SHADOW_CELL_BITS) / 1024);
     k_sort_shadow_scatter_plain<<<c.grid, 256, 0, c.stream>>>(*c.scene, *c.pass, to.s_o, to.s_d, to.s_c);
+    return 4;
+}
+// Bins the rays a plain pass queued for `bounce` into `to` (a pass record whose queue of that
+// bounce's parity points at the second set); c.pass is the record the shading counted with.
+static int launch_sort_rays(const LaunchCtx& c, int bounce, const DevPass& to) {
+    const int qi = bounce & 1;
+    launch_sort_scan(c, c.pass->sort_count, ((96 << c.pass->sort_ray_bits) + 1023) / 1024);
+    k_sort_rays_scatter_plain<<<c.grid, 256, 0, c.stream>>>(*c.scene, *c.pass, bounce, to.q_o[qi], to.q_d[qi]);
     return 4;
 }
 static void launch_film_mean(const LaunchCtx& c, double* out3) { k_film_mean<<<c.grid, 256, 0, c.stream>>>(*c.pass, out3); }
@@ -2191,6 +2242,7 @@ KernelSet kernel_set() {
     k.film = launch_film;
     k.end_pass = launch_end_pass;
     k.sort_shadow = launch_sort_shadow;
+    k.sort_rays = launch_sort_rays;
     k.film_mean = launch_film_mean;
     k.film_average = launch_film_average;
 #endif

@@ -30,6 +30,7 @@ struct KernelSet {
     void (*film)(const LaunchCtx&);
     void (*end_pass)(const LaunchCtx&);
     int (*sort_shadow)(const LaunchCtx&, const DevPass& to) = nullptr;  // plain passes: bins the deferred shadow rays
+    int (*sort_rays)(const LaunchCtx&, int bounce, const DevPass& to) = nullptr;  // plain passes: bins a bounce's rays
     void (*film_mean)(const LaunchCtx&, double* out3);
     void (*film_average)(const LaunchCtx&, float* rgb, int* samples);
     void (*init_tables)(cudaStream_t, const int* perm256, const float* grad36);

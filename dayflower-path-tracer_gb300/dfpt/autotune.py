@@ -178,12 +178,15 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbos
             "shadow_defer": kernel.get_tuning("shadow_defer"), "defer_ms_per_step": {str(k): round(v, 3) for k, v in defer.items()}}
 
 
-def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), verbose: bool = False) -> dict:
+def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), ray_sort=(0, 9, 12, 15),
+               verbose: bool = False) -> dict:
     """Picks the launch structure of one-pass calls (the interactive frame loop): times `frames`
     calls of dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and sets the
     fastest, then keeps or drops the binning of the shadow rays (`pass_shadow_sort`: its scan has a
-    fixed cost that small frames may not earn back). Every choice gives each path the same steps;
-    only the launch structure and the processing order change."""
+    fixed cost that small frames may not earn back), then picks the binning of bounce 1's rays
+    (`pass_ray_sort`: 0 = none, else the origin grid's bits) and times the tail candidates once
+    more with it. Every choice gives each path the same steps; only the launch structure and the
+    processing order change."""
     def frame_ms():
         kernel.execute(1)
         kernel.synchronize()
@@ -206,5 +209,20 @@ def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), verbose: bo
     kernel.set_tuning("pass_shadow_sort", other)
     sort[other] = frame_ms()
     kernel.set_tuning("pass_shadow_sort", min(sort, key=sort.get))
+    rays = {}
+    for bits in ray_sort:
+        kernel.set_tuning("pass_ray_sort", bits)
+        rays[bits] = frame_ms()
+        if verbose:
+            print(f"pass_ray_sort {bits}: {rays[bits]:.3f} ms/frame", flush=True)
+    bits = min(rays, key=rays.get)
+    kernel.set_tuning("pass_ray_sort", bits)
+    if bits:
+        # The tail may start elsewhere once bounce 1's rays arrive in bin order.
+        for t in candidates:
+            kernel.set_tuning("tail_bounce", t)
+            results[t] = frame_ms()
+        best = min(results, key=results.get)
+        kernel.set_tuning("tail_bounce", best)
     return {"tail_bounce": best, "ms_per_frame": results, "pass_shadow_sort": min(sort, key=sort.get),
-            "shadow_sort_ms_per_frame": sort}
+            "shadow_sort_ms_per_frame": sort, "pass_ray_sort": bits, "ray_sort_ms_per_frame": rays}

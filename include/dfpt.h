@@ -240,7 +240,10 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *   "pass_shadow_sort"  1 (default): a plain pass bins its deferred sun shadow rays by origin cell
  *                       before their launch (processing order only; a second copy of the shadow
  *                       queue); 0 in queue order;
- *   "ray_sort"          1 (default) bins rays by direction and origin cell between the bounces of
+ *   "pass_ray_sort"     0 (default): a plain pass traces bounce 1's rays in queue order; 3, 6, 9,
+ *                       12 or 15: in bins of a 6 x 4 x 4 cube-map direction over an origin grid of
+ *                       that many bits (processing order only; a second copy of bounce 1's queue);
+ *   "ray_sort"       1 (default) bins rays by direction and origin cell between the bounces of
  *                       wide passes (processing order only);
  *   "shadow_sort"       with ray_sort, 1 (default) also bins the sun shadow rays by origin cell
  *                       before their launch;

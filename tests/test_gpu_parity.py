@@ -328,15 +328,18 @@ def test_tail_launch_equals_per_bounce_launches(scenes, name):
     one launch) takes every path through the same steps as a launch per bounce: the same films
     (sun contributions are added with float atomics: a few ulps), the same segments, nodes and
     triangles, the same selection buffer - with the deferred shadow rays binned by origin cell
-    before their launch (pass_shadow_sort) or not."""
+    before their launch (pass_shadow_sort) or not, and with bounce 1's rays binned by direction and
+    origin cell (pass_ray_sort, the grid's bits) or not."""
     scene, sky, params, (w, h) = scenes[name]
     params = dict(params, renderer_type=2, pt_ray_depth_maximum=6, pt_ray_depth_russian_roulette=3)
     ref = None
-    for tb, sort in ((0, 0), (1, 0), (2, 0), (5, 0), (0, 1), (2, 1)):
+    for tb, sort, rays in ((0, 0, 0), (1, 0, 0), (2, 0, 0), (5, 0, 0), (0, 1, 0), (2, 1, 0),
+                           (0, 0, 9), (1, 1, 12), (2, 1, 6), (0, 1, 15)):
         k = _kernel(scene, sky, params, w, h, strict=False)
         k.set_tuning("wide_samples", 1)
         k.set_tuning("tail_bounce", tb)
         k.set_tuning("pass_shadow_sort", sort)
+        k.set_tuning("pass_ray_sort", rays)
         k.set_counting(True)
         k.execute(4)
         film, samples = k.film()
@@ -346,6 +349,6 @@ def test_tail_launch_equals_per_bounce_launches(scenes, name):
         if ref is None:
             ref = got
             continue
-        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, sort, np.abs(got[0] - ref[0]).max())
-        assert np.array_equal(got[1], ref[1]), (tb, sort, got[1], ref[1])
-        assert np.array_equal(got[2], ref[2]), (tb, sort)
+        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, sort, rays, np.abs(got[0] - ref[0]).max())
+        assert np.array_equal(got[1], ref[1]), (tb, sort, rays, got[1], ref[1])
+        assert np.array_equal(got[2], ref[2]), (tb, sort, rays)
