@@ -789,6 +789,8 @@ def main():
         "frame_loop": {"value": fl_value, "unit": UNIT, "frames": S, "ms_per_frame": fl_s / S * 1e3,
                        "fraction_of_value": fl_value / value, "tail_bounce": frame_tuning["tail_bounce"],
                        "tail_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["ms_per_frame"].items()},
+                       "tail_blocks": frame_tuning["tail_blocks"],
+                       "tail_blocks_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["tail_blocks_ms_per_frame"].items()},
                        "shadow_sort": frame_tuning["pass_shadow_sort"],
                        "shadow_sort_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["shadow_sort_ms_per_frame"].items()},
                        "ray_sort": frame_tuning["pass_ray_sort"],

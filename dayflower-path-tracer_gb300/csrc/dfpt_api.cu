@@ -1658,6 +1658,12 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "tail_blocks") == 0) {
+        if (value < 2 || value > 4) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_blocks %d outside [2, 4]", value);
+        h->ctx.tail_blocks = value;
+        h->graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "tail_bounce") == 0) {
         if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %d outside [0, %d]", value, DFPT_MAX_DEPTH);
         h->tail_bounce = value;
@@ -1686,6 +1692,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (std::strcmp(key, "tail_bounce") == 0) { *value = h->tail_bounce; return DFPT_OK; }
     if (std::strcmp(key, "pass_shadow_sort") == 0) { *value = h->pass_shadow_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "pass_ray_sort") == 0) { *value = h->pass_ray_sort; return DFPT_OK; }
+    if (std::strcmp(key, "tail_blocks") == 0) { *value = h->ctx.tail_blocks; return DFPT_OK; }
     if (std::strcmp(key, "ray_sort") == 0) { *value = h->ray_sort ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_defer") == 0) { *value = h->shadow_defer ? 1 : 0; return DFPT_OK; }
     if (std::strcmp(key, "shadow_sort") == 0) { *value = h->shadow_sort ? 1 : 0; return DFPT_OK; }

@@ -2025,22 +2025,33 @@ struct TraceCfg {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<false, false, V, BLOCK, MINB>, BLOCK, 0);
         return sms * (b > 0 ? b : 1);
     }
-    // The tail kernel: traversal and shading in one kernel, compiled for two resident blocks; its
-    // grid (SMs x resident blocks) is found once per process. Its walk is the configuration's when
-    // that is the threaded walk (0) or the compact pair walk (5), else the prefetching walk (1),
-    // so that three instantiations serve every configuration (the other walks lost to these in
-    // whole launches).
+    // The tail kernel: traversal and shading in one kernel, compiled for 2 resident blocks of 256,
+    // and with the compact pair walk of the fast set also for 3 or 4 (c.tail_blocks: fewer
+    // registers, more warps to hide the walk's load latency); its grid (SMs x resident blocks) is
+    // found once per process. Its walk is the configuration's when that is the threaded walk (0)
+    // or the compact pair walk (5), else the prefetching walk (1), so that three walks serve every
+    // configuration (the other walks lost to these in whole launches).
     static constexpr int TVV = (V == 0 || V == 5) ? V : 1;
-    static void tail(const LaunchCtx& c, int b0, int nb) {
+    template <int TB>
+    static void tail_t(const LaunchCtx& c, int b0, int nb) {
         static int grid_tail = 0;
         if (grid_tail == 0) {
             int dev = 0, sms = 0, b = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tail<TVV, 256, 2>, 256, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tail<TVV, 256, TB>, 256, 0);
             grid_tail = (sms > 0 ? sms : 1) * (b > 0 ? b : 1);
         }
-        k_tail<TVV, 256, 2><<<grid_tail, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, b0, nb);
+        k_tail<TVV, 256, TB><<<grid_tail, 256, 0, c.stream>>>(*c.scene, c.params, *c.pass, b0, nb);
+    }
+    static void tail(const LaunchCtx& c, int b0, int nb) {
+#ifdef DFPT_EXTENDED_KERNELS
+        if constexpr (TVV == 5) {
+            if (c.tail_blocks >= 4) { tail_t<4>(c, b0, nb); return; }
+            if (c.tail_blocks == 3) { tail_t<3>(c, b0, nb); return; }
+        }
+#endif
+        tail_t<2>(c, b0, nb);
     }
 #endif
 #ifdef DFPT_EXTENDED_KERNELS

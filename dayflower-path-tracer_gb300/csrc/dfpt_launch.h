@@ -16,6 +16,7 @@ struct LaunchCtx {
     int grid, grid_trace, grid_simple;
     int trace_config;  // index into the kernel set's traversal configurations
     const DevBatch* batch = nullptr;  // batch launches only
+    int tail_blocks = 2;              // resident blocks per SM the tail kernel is compiled for (2-4)
 };
 
 struct KernelSet {

@@ -178,15 +178,16 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbos
             "shadow_defer": kernel.get_tuning("shadow_defer"), "defer_ms_per_step": {str(k): round(v, 3) for k, v in defer.items()}}
 
 
-def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), ray_sort=(0, 9, 12, 15),
+def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), blocks=(2, 3, 4), ray_sort=(0, 9, 12, 15),
                verbose: bool = False) -> dict:
     """Picks the launch structure of one-pass calls (the interactive frame loop): times `frames`
-    calls of dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and sets the
-    fastest, then keeps or drops the binning of the shadow rays (`pass_shadow_sort`: its scan has a
-    fixed cost that small frames may not earn back), then picks the binning of bounce 1's rays
-    (`pass_ray_sort`: 0 = none, else the origin grid's bits) and times the tail candidates once
-    more with it. Every choice gives each path the same steps; only the launch structure and the
-    processing order change."""
+    calls of dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and per
+    `tail_blocks` (resident blocks of the tail kernel) and sets the fastest pair, then keeps or
+    drops the binning of the shadow rays (`pass_shadow_sort`: its scan has a fixed cost that small
+    frames may not earn back), then picks the binning of bounce 1's rays (`pass_ray_sort`: 0 =
+    none, else the origin grid's bits) and times the tail candidates once more with it. Every
+    choice gives each path the same steps; only the launch structure and the processing order
+    change."""
     def frame_ms():
         kernel.execute(1)
         kernel.synchronize()
@@ -196,15 +197,25 @@ def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), ray_sort=(0
         kernel.synchronize()
         return (time.perf_counter() - t0) / frames * 1e3
 
-    results = {}
-    for t in candidates:
+    def sweep_tail():
+        table = {}
+        for b in blocks:
+            kernel.set_tuning("tail_blocks", b)
+            for t in candidates:
+                if t == 0 and b != blocks[0]:
+                    table[(b, t)] = table[(blocks[0], 0)]  # no tail launch: the blocks do not matter
+                    continue
+                kernel.set_tuning("tail_bounce", t)
+                table[(b, t)] = frame_ms()
+                if verbose:
+                    print(f"tail_blocks {b} tail_bounce {t}: {table[(b, t)]:.3f} ms/frame", flush=True)
+        b, t = min(table, key=table.get)
+        kernel.set_tuning("tail_blocks", b)
         kernel.set_tuning("tail_bounce", t)
-        results[t] = frame_ms()
-        if verbose:
-            print(f"tail_bounce {t}: {results[t]:.3f} ms/frame", flush=True)
-    best = min(results, key=results.get)
-    kernel.set_tuning("tail_bounce", best)
-    sort = {kernel.get_tuning("pass_shadow_sort"): results[best]}
+        return table, b, t
+
+    table, tb_blocks, best = sweep_tail()
+    sort = {kernel.get_tuning("pass_shadow_sort"): table[(tb_blocks, best)]}
     other = 1 - next(iter(sort))
     kernel.set_tuning("pass_shadow_sort", other)
     sort[other] = frame_ms()
@@ -219,10 +230,9 @@ def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), ray_sort=(0
     kernel.set_tuning("pass_ray_sort", bits)
     if bits:
         # The tail may start elsewhere once bounce 1's rays arrive in bin order.
-        for t in candidates:
-            kernel.set_tuning("tail_bounce", t)
-            results[t] = frame_ms()
-        best = min(results, key=results.get)
-        kernel.set_tuning("tail_bounce", best)
-    return {"tail_bounce": best, "ms_per_frame": results, "pass_shadow_sort": min(sort, key=sort.get),
-            "shadow_sort_ms_per_frame": sort, "pass_ray_sort": bits, "ray_sort_ms_per_frame": rays}
+        table, tb_blocks, best = sweep_tail()
+    return {"tail_bounce": best, "tail_blocks": tb_blocks,
+            "ms_per_frame": {t: table[(tb_blocks, t)] for t in candidates},
+            "tail_blocks_ms_per_frame": {b: min(table[(b, t)] for t in candidates) for b in blocks},
+            "pass_shadow_sort": min(sort, key=sort.get), "shadow_sort_ms_per_frame": sort,
+            "pass_ray_sort": bits, "ray_sort_ms_per_frame": rays}

@@ -237,6 +237,10 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       of 4, counter-based RNG, path tracer without wireframes), 0 in row order;
  *   "tail_bounce"       t >= 1: a plain pass runs bounces t .. depth-1 and the final any-hit of each
  *                       path in one launch (same steps per path); 0 (default) a launch per bounce;
+ *   "tail_blocks"       2 (default), 3 or 4: resident blocks of 256 threads per SM the tail launch
+ *                       is compiled for (fewer registers per thread, more warps) when it walks with
+ *                       the compact pair walk (configurations 16 and 17) in the fast kernel set; other
+ *                       walks and the strict set use 2;
  *   "pass_shadow_sort"  1 (default): a plain pass bins its deferred sun shadow rays by origin cell
  *                       before their launch (processing order only; a second copy of the shadow
  *                       queue); 0 in queue order;

@@ -325,18 +325,20 @@ def test_pixel_tile_order_keeps_every_pixel(scenes):
 @pytest.mark.parametrize("name", ["spheres", "meshes"])
 def test_tail_launch_equals_per_bounce_launches(scenes, name):
     """The tail kernel (tail_bounce t: bounces t .. depth-1 and the final any-hit of each path in
-    one launch) takes every path through the same steps as a launch per bounce: the same films
-    (sun contributions are added with float atomics: a few ulps), the same segments, nodes and
-    triangles, the same selection buffer - with the deferred shadow rays binned by origin cell
-    before their launch (pass_shadow_sort) or not, and with bounce 1's rays binned by direction and
-    origin cell (pass_ray_sort, the grid's bits) or not."""
+    one launch, compiled for 2, 3 or 4 resident blocks) takes every path through the same steps as a
+    launch per bounce: the same films (sun contributions are added with float atomics: a few ulps),
+    the same segments, nodes and triangles, the same selection buffer - with the deferred shadow
+    rays binned by origin cell before their launch (pass_shadow_sort) or not, and with bounce 1's
+    rays binned by direction and origin cell (pass_ray_sort, the grid's bits) or not."""
     scene, sky, params, (w, h) = scenes[name]
     params = dict(params, renderer_type=2, pt_ray_depth_maximum=6, pt_ray_depth_russian_roulette=3)
     ref = None
-    for tb, sort, rays in ((0, 0, 0), (1, 0, 0), (2, 0, 0), (5, 0, 0), (0, 1, 0), (2, 1, 0),
-                           (0, 0, 9), (1, 1, 12), (2, 1, 6), (0, 1, 15)):
+    for tb, sort, rays, blocks in ((0, 0, 0, 2), (1, 0, 0, 2), (2, 0, 0, 2), (5, 0, 0, 2), (0, 1, 0, 2),
+                                   (2, 1, 0, 2), (1, 1, 0, 3), (2, 1, 0, 4), (0, 0, 9, 2), (1, 1, 12, 3),
+                                   (2, 1, 6, 2), (0, 1, 15, 2)):
         k = _kernel(scene, sky, params, w, h, strict=False)
         k.set_tuning("wide_samples", 1)
+        k.set_tuning("tail_blocks", blocks)
         k.set_tuning("tail_bounce", tb)
         k.set_tuning("pass_shadow_sort", sort)
         k.set_tuning("pass_ray_sort", rays)
@@ -349,6 +351,6 @@ def test_tail_launch_equals_per_bounce_launches(scenes, name):
         if ref is None:
             ref = got
             continue
-        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, sort, rays, np.abs(got[0] - ref[0]).max())
-        assert np.array_equal(got[1], ref[1]), (tb, sort, rays, got[1], ref[1])
-        assert np.array_equal(got[2], ref[2]), (tb, sort, rays)
+        assert np.allclose(got[0], ref[0], rtol=1e-5, atol=1e-6), (tb, sort, rays, blocks, np.abs(got[0] - ref[0]).max())
+        assert np.array_equal(got[1], ref[1]), (tb, sort, rays, blocks, got[1], ref[1])
+        assert np.array_equal(got[2], ref[2]), (tb, sort, rays, blocks)
