@@ -706,7 +706,8 @@ def main():
     # launch for one-pass calls picked first, outside the timed frames).
     from dfpt.autotune import tune_frame
 
-    frame_tuning = tune_frame(k)
+    main_config = k.get_tuning("trace_config")
+    frame_tuning = tune_frame(k, configs=tuple(dict.fromkeys((main_config, 16, 17))))
     k_pixel_tiles = k.get_tuning("pixel_tiles")
     fl_s = frame_loop(k, cam, host_img, S, max(3, args.warmup), barrier)
     fl_kernels = frame_kernels(k)
@@ -789,6 +790,8 @@ def main():
         "frame_loop": {"value": fl_value, "unit": UNIT, "frames": S, "ms_per_frame": fl_s / S * 1e3,
                        "fraction_of_value": fl_value / value, "tail_bounce": frame_tuning["tail_bounce"],
                        "tail_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["ms_per_frame"].items()},
+                       "trace_config": frame_tuning["trace_config"],
+                       "config_ms_per_frame": {str(c): round(v, 3) for c, v in frame_tuning["config_ms_per_frame"].items()},
                        "tail_blocks": frame_tuning["tail_blocks"],
                        "tail_blocks_ms_per_frame": {str(t): round(v, 3) for t, v in frame_tuning["tail_blocks_ms_per_frame"].items()},
                        "shadow_sort": frame_tuning["pass_shadow_sort"],

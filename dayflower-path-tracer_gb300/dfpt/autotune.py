@@ -179,10 +179,12 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbos
 
 
 def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), blocks=(2, 3, 4), ray_sort=(0, 9, 12, 15),
-               verbose: bool = False) -> dict:
+               configs=None, verbose: bool = False) -> dict:
     """Picks the launch structure of one-pass calls (the interactive frame loop): times `frames`
     calls of dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and per
-    `tail_blocks` (resident blocks of the tail kernel) and sets the fastest pair, then keeps or
+    `tail_blocks` (resident blocks of the tail kernel) - for each traversal configuration in
+    `configs` when given (the primary rays', shadow rays' and tail's walk), else the handle's - and
+    sets the fastest, then keeps or
     drops the binning of the shadow rays (`pass_shadow_sort`: its scan has a fixed cost that small
     frames may not earn back), then picks the binning of bounce 1's rays (`pass_ray_sort`: 0 =
     none, else the origin grid's bits) and times the tail candidates once more with it. Every
@@ -214,7 +216,20 @@ def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), blocks=(2, 
         kernel.set_tuning("tail_bounce", t)
         return table, b, t
 
-    table, tb_blocks, best = sweep_tail()
+    if configs:
+        per_config = {}
+        for cfg in configs:
+            kernel.set_tuning("trace_config", cfg)
+            t_cfg, b_cfg, best_cfg = sweep_tail()
+            per_config[cfg] = (t_cfg[(b_cfg, best_cfg)], t_cfg, b_cfg, best_cfg)
+        cfg = min(per_config, key=lambda c: per_config[c][0])
+        kernel.set_tuning("trace_config", cfg)
+        _, table, tb_blocks, best = per_config[cfg]
+        kernel.set_tuning("tail_blocks", tb_blocks)
+        kernel.set_tuning("tail_bounce", best)
+    else:
+        per_config = {}
+        table, tb_blocks, best = sweep_tail()
     sort = {kernel.get_tuning("pass_shadow_sort"): table[(tb_blocks, best)]}
     other = 1 - next(iter(sort))
     kernel.set_tuning("pass_shadow_sort", other)
@@ -231,7 +246,9 @@ def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), blocks=(2, 
     if bits:
         # The tail may start elsewhere once bounce 1's rays arrive in bin order.
         table, tb_blocks, best = sweep_tail()
-    return {"tail_bounce": best, "tail_blocks": tb_blocks,
+    return {"trace_config": kernel.get_tuning("trace_config"),
+            "config_ms_per_frame": {c: v[0] for c, v in per_config.items()},
+            "tail_bounce": best, "tail_blocks": tb_blocks,
             "ms_per_frame": {t: table[(tb_blocks, t)] for t in candidates},
             "tail_blocks_ms_per_frame": {b: min(table[(b, t)] for t in candidates) for b in blocks},
             "pass_shadow_sort": min(sort, key=sort.get), "shadow_sort_ms_per_frame": sort,
