@@ -464,7 +464,7 @@ struct dfpt_handle {
     // batch stages (one scene), so each launch carries k samples per pixel (see render_wide).
     int wide_samples = 8;
     bool pixel_tiles = true;   // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
-    int tail_bounce = 0;       // plain passes: first bounce of the tail launch (0: a launch per bounce)
+    int tail_bounce = -1;      // plain passes: first bounce of the tail launch (-1: a launch per bounce)
     // Plain passes: the deferred shadow rays binned by origin cell before their launch.
     bool pass_shadow_sort = true;
     DevBuf<int> p_sort_bins;                  // offsets, (unused), shadow counts, chunk sums
@@ -750,8 +750,9 @@ int issue_pass(dfpt_handle* h) {
         mark(h, KIND_SIMPLE); K.simple(c); ++k;
     } else {
         const int nb = h->params.pt_ray_depth_maximum < 1 ? 1 : (h->params.pt_ray_depth_maximum > DFPT_MAX_DEPTH ? DFPT_MAX_DEPTH : h->params.pt_ray_depth_maximum);
-        // With tail_bounce t, bounces t .. nb - 1 and the final any-hit run in one tail launch.
-        const int tb = (h->tail_bounce >= 1 && h->tail_bounce < nb && K.tail) ? h->tail_bounce : nb;
+        // With tail_bounce t, bounces t .. nb - 1 and the final any-hit run in one tail launch (t = 0:
+        // the camera rays' traversal and shading too).
+        const int tb = (h->tail_bounce >= 0 && h->tail_bounce < nb && K.tail) ? h->tail_bounce : nb;
         mark(h, KIND_CAMERA); K.camera(c); ++k;
         // With pass_ray_sort, bounce 0's shading counts the bins of the rays it queues, and bounce
         // 1 (its traversal and shading, or the tail from there) reads them in bin order.
@@ -1665,7 +1666,7 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         return DFPT_OK;
     }
     if (std::strcmp(key, "tail_bounce") == 0) {
-        if (value < 0 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %d outside [0, %d]", value, DFPT_MAX_DEPTH);
+        if (value < -1 || value > DFPT_MAX_DEPTH) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "tail_bounce %d outside [-1, %d]", value, DFPT_MAX_DEPTH);
         h->tail_bounce = value;
         h->graph_valid = false;
         return DFPT_OK;

@@ -178,10 +178,10 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbos
             "shadow_defer": kernel.get_tuning("shadow_defer"), "defer_ms_per_step": {str(k): round(v, 3) for k, v in defer.items()}}
 
 
-def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), blocks=(2, 3, 4), ray_sort=(0, 9, 12, 15),
+def tune_frame(kernel, frames: int = 16, candidates=(-1, 0, 1, 2, 3, 4), blocks=(2, 3, 4), ray_sort=(0, 9, 12, 15),
                configs=None, verbose: bool = False) -> dict:
     """Picks the launch structure of one-pass calls (the interactive frame loop): times `frames`
-    calls of dfpt_render(1) per `tail_bounce` candidate (0 = a launch per bounce) and per
+    calls of dfpt_render(1) per `tail_bounce` candidate (-1 = a launch per bounce) and per
     `tail_blocks` (resident blocks of the tail kernel) - for each traversal configuration in
     `configs` when given (the primary rays', shadow rays' and tail's walk), else the handle's - and
     sets the fastest, then keeps or
@@ -204,8 +204,8 @@ def tune_frame(kernel, frames: int = 16, candidates=(0, 1, 2, 3, 4), blocks=(2, 
         for b in blocks:
             kernel.set_tuning("tail_blocks", b)
             for t in candidates:
-                if t == 0 and b != blocks[0]:
-                    table[(b, t)] = table[(blocks[0], 0)]  # no tail launch: the blocks do not matter
+                if t < 0 and b != blocks[0]:
+                    table[(b, t)] = table[(blocks[0], t)]  # no tail launch: the blocks do not matter
                     continue
                 kernel.set_tuning("tail_bounce", t)
                 table[(b, t)] = frame_ms()

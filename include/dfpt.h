@@ -235,8 +235,9 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *   "pixel_tiles"       1 (default) runs a plain pass's queue slots over 8 x 4 pixel tiles (a warp's
  *                       primary rays leave a compact block of pixels; width a multiple of 8, height
  *                       of 4, counter-based RNG, path tracer without wireframes), 0 in row order;
- *   "tail_bounce"       t >= 1: a plain pass runs bounces t .. depth-1 and the final any-hit of each
- *                       path in one launch (same steps per path); 0 (default) a launch per bounce;
+ *   "tail_bounce"       t >= 0: a plain pass runs bounces t .. depth-1 and the final any-hit of each
+ *                       path in one launch (same steps per path; t = 0 includes the camera rays'
+ *                       traversal and shading); -1 (default) a launch per bounce;
  *   "tail_blocks"       2 (default), 3 or 4: resident blocks of 256 threads per SM the tail launch
  *                       is compiled for (fewer registers per thread, more warps) when it walks with
  *                       the compact pair walk (configurations 16 and 17) in the fast kernel set; other

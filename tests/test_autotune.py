@@ -16,7 +16,7 @@ VALID = {
     "wide_samples": set(range(1, 65)),
     "ray_sort": {0, 1},
     "shadow_defer": {0, 1},
-    "tail_bounce": set(range(0, 33)),
+    "tail_bounce": set(range(-1, 33)),
     "tail_blocks": {2, 3, 4},
     "pass_shadow_sort": {0, 1},
     "pass_ray_sort": {0, 3, 6, 9, 12, 15},
@@ -84,7 +84,7 @@ def clock(monkeypatch):
     return c
 
 
-FRAME_DEFAULTS = {"trace_config": 17, "tail_bounce": 0, "tail_blocks": 2, "pass_shadow_sort": 1, "pass_ray_sort": 0}
+FRAME_DEFAULTS = {"trace_config": 17, "tail_bounce": -1, "tail_blocks": 2, "pass_shadow_sort": 1, "pass_ray_sort": 0}
 
 
 def frame_cost(best):
@@ -94,7 +94,7 @@ def frame_cost(best):
         c += 0.05 * abs(s["trace_config"] - best["trace_config"])
         c += 0.11 * abs(s["tail_bounce"] - best["tail_bounce"])
         # Without a tail launch the blocks do not matter.
-        if s["tail_bounce"] != 0:
+        if s["tail_bounce"] >= 0:
             c += 0.07 * abs(s["tail_blocks"] - best["tail_blocks"])
         c += 0.03 * (s["pass_shadow_sort"] != best["pass_shadow_sort"])
         c += 0.02 * abs(s["pass_ray_sort"] - best["pass_ray_sort"]) / 3
@@ -106,6 +106,8 @@ def frame_cost(best):
     {"trace_config": 16, "tail_bounce": 1, "tail_blocks": 4, "pass_shadow_sort": 1, "pass_ray_sort": 0},
     {"trace_config": 17, "tail_bounce": 2, "tail_blocks": 3, "pass_shadow_sort": 0, "pass_ray_sort": 0},
     {"trace_config": 17, "tail_bounce": 3, "tail_blocks": 2, "pass_shadow_sort": 0, "pass_ray_sort": 9},
+    {"trace_config": 16, "tail_bounce": 0, "tail_blocks": 3, "pass_shadow_sort": 0, "pass_ray_sort": 0},
+    {"trace_config": 16, "tail_bounce": -1, "tail_blocks": 2, "pass_shadow_sort": 1, "pass_ray_sort": 12},
 ])
 def test_tune_frame_picks_the_cheapest_structure(clock, best):
     k = FakeKernel(clock, frame_cost(best), FRAME_DEFAULTS)

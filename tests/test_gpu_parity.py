@@ -325,17 +325,17 @@ def test_pixel_tile_order_keeps_every_pixel(scenes):
 @pytest.mark.parametrize("name", ["spheres", "meshes"])
 def test_tail_launch_equals_per_bounce_launches(scenes, name):
     """The tail kernel (tail_bounce t: bounces t .. depth-1 and the final any-hit of each path in
-    one launch, compiled for 2, 3 or 4 resident blocks) takes every path through the same steps as a
-    launch per bounce: the same films (sun contributions are added with float atomics: a few ulps),
+    one launch, from the camera rays on with t = 0, compiled for 2, 3 or 4 resident blocks) takes
+    every path through the same steps as a launch per bounce (t = -1): the same films (sun contributions are added with float atomics: a few ulps),
     the same segments, nodes and triangles, the same selection buffer - with the deferred shadow
     rays binned by origin cell before their launch (pass_shadow_sort) or not, and with bounce 1's
     rays binned by direction and origin cell (pass_ray_sort, the grid's bits) or not."""
     scene, sky, params, (w, h) = scenes[name]
     params = dict(params, renderer_type=2, pt_ray_depth_maximum=6, pt_ray_depth_russian_roulette=3)
     ref = None
-    for tb, sort, rays, blocks in ((0, 0, 0, 2), (1, 0, 0, 2), (2, 0, 0, 2), (5, 0, 0, 2), (0, 1, 0, 2),
-                                   (2, 1, 0, 2), (1, 1, 0, 3), (2, 1, 0, 4), (0, 0, 9, 2), (1, 1, 12, 3),
-                                   (2, 1, 6, 2), (0, 1, 15, 2)):
+    for tb, sort, rays, blocks in ((-1, 0, 0, 2), (1, 0, 0, 2), (2, 0, 0, 2), (5, 0, 0, 2), (-1, 1, 0, 2),
+                                   (2, 1, 0, 2), (1, 1, 0, 3), (2, 1, 0, 4), (0, 0, 0, 2), (0, 1, 0, 4),
+                                   (-1, 0, 9, 2), (1, 1, 12, 3), (2, 1, 6, 2), (-1, 1, 15, 2)):
         k = _kernel(scene, sky, params, w, h, strict=False)
         k.set_tuning("wide_samples", 1)
         k.set_tuning("tail_blocks", blocks)
