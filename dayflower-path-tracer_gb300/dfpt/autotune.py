@@ -236,7 +236,9 @@ def tune_frame(kernel, frames: int = 16, candidates=(-1, 0, 1, 2, 3, 4), blocks=
     sort[other] = frame_ms()
     kernel.set_tuning("pass_shadow_sort", min(sort, key=sort.get))
     rays = {}
-    for bits in ray_sort:
+    # Bounce 1's rays are binned between bounce 0's shading and their traversal: not with a tail
+    # launch that starts at the camera rays.
+    for bits in ray_sort if best != 0 else (0,):
         kernel.set_tuning("pass_ray_sort", bits)
         rays[bits] = frame_ms()
         if verbose:
@@ -246,6 +248,9 @@ def tune_frame(kernel, frames: int = 16, candidates=(-1, 0, 1, 2, 3, 4), blocks=
     if bits:
         # The tail may start elsewhere once bounce 1's rays arrive in bin order.
         table, tb_blocks, best = sweep_tail()
+        if best == 0:
+            bits = 0
+            kernel.set_tuning("pass_ray_sort", 0)
     return {"trace_config": kernel.get_tuning("trace_config"),
             "config_ms_per_frame": {c: v[0] for c, v in per_config.items()},
             "tail_bounce": best, "tail_blocks": tb_blocks,

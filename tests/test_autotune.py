@@ -122,6 +122,9 @@ def test_tune_frame_picks_the_cheapest_structure(clock, best):
     assert set(out["config_ms_per_frame"]) == {16, 17}
     # The reported per-bounce times belong to the chosen blocks and configuration.
     assert min(out["ms_per_frame"], key=out["ms_per_frame"].get) == best["tail_bounce"]
+    if best["tail_bounce"] == 0:
+        # A tail from the camera rays leaves no bounce-1 queue to bin: the binning is not tried.
+        assert all(v == 0 for key, v in k.sets if key == "pass_ray_sort")
 
 
 def test_tune_frame_without_configs_keeps_the_handle_configuration(clock):
