@@ -18,7 +18,8 @@ tests/test_parity_statistic.py):
                   than 1% of the pixel channels with |z| > 4, |mean z| < 0.2 (or 4 standard
                   errors); over 8 x 8 pixel blocks for the scene with HDR emitters.
 Thin-lens depth of field and the fisheye lens (GPURendererKernel.java:643-704) are checked in the
-strict ray caster (hit ids bit-exact) and in bench mode.
+strict ray caster (hit ids bit-exact) and in bench mode. The interactive frame loop's mode (one
+pass per call through the tail launch) is checked on the scaled mesh scene the same way.
 """
 import numpy as np
 import pytest
@@ -31,22 +32,22 @@ BENCH_TUNING = {"wide_samples": 64, "ray_sort": 1, "shadow_defer": 1, "trace_con
 SEED_SAME, SEED_ORACLE = 0x5EED0001, 0x0AC1E002
 
 
-def _bench_kernel(scene, sky, params, w, h, seed, culling=0):
+def _bench_kernel(scene, sky, params, w, h, seed, culling=0, tuning=BENCH_TUNING):
     from dfpt.kernel import RendererKernel
 
     k = RendererKernel(scene, sky, params)
     k.update(w, h)
     k.set_strict(False)
-    for key, v in BENCH_TUNING.items():
+    for key, v in tuning.items():
         k.set_tuning(key, v)
     k.set_tuning("primitive_culling", culling)
     k.set_seed(seed)
     return k
 
 
-def _render(scene, sky, params, w, h, n, seed, culling=0):
-    k = _bench_kernel(scene, sky, params, w, h, seed, culling)
-    assert k.get_tuning("wide_samples") == 64 and k.get_tuning("trace_config") == 16
+def _render(scene, sky, params, w, h, n, seed, culling=0, tuning=BENCH_TUNING):
+    k = _bench_kernel(scene, sky, params, w, h, seed, culling, tuning)
+    assert all(k.get_tuning(key) == v for key, v in tuning.items())
     k.execute(n)
     film, samples = k.film()
     film, samples = film.copy(), samples.copy()
@@ -59,7 +60,7 @@ def _render(scene, sky, params, w, h, n, seed, culling=0):
     return film
 
 
-def _check(oracle_mod, scene, sky, params, w, h, n, cullings=(0,), mask=None, block=None, z_tail=0.01):
+def _check(oracle_mod, scene, sky, params, w, h, n, cullings=(0,), mask=None, block=None, z_tail=0.01, tuning=BENCH_TUNING):
     """`mask`: the pixels compared (all by default); the fisheye case leaves out the pixels whose
     jittered rays fall on both sides of the lens circle (their film restarts at each rejection,
     so their mean is not the plain mean of their samples). `block`: the converged statistics over
@@ -74,11 +75,11 @@ def _check(oracle_mod, scene, sky, params, w, h, n, cullings=(0,), mask=None, bl
     ref["half"] = full["half"]
     out = {}
     for c in cullings:
-        a_same = _render(scene, sky, params, w, h, n, SEED_ORACLE, c)
+        a_same = _render(scene, sky, params, w, h, n, SEED_ORACLE, c, tuning)
         rel = same_stream_rel_rmse(px(a_same), px(same["film"]))
         ratio = same_stream_mean_ratio(px(a_same), px(same["film"]))
         assert rel <= 0.01 and abs(ratio) <= 1e-3, (c, rel, ratio)
-        a = _render(scene, sky, params, w, h, n, SEED_SAME, c)
+        a = _render(scene, sky, params, w, h, n, SEED_SAME, c, tuning)
         s = film_stats(px(a), n, ref, 4 * n, block=None if block is None else (h, w, block))
         assert_converged(s, z_tail=z_tail)
         out[c] = (rel, s)
@@ -99,6 +100,21 @@ def test_mesh_scene_scaled_bench_mode(oracle_mod):
 
     scene, sky, params, (w, h) = synthetic.mesh_scene(width=192, height=108, frequency=30, grid=128)
     _check(oracle_mod, scene, sky, params, w, h, 128)
+
+
+# The interactive frame loop's mode: one pass per call (plain passes) in pixel-tile order, the tail
+# launch from bounce t compiled for b resident blocks, the deferred shadow rays binned by origin cell.
+FRAME_TUNING = {"wide_samples": 1, "trace_config": 16, "pixel_tiles": 1, "pass_shadow_sort": 1}
+
+
+@pytest.mark.parametrize("tail_bounce,tail_blocks", [(1, 4), (0, 3)])
+def test_mesh_scene_scaled_frame_mode(oracle_mod, tail_bounce, tail_blocks):
+    """The scaled mesh scene (as above) rendered pass by pass in the frame loop's configuration."""
+    from dfpt import synthetic
+
+    scene, sky, params, (w, h) = synthetic.mesh_scene(width=192, height=108, frequency=30, grid=128)
+    tuning = dict(FRAME_TUNING, tail_bounce=tail_bounce, tail_blocks=tail_blocks)
+    _check(oracle_mod, scene, sky, params, w, h, 128, tuning=tuning)
 
 
 def test_instances_scene_scaled_bench_mode(oracle_mod):
