@@ -465,6 +465,7 @@ struct dfpt_handle {
     int wide_samples = 8;
     bool pixel_tiles = true;   // plain passes in 8 x 4 pixel-tile slot order (DevParams::pixel_tiles)
     int tail_bounce = -1;      // plain passes: first bounce of the tail launch (-1: a launch per bounce)
+    int shadow_config = -1;    // traversal configuration of the sun shadow-ray launches (-1: trace_config's)
     // Plain passes: the deferred shadow rays binned by origin cell before their launch.
     bool pass_shadow_sort = true;
     DevBuf<int> p_sort_bins;                  // offsets, (unused), shadow counts, chunk sums
@@ -779,14 +780,16 @@ int issue_pass(dfpt_handle* h) {
         // The sun shadow rays of all bounces, traced together (binned by origin cell first when
         // pass_shadow_sort is on: shading and the tail counted the bins).
         if (h->sky.is_sun_active == 1) {
+            LaunchCtx cs = c;
+            if (h->shadow_config >= 0 && h->shadow_config < K.trace_configs) {
+                cs.trace_config = h->shadow_config;
+                cs.grid_trace = K.trace_grid(h->shadow_config, h->sms);
+            }
             if (h->pass.sort_count_shadow && K.sort_shadow) {
                 mark(h, KIND_SORT); k += K.sort_shadow(c, h->pass_shadow2);
-                LaunchCtx c2 = c;
-                c2.pass = &h->pass_shadow2;
-                mark(h, KIND_SHADOW); K.shadow(c2, 0); ++k;
-            } else {
-                mark(h, KIND_SHADOW); K.shadow(c, 0); ++k;
+                cs.pass = &h->pass_shadow2;
             }
+            mark(h, KIND_SHADOW); K.shadow(cs, 0); ++k;
         }
     }
     if (h->params.wireframes == 1) { mark(h, KIND_WIREFRAME); K.wireframe(c); ++k; }
@@ -918,6 +921,10 @@ int wide_prepare(dfpt_handle* h) {
     c.batch = &h->wq;
     h->wctx_shadow = c;
     h->wctx_shadow.pass = &h->wpass_shadow;
+    if (h->shadow_config >= 0 && h->shadow_config < h->wide.trace_configs) {
+        h->wctx_shadow.trace_config = h->shadow_config;
+        h->wctx_shadow.grid_trace = h->wide.trace_grid(h->shadow_config, h->sms);
+    }
     return DFPT_OK;
 }
 
@@ -936,11 +943,14 @@ int issue_wide_wave(dfpt_handle* h) {
     // with shadow_defer, all bounces' at once after the last bounce (queue of slots x depth).
     auto shadows = [&]() {
         if (h->sky.is_sun_active != 1) return;
+        // h->wctx_shadow: the shadow launches' configuration, reading the binned copy.
         if (h->wpass.sorted_queues && h->wpass.sort_count_shadow) {
             mark(h, KIND_SORT); k += K.b_sort_shadow(c, h->wpass_shadow);
             mark(h, KIND_SHADOW); K.b_shadow(h->wctx_shadow, 0); ++k;
         } else {
-            mark(h, KIND_SHADOW); K.b_shadow(c, 0); ++k;
+            LaunchCtx cs = h->wctx_shadow;
+            cs.pass = c.pass;
+            mark(h, KIND_SHADOW); K.b_shadow(cs, 0); ++k;
         }
         mark(h, KIND_END); K.b_shadow_reset(c, 0); ++k;
     };
@@ -1595,6 +1605,13 @@ int dfpt_set_tuning(dfpt_handle* h, const char* key, int32_t value) {
         h->wide_graph_valid = false;
         return DFPT_OK;
     }
+    if (std::strcmp(key, "shadow_config") == 0) {
+        if (value < -1 || value >= h->fast.trace_configs) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "shadow_config %d out of range", value);
+        h->shadow_config = value;
+        h->graph_valid = false;
+        h->wide_graph_valid = false;
+        return DFPT_OK;
+    }
     if (std::strcmp(key, "ray_sort") == 0) {
         h->ray_sort = value != 0;
         h->wide_graph_valid = false;
@@ -1685,6 +1702,7 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     if (!h || !key || !value) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (std::strcmp(key, "trace_config") == 0) { *value = h->ctx.trace_config; return DFPT_OK; }
     if (std::strcmp(key, "trace_configs") == 0) { *value = h->fast.trace_configs; return DFPT_OK; }
+    if (std::strcmp(key, "shadow_config") == 0) { *value = h->shadow_config; return DFPT_OK; }
     if (std::strcmp(key, "primitive_culling") == 0) { *value = h->sc.scene.use_culling; return DFPT_OK; }
     if (std::strcmp(key, "pair_stack") == 0) { *value = h->sc.scene.pair_stack; return DFPT_OK; }
     if (std::strcmp(key, "l2_persist") == 0) { *value = h->l2_window.num_bytes > 0 ? 1 : 0; return DFPT_OK; }

@@ -220,6 +220,8 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       blocks per SM, 0..N-1, N readable as "trace_configs"); every configuration
  *                       visits the same nodes in the same order (default 16: the compact pair
  *                       walk for closest hits, the autotuner's usual pick);
+ *   "shadow_config"     the configuration of the sun shadow-ray (any-hit) launches; -1 (default)
+ *                       the trace_config's (any hit is the same hit-or-miss in every walk order);
  *   "pair_stack"        stack entries of the compact pair walk (1..8, default 8); fewer entries
  *                       take its overflow path more often (same hits; a rejected node may then be
  *                       counted twice by the visit counters);

@@ -192,7 +192,8 @@ def test_trace_configs_agree(scenes):
     handle per configuration, so every run draws from pass 0 of the same stream). The compact pair
     walk also runs with 1- and 2-entry stacks, which drop stack entries on most walks: its hits
     stay exact, and its node counter may count a right child twice (the threaded continuation
-    re-tests one its parent's step rejected), never fewer."""
+    re-tests one its parent's step rejected), never fewer. The sun shadow rays walked in another
+    configuration than the closest hits (shadow_config) change nothing either."""
     scene, sky, params, (w, h) = scenes["meshes"]
     ref = None
     n = None
@@ -203,9 +204,11 @@ def test_trace_configs_agree(scenes):
         if cases is None:
             n = k.get_tuning("trace_configs")
             assert n > COMPACT_PAIR_CONFIG
-            cases = [(c, 8) for c in range(n)] + [(COMPACT_PAIR_CONFIG, 1), (COMPACT_PAIR_CONFIG, 2)]
+            cases = [(c, 8, -1) for c in range(n)] + [(COMPACT_PAIR_CONFIG, 1, -1), (COMPACT_PAIR_CONFIG, 2, -1)]
+            cases += [(COMPACT_PAIR_CONFIG, 8, 0), (COMPACT_PAIR_CONFIG, 8, 1), (0, 8, COMPACT_PAIR_CONFIG)]
         k.set_tuning("trace_config", cases[cfg][0])
         k.set_tuning("pair_stack", cases[cfg][1])
+        k.set_tuning("shadow_config", cases[cfg][2])
         k.set_counting(True)
         k.execute(1)
         film, _ = k.film()
@@ -232,15 +235,18 @@ def test_wide_passes_equal_pass_by_pass(scenes, name):
     film of n single passes: same samples per pixel, same Kahan order; float atomics of the sun
     contributions leave a few ulps (rtol 1e-5). A clear between calls restarts both the same way;
     the selection buffer and the image come from the last (normal) pass in both. The same holds
-    with the shadow rays of all bounces deferred to one launch."""
+    with the shadow rays of all bounces deferred to one launch, and with the shadow rays walked in
+    another traversal configuration (shadow_config: any hit is the same hit-or-miss)."""
     scene, sky, params, (w, h) = scenes[name]
     out = []
-    # (passes per wave, ray binning, deferred shadow rays)
-    for wide, sort, defer in ((1, 0, 0), (8, 1, 0), (8, 0, 0), (8, 1, 1), (8, 0, 1)):
+    # (passes per wave, ray binning, deferred shadow rays, shadow rays' traversal configuration)
+    for wide, sort, defer, scfg in ((1, 0, 0, -1), (8, 1, 0, -1), (8, 0, 0, -1), (8, 1, 1, -1), (8, 0, 1, -1),
+                                    (8, 1, 1, 0), (8, 0, 0, 1), (1, 0, 0, 11)):
         k = _kernel(scene, sky, dict(params, renderer_type=2), w, h)
         k.set_tuning("wide_samples", wide)
         k.set_tuning("ray_sort", sort)
         k.set_tuning("shadow_defer", defer)
+        k.set_tuning("shadow_config", scfg)
         k.execute(13)
         k.clear()
         k.execute(11)
