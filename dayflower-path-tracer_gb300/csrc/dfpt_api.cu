@@ -1718,6 +1718,125 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
     return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "unknown tuning key '%s'", key);
 }
 
+// ---- Native frame tuner --------------------------------------------------------------------
+// The launch structure of one-pass dfpt_render calls, picked by timing them (CUDA events on the
+// handle's stream): the traversal configuration (the handle's, 16, 17), the tail launch's first
+// bounce (-1 .. 4) and resident blocks (2 .. 4), then the shadow-ray binning on or off. The
+// buffers a pass writes that outlive it (film, image, selection buffer, per-pixel RNG states and
+// flags, primary-hit records, counters) and the pass counter are saved first and put back after,
+// so the call changes only the tuning.
+namespace {
+struct SavedRegion {
+    void* p;
+    size_t bytes;
+};
+#define DFPT_REGION_OF(b) SavedRegion{(void*)(b).p, (b).n * sizeof(*(b).p)}
+
+int tune_frame_sweep(dfpt_handle* h, int frames, float* best_ms) {
+    const int nb = bounces_of(h);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        (void)cudaGetLastError();
+        if (e0) cudaEventDestroy(e0);
+        return dfpt_fail(DFPT_ERR_CUDA, "cudaEventCreate failed");
+    }
+    auto frame_ms = [&](float& ms) -> int {
+        int r = dfpt_render(h, 1);  // untimed: builds the pass graph of this structure
+        if (!r && cudaEventRecord(e0, h->stream) != cudaSuccess) r = dfpt_fail(DFPT_ERR_CUDA, "cudaEventRecord failed");
+        for (int i = 0; !r && i < frames; ++i) r = dfpt_render(h, 1);
+        if (!r && cudaEventRecord(e1, h->stream) != cudaSuccess) r = dfpt_fail(DFPT_ERR_CUDA, "cudaEventRecord failed");
+        if (!r && cudaEventSynchronize(e1) != cudaSuccess) r = dfpt_fail(DFPT_ERR_CUDA, "frame timing failed");
+        if (!r && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = dfpt_fail(DFPT_ERR_CUDA, "cudaEventElapsedTime failed");
+        if (r) (void)cudaGetLastError();
+        ms /= (float)frames;
+        return r;
+    };
+    int configs[3] = {h->ctx.trace_config, 16, 17};
+    int best_cfg = h->ctx.trace_config, best_blocks = h->ctx.tail_blocks, best_tail = h->tail_bounce;
+    float best = 3.4e38f;
+    int r = DFPT_OK;
+    for (int ci = 0; ci < 3 && !r; ++ci) {
+        const int cfg = configs[ci];
+        if (cfg >= h->fast.trace_configs || (ci > 0 && cfg == configs[0]) || (ci == 2 && cfg == configs[1])) continue;
+        r = dfpt_set_tuning(h, "trace_config", cfg);
+        for (int blocks = 2; blocks <= 4 && !r; ++blocks) {
+            r = dfpt_set_tuning(h, "tail_blocks", blocks);
+            for (int tail = -1; tail <= 4 && tail < nb && !r; ++tail) {
+                if (tail < 0 && blocks != 2) continue;  // no tail launch: its blocks do not matter
+                r = dfpt_set_tuning(h, "tail_bounce", tail);
+                float ms = 0.0f;
+                if (!r) r = frame_ms(ms);
+                if (!r && ms < best) { best = ms; best_cfg = cfg; best_blocks = blocks; best_tail = tail; }
+            }
+        }
+    }
+    if (!r) r = dfpt_set_tuning(h, "trace_config", best_cfg);
+    if (!r) r = dfpt_set_tuning(h, "tail_blocks", best_blocks);
+    if (!r) r = dfpt_set_tuning(h, "tail_bounce", best_tail);
+    if (!r) {
+        const bool sort = h->pass_shadow_sort;
+        float ms = 0.0f;
+        r = dfpt_set_tuning(h, "pass_shadow_sort", sort ? 0 : 1);
+        if (!r) r = frame_ms(ms);
+        if (!r && ms < best) best = ms;
+        else if (!r) r = dfpt_set_tuning(h, "pass_shadow_sort", sort ? 1 : 0);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!r && best_ms) *best_ms = best;
+    return r;
+}
+}  // namespace
+
+int dfpt_tune_frame(dfpt_handle* h, int32_t frames, float* ms_per_frame) {
+    if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
+    if (frames < 1 || frames > 1024) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "frames %d outside [1, 1024]", frames);
+    if (h->diff_on) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "dfpt_tune_frame inside a differentiable forward (call dfpt_diff_end first)");
+    if (ms_per_frame) *ms_per_frame = 0.0f;
+    // The other renderers run one kernel per pass: nothing to choose.
+    if (is_simple_mode(h->params.renderer_type)) return DFPT_OK;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    SavedRegion regions[] = {DFPT_REGION_OF(h->film_sum), DFPT_REGION_OF(h->film_comp), DFPT_REGION_OF(h->film_n),
+                             DFPT_REGION_OF(h->bgra), DFPT_REGION_OF(h->primitive_offsets), DFPT_REGION_OF(h->pixel_flags),
+                             DFPT_REGION_OF(h->rng), DFPT_REGION_OF(h->stats), DFPT_REGION_OF(h->hit_prim),
+                             DFPT_REGION_OF(h->hit_type), DFPT_REGION_OF(h->hit_off), DFPT_REGION_OF(h->hit_dist),
+                             DFPT_REGION_OF(h->hit_normal)};
+    size_t total = 0;
+    for (const SavedRegion& g : regions) total += (g.bytes + 255) & ~(size_t)255;
+    DevBuf<uint8_t> saved;
+    CUDA_TRY(saved.alloc(total));
+    size_t at = 0;
+    cudaError_t ce = cudaSuccess;
+    for (const SavedRegion& g : regions) {
+        if (ce == cudaSuccess && g.bytes) ce = cudaMemcpyAsync(saved.p + at, g.p, g.bytes, cudaMemcpyDeviceToDevice, h->stream);
+        at += (g.bytes + 255) & ~(size_t)255;
+    }
+    if (ce != cudaSuccess) {
+        (void)cudaGetLastError();
+        saved.release();
+        return dfpt_fail(DFPT_ERR_CUDA, "saving the film before tuning: %s", cudaGetErrorString(ce));
+    }
+    const int host_pass0 = h->host_pass;
+    const int r = tune_frame_sweep(h, frames, ms_per_frame);
+    // Put back what the timed passes wrote, and the pass counter (the next pass reads it).
+    at = 0;
+    ce = cudaSuccess;
+    for (const SavedRegion& g : regions) {
+        if (ce == cudaSuccess && g.bytes) ce = cudaMemcpyAsync(g.p, saved.p + at, g.bytes, cudaMemcpyDeviceToDevice, h->stream);
+        at += (g.bytes + 255) & ~(size_t)255;
+    }
+    h->host_pass = host_pass0;
+    h->pass_index_host = host_pass0;
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(h->pass_index.p, &h->pass_index_host, sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+    saved.release();
+    if (ce != cudaSuccess) {
+        (void)cudaGetLastError();
+        return dfpt_fail(DFPT_ERR_CUDA, "restoring the film after tuning: %s", cudaGetErrorString(ce));
+    }
+    return r;
+}
+
 int dfpt_set_record_hits(dfpt_handle* h, int32_t enabled) {
     if (!h) return dfpt_fail(DFPT_ERR_INVALID_ARGUMENT, "handle == NULL");
     h->record_hits = enabled != 0;

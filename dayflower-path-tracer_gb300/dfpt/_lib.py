@@ -126,6 +126,7 @@ SIGNATURES = {
     "dfpt_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
     "dfpt_set_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
     "dfpt_get_tuning": (C.c_int, [C.c_void_p, C.c_char_p, i32p]),
+    "dfpt_tune_frame": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "dfpt_l2_reset": (C.c_int, []),
     "dfpt_probe_read_bandwidth": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, f64p]),
     "dfpt_read_profile": (C.c_int, [C.c_void_p, f64p, i32p]),

@@ -180,6 +180,14 @@ class RendererKernel:
         check(self._lib.dfpt_get_tuning(self._need(), key.encode(), C.byref(v)))
         return int(v.value)
 
+    def tune_frame_native(self, frames: int = 16) -> float:
+        """dfpt_tune_frame: the C-ABI's own frame tuner (for hosts without Python); returns the
+        chosen structure's device milliseconds per one-pass frame. Leaves the film and the random
+        streams as they were."""
+        ms = C.c_float()
+        check(self._lib.dfpt_tune_frame(self._need(), int(frames), C.byref(ms)))
+        return float(ms.value)
+
     def launch_count(self) -> int:
         c = C.c_uint64()
         check(self._lib.dfpt_launch_count(self._need(), C.byref(c)))

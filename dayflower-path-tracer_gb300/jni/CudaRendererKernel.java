@@ -244,6 +244,10 @@ public final class CudaRendererKernel extends AbstractRendererKernel {
 		this.handle = nativeCreate(c.getPoint2Fs(), c.getPoint3Fs(), c.getVector3Fs(), c.getPlanes(), c.getSpheres(), c.getTerrains(), c.getTriangles(), c.getBoundingVolumeHierarchies(), c.getTextures(), c.getSurfaces(), c.getPrimitives(), c.getPrimitivesObjectToWorld(), c.getPrimitivesWorldToObject(), c.getCamera(), skyDoubles(sky), skyFloats(sky), this.skyFlags, resolutionX, resolutionY, System.nanoTime());
 
 		pushParams();
+
+//		The launch structure of execute()'s one-pass renders, picked once for this scene and size; the
+//		film and the random streams stay as they were.
+		nativeTuneFrame(this.handle, 8);
 	}
 
 	/* GPURendererKernel.java:455-461: the camera writes its 19 floats into the compiled scene's array. */
@@ -395,6 +399,8 @@ public final class CudaRendererKernel extends AbstractRendererKernel {
 	private static native void nativeClear(long handle);
 
 	private static native void nativeRender(long handle, int passes);
+
+	private static native void nativeTuneFrame(long handle, int frames);
 
 	private static native void nativeReadBgra8(long handle, byte[] bgra);
 

@@ -232,6 +232,14 @@ JNIEXPORT void JNICALL Java_org_dayflower_pathtracer_kernel_CudaRendererKernel_n
     throw_if(env, dfpt_render(kernel_of(h)->handle, passes));
 }
 
+/* The frame loop's launch structure for this kernel's scene and size (dfpt_tune_frame); the film,
+ * image and random streams are left as they were. */
+JNIEXPORT void JNICALL Java_org_dayflower_pathtracer_kernel_CudaRendererKernel_nativeTuneFrame(JNIEnv* env, jclass cls, jlong h, jint frames) {
+    (void)cls;
+    if (!need_handle(env, h)) return;
+    throw_if(env, dfpt_tune_frame(kernel_of(h)->handle, frames, NULL));
+}
+
 /* The array must hold width x height x 4 bytes of the size given to nativeCreate. */
 JNIEXPORT void JNICALL Java_org_dayflower_pathtracer_kernel_CudaRendererKernel_nativeReadBgra8(JNIEnv* env, jclass cls, jlong h, jbyteArray out) {
     (void)cls;

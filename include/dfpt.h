@@ -259,6 +259,18 @@ int dfpt_read_profile(dfpt_handle* handle, double* ms_by_kind10, int32_t* launch
  *                       shadow queue holds depth x as many rays). */
 int dfpt_set_tuning(dfpt_handle* handle, const char* key, int32_t value);
 int dfpt_get_tuning(dfpt_handle* handle, const char* key, int32_t* value);
+
+/* Picks the launch structure of one-pass dfpt_render calls - the interactive frame loop of
+ * DayflowerApplication (execute() + get() per frame) - for this handle's scene, size and knobs:
+ * times `frames` (1..1024) one-pass renders per candidate with CUDA events on the handle's stream
+ * and sets the fastest "trace_config" (the handle's, 16 or 17), "tail_bounce" (-1..4),
+ * "tail_blocks" (2..4) and "pass_shadow_sort". It renders about 40 x (frames + 1) passes, then puts
+ * back the film, image, selection buffer, per-pixel random states, primary-hit records, counters
+ * and pass counter as they were: only the tuning changes. `ms_per_frame` (may be NULL) receives
+ * the chosen structure's device time per frame (0 for the renderers with one kernel per pass,
+ * which have nothing to tune). Not during a differentiable forward. Allocates a temporary copy
+ * of those buffers (about 80 bytes per pixel). */
+int dfpt_tune_frame(dfpt_handle* handle, int32_t frames, float* ms_per_frame);
 /* Measurement hook (no reference counterpart): returns every persisting L2 line of this process
  * to normal, as a benchmark's L2 flush between timed steps must. */
 int dfpt_l2_reset(void);

@@ -328,6 +328,38 @@ def test_pixel_tile_order_keeps_every_pixel(scenes):
     assert np.array_equal(p0, p1)
 
 
+@pytest.mark.parametrize("rng_kind,hits", [(0, False), (1, True)])
+def test_native_frame_tuner_leaves_film_and_streams(scenes, rng_kind, hits):
+    """dfpt_tune_frame renders one-pass frames with every candidate launch structure, then puts back
+    the film, image, selection buffer, per-pixel random states (the LCG's too), primary-hit records
+    and pass counter: a handle that tuned between two renders ends with the film, selection buffer
+    and hit records of a handle that never tuned (films within the ulps of float atomics), and the
+    tunings it leaves are values the C-ABI accepts."""
+    scene, sky, params, (w, h) = scenes["meshes"]
+    params = dict(params, renderer_type=2, pt_ray_depth_maximum=6, pt_ray_depth_russian_roulette=3, rng_kind=rng_kind)
+    out = []
+    for tune in (False, True):
+        k = _kernel(scene, sky, params, w, h, strict=False, hits=hits)
+        cfg0 = k.get_tuning("trace_config")
+        k.execute(3)
+        if tune:
+            ms = k.tune_frame_native(2)
+            assert ms > 0
+            assert k.get_tuning("trace_config") in (cfg0, 16, 17)
+            assert -1 <= k.get_tuning("tail_bounce") <= 4 and k.get_tuning("tail_blocks") in (2, 3, 4)
+            assert k.get_tuning("pass_shadow_sort") in (0, 1)
+        k.execute(2)
+        film, n = k.film()
+        out.append((film.copy(), n.copy(), k.primitive_offsets().copy(), [a.copy() for a in k.hits()] if hits else []))
+        k.dispose()
+    (fa, na, pa, ha), (fb, nb, pb, hb) = out
+    assert (na == 5).all() and np.array_equal(na, nb)
+    np.testing.assert_allclose(fb, fa, rtol=1e-5, atol=1e-6)
+    assert np.array_equal(pa, pb)
+    for x, y in zip(ha, hb):
+        assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("name", ["spheres", "meshes"])
 def test_tail_launch_equals_per_bounce_launches(scenes, name):
     """The tail kernel (tail_bounce t: bounces t .. depth-1 and the final any-hit of each path in

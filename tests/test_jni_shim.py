@@ -4,8 +4,9 @@ stand-in jni.h and driven through a fake JNIEnv (tests/jni/): no JDK exists on e
 CPU: the shim compiles with warnings as errors, exports one function per native method of
 CudaRendererKernel.java with the matching parameter count, and turns every failure of the core
 into the Java exception the reference would throw, holding no critical section across other JNI
-calls. GPU: a kernel created and driven through the shim renders the same image and selection
-buffer as the ctypes binding with the same seed and knobs, across a sun toggle and a clear.
+calls. GPU: a kernel created and driven through the shim (its frame tuner included) renders the
+same image and selection buffer as the ctypes binding with the same seed and knobs, across a sun
+toggle and a clear.
 """
 import ctypes as C
 
@@ -94,6 +95,9 @@ def test_shim_renders_what_the_c_abi_renders(shim):
     assert handle != 0, shim.exception()
     ints, floats = _jni.param_arrays(ref.params)
     shim.nativeSetParams(handle, shim.array(ints), shim.array(floats))
+    assert shim.exception() is None
+    # CudaRendererKernel.update() ends with the frame tuner, which leaves film and streams as they were.
+    shim.nativeTuneFrame(handle, 2)
     assert shim.exception() is None
 
     def frame_pair(frames):
