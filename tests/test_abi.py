@@ -126,3 +126,13 @@ def test_read_probe_rejects_bad_arguments_without_device(lib):
     assert lib.dfpt_probe_read_bandwidth(C.c_void_p(aligned), 4096, 1, None, C.byref(g)) == -1  # under 1 MiB
     assert lib.dfpt_probe_read_bandwidth(C.c_void_p(aligned), (1 << 20) + 8, 1, None, C.byref(g)) == -1  # not a multiple of 16
     assert lib.dfpt_probe_read_bandwidth(C.c_void_p(aligned), 1 << 20, 0, None, C.byref(g)) == -1
+
+
+def test_handle_entry_points_reject_a_null_handle_without_device(lib):
+    """The tuning entry points check their arguments before any device work."""
+    ms = C.c_float(-1.0)
+    v = C.c_int32()
+    assert lib.dfpt_tune_frame(None, 4, C.byref(ms)) == -1
+    assert lib.dfpt_set_tuning(None, b"tail_bounce", 0) == -1
+    assert lib.dfpt_get_tuning(None, b"tail_bounce", C.byref(v)) == -1
+    assert b"NULL" in lib.dfpt_last_error() or b"handle" in lib.dfpt_last_error()
