@@ -549,10 +549,12 @@ def frame_kernels(k, frames=8):
     return {kk: round(v, 4) for kk, v in tot.items() if v > 0}
 
 
-# ncu figures of the closest-hit traversal kernel on mesh_scene (960x540, 4-pass waves, pixel-major
-# slots, configuration 16; one --set full capture): active lanes per issued instruction at bounces
-# 0 and 1, and the fraction of cycles with an instruction issued.
-TRACE_NCU = {"lanes_per_instruction": {"bounce0": 16.1, "bounce1": 9.1}, "issue_active": [0.64, 0.73]}
+# ncu figures of the closest-hit traversal kernel on mesh_scene (960x540, a 16-pass wave, pixel-major
+# slots, configuration 17; one --set full capture of the timed step's bounces 0 and 1): active lanes
+# per issued instruction, the fraction of cycles with an instruction issued, and warps active (of
+# the SM's maximum; the register limit allows 0.625).
+TRACE_NCU = {"config": 17, "lanes_per_instruction": {"bounce0": 17.5, "bounce1": 9.4}, "issue_active": [0.756, 0.710],
+             "warps_active": [0.618, 0.578]}
 
 
 def main():
