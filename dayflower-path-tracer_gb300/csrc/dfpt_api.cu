@@ -438,7 +438,7 @@ struct dfpt_handle {
     int shadow_config = -1;    // traversal configuration of the sun shadow-ray launches (-1: trace_config's)
     // Plain passes: the deferred shadow rays binned by origin cell before their launch.
     bool pass_shadow_sort = true;
-    DevBuf<int> p_sort_bins;                  // offsets, (unused), shadow counts, chunk sums
+    DevBuf<int> p_sort_bins;                  // offsets, bounce-1 ray counts, shadow counts, chunk sums
     DevBuf<float4> p_s2_o, p_s2_d, p_s2_c;    // the binned copy of the shadow queue
     size_t p_s2_capacity = 0;
     DevPass pass_shadow2{};                   // `pass` reading the binned copy

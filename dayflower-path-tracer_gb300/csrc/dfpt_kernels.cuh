@@ -2205,6 +2205,8 @@ static void launch_film(const LaunchCtx& c) { k_film<<<c.grid, 256, 0, c.stream>
 static void launch_end_pass(const LaunchCtx& c) { k_end_pass<<<1, 32, 0, c.stream>>>(*c.pass); }
 // Bins a plain pass's deferred shadow rays into `to` (a pass record whose s_* point at the second
 // set); shading counted the bins. Returns the kernels launched.
+static_assert(DFPT_SHADOW_CELL_BITS >= 10 && (1 << DFPT_SHADOW_CELL_BITS) <= DFPT_SORT_BINS,
+              "the plain shadow scan covers whole chunks of 1024 bins within the bin array");
 static int launch_sort_shadow(const LaunchCtx& c, const DevPass& to) {
     launch_sort_scan(c, c.pass->sort_count_shadow, (1 << DFPT_SHADOW_CELL_BITS) / 1024);
     k_sort_shadow_scatter_plain<<<c.grid, 256, 0, c.stream>>>(*c.scene, *c.pass, to.s_o, to.s_d, to.s_c);
