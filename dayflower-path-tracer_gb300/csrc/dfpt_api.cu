@@ -1690,8 +1690,9 @@ int dfpt_get_tuning(dfpt_handle* h, const char* key, int32_t* value) {
 
 // ---- Native frame tuner --------------------------------------------------------------------
 // The launch structure of one-pass dfpt_render calls, picked by timing them (CUDA events on the
-// handle's stream): the traversal configuration (the handle's, 16, 17), the tail launch's first
-// bounce (-1 .. 4) and resident blocks (2 .. 4), then the shadow-ray binning on or off. The
+// handle's stream): the primitive culling mode (scenes with enough bounded primitives), the
+// traversal configuration (the handle's, 16, 17), the tail launch's first bounce (-1 .. 4) and
+// resident blocks (2 .. 4), then the shadow-ray binning on or off. The
 // buffers a pass writes that outlive it (film, image, selection buffer, per-pixel RNG states and
 // flags, primary-hit records, counters) and the pass counter are saved first and put back after,
 // so the call changes only the tuning.
@@ -1721,10 +1722,29 @@ int tune_frame_sweep(dfpt_handle* h, int frames, float* best_ms) {
         ms /= (float)frames;
         return r;
     };
+    int r = DFPT_OK;
+    // Primitive culling first, where the scene has enough bounded primitives for it (the setter
+    // keeps 0 otherwise); every mode gives the same hits.
+    {
+        const int cull0 = h->sc.scene.use_culling;
+        r = dfpt_set_tuning(h, "primitive_culling", 1);
+        if (!r && h->sc.scene.use_culling == 1) {
+            float best_ms = 3.4e38f;
+            int best_mode = cull0;
+            for (int mode = 0; mode <= 2 && !r; ++mode) {
+                float ms = 0.0f;
+                r = dfpt_set_tuning(h, "primitive_culling", mode);
+                if (!r) r = frame_ms(ms);
+                if (!r && ms < best_ms) { best_ms = ms; best_mode = mode; }
+            }
+            if (!r) r = dfpt_set_tuning(h, "primitive_culling", best_mode);
+        } else if (!r) {
+            r = dfpt_set_tuning(h, "primitive_culling", cull0);
+        }
+    }
     int configs[3] = {h->ctx.trace_config, 16, 17};
     int best_cfg = h->ctx.trace_config, best_blocks = h->ctx.tail_blocks, best_tail = h->tail_bounce;
     float best = 3.4e38f;
-    int r = DFPT_OK;
     for (int ci = 0; ci < 3 && !r; ++ci) {
         const int cfg = configs[ci];
         if (cfg >= h->fast.trace_configs || (ci > 0 && cfg == configs[0]) || (ci == 2 && cfg == configs[1])) continue;

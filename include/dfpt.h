@@ -263,8 +263,9 @@ int dfpt_get_tuning(dfpt_handle* handle, const char* key, int32_t* value);
 /* Picks the launch structure of one-pass dfpt_render calls - the interactive frame loop of
  * DayflowerApplication (execute() + get() per frame) - for this handle's scene, size and knobs:
  * times `frames` (1..1024) one-pass renders per candidate with CUDA events on the handle's stream
- * and sets the fastest "trace_config" (the handle's, 16 or 17), "tail_bounce" (-1..4),
- * "tail_blocks" (2..4) and "pass_shadow_sort". It renders about 40 x (frames + 1) passes, then puts
+ * and sets the fastest "primitive_culling" (0..2, scenes with enough bounded primitives),
+ * "trace_config" (the handle's, 16 or 17), "tail_bounce" (-1..4), "tail_blocks" (2..4) and
+ * "pass_shadow_sort". It renders about 45 x (frames + 1) passes, then puts
  * back the film, image, selection buffer, per-pixel random states, primary-hit records, counters
  * and pass counter as they were: only the tuning changes. `ms_per_frame` (may be NULL) receives
  * the chosen structure's device time per frame (0 for the renderers with one kernel per pass,

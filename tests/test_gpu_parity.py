@@ -360,6 +360,30 @@ def test_native_frame_tuner_leaves_film_and_streams(scenes, rng_kind, hits):
         assert np.array_equal(x, y)
 
 
+def test_native_frame_tuner_picks_culling_with_the_same_film():
+    """On a scene with many bounded primitives (64 spheres on a plane) the C-ABI frame tuner also
+    times the primitive culling modes; whichever it keeps, renders after it equal a handle that never
+    tuned (every culling mode gives the same hits)."""
+    from dfpt import synthetic
+
+    scene, sky, params, (w, h) = synthetic.spheres_on_plane(width=64, height=48, count=64)
+    out = []
+    for tune in (False, True):
+        k = _kernel(scene, sky, dict(params), w, h, strict=False)
+        k.execute(2)
+        if tune:
+            assert k.tune_frame_native(2) > 0
+            assert k.get_tuning("primitive_culling") in (0, 1, 2)
+        k.execute(2)
+        film, n = k.film()
+        out.append((film.copy(), n.copy(), k.primitive_offsets().copy()))
+        k.dispose()
+    (fa, na, pa), (fb, nb, pb) = out
+    assert np.array_equal(na, nb) and (na == 4).all()
+    np.testing.assert_allclose(fb, fa, rtol=1e-5, atol=1e-6)
+    assert np.array_equal(pa, pb)
+
+
 @pytest.mark.parametrize("name", ["spheres", "meshes"])
 def test_tail_launch_equals_per_bounce_launches(scenes, name):
     """The tail kernel (tail_bounce t: bounces t .. depth-1 and the final any-hit of each path in
