@@ -179,8 +179,10 @@ def tune_wide(kernel, passes: int = 16, candidates=(1, 4, 8, 16, 32, 64), verbos
 
 
 def tune_frame(kernel, frames: int = 16, candidates=(-1, 0, 1, 2, 3, 4), blocks=(2, 3, 4), ray_sort=(0, 9, 12, 15),
-               configs=None, verbose: bool = False) -> dict:
-    """Picks the launch structure of one-pass calls (the interactive frame loop): times `frames`
+               configs=None, culling: bool = False, verbose: bool = False) -> dict:
+    """Picks the launch structure of one-pass calls (the interactive frame loop), as dfpt_tune_frame
+    does in the C-ABI: with `culling`, first the primitive culling mode (scenes with enough bounded
+    primitives; every mode gives the same hits); then times `frames`
     calls of dfpt_render(1) per `tail_bounce` candidate (-1 = a launch per bounce) and per
     `tail_blocks` (resident blocks of the tail kernel) - for each traversal configuration in
     `configs` when given (the primary rays', shadow rays' and tail's walk), else the handle's - and
@@ -216,6 +218,17 @@ def tune_frame(kernel, frames: int = 16, candidates=(-1, 0, 1, 2, 3, 4), blocks=
         kernel.set_tuning("tail_bounce", t)
         return table, b, t
 
+    cull = {}
+    if culling:
+        mode0 = kernel.get_tuning("primitive_culling")
+        kernel.set_tuning("primitive_culling", 1)
+        if kernel.get_tuning("primitive_culling") == 1:
+            for mode in (0, 1, 2):
+                kernel.set_tuning("primitive_culling", mode)
+                cull[mode] = frame_ms()
+            kernel.set_tuning("primitive_culling", min(cull, key=cull.get))
+        else:
+            kernel.set_tuning("primitive_culling", mode0)
     if configs:
         per_config = {}
         for cfg in configs:
@@ -251,7 +264,8 @@ def tune_frame(kernel, frames: int = 16, candidates=(-1, 0, 1, 2, 3, 4), blocks=
         if best == 0:
             bits = 0
             kernel.set_tuning("pass_ray_sort", 0)
-    return {"trace_config": kernel.get_tuning("trace_config"),
+    return {"primitive_culling": kernel.get_tuning("primitive_culling") if culling else None, "culling_ms_per_frame": cull,
+            "trace_config": kernel.get_tuning("trace_config"),
             "config_ms_per_frame": {c: v[0] for c, v in per_config.items()},
             "tail_bounce": best, "tail_blocks": tb_blocks,
             "ms_per_frame": {t: table[(tb_blocks, t)] for t in candidates},

@@ -127,6 +127,20 @@ def test_tune_frame_picks_the_cheapest_structure(clock, best):
         assert all(v == 0 for key, v in k.sets if key == "pass_ray_sort")
 
 
+def test_tune_frame_picks_the_culling_mode_first(clock):
+    best = {"trace_config": 17, "tail_bounce": 1, "tail_blocks": 4, "pass_shadow_sort": 1, "pass_ray_sort": 0}
+    base = frame_cost(best)
+
+    def cost(s):
+        return base(s) + 1e-3 * abs(s["primitive_culling"] - 2)
+
+    k = FakeKernel(clock, cost, dict(FRAME_DEFAULTS, primitive_culling=0))
+    out = autotune.tune_frame(k, culling=True)
+    assert k.state["primitive_culling"] == 2 and out["primitive_culling"] == 2
+    assert set(out["culling_ms_per_frame"]) == {0, 1, 2}
+    assert (out["tail_bounce"], out["tail_blocks"]) == (1, 4)
+
+
 def test_tune_frame_without_configs_keeps_the_handle_configuration(clock):
     best = {"trace_config": 16, "tail_bounce": 1, "tail_blocks": 4, "pass_shadow_sort": 1, "pass_ray_sort": 0}
     k = FakeKernel(clock, frame_cost(best), FRAME_DEFAULTS)
