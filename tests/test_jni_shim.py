@@ -74,6 +74,8 @@ def test_bad_sky_arrays_throw_before_any_device_work(shim):
 def test_calls_without_a_kernel_throw_illegal_state_exception(shim):
     shim.nativeRender(0, 1)
     assert shim.exception()[0] == "java/lang/IllegalStateException"
+    shim.nativeTuneFrame(0, 8)
+    assert shim.exception()[0] == "java/lang/IllegalStateException"
     img = np.zeros(16, np.uint8)
     shim.nativeReadBgra8(0, shim.array(img))
     assert shim.exception()[0] == "java/lang/IllegalStateException"
